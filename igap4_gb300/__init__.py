@@ -1,0 +1,310 @@
+"""igap4_gb300 -- GB300-native element assembly and Newton-Krylov for IGAP4.
+
+Python access to ``libigapgpu.so`` through its C ABI (``include/igapgpu.h``).
+Arrays may be numpy arrays (host) or CUDA tensors (anything exposing
+``data_ptr()``); the library detects device pointers itself.  There is no CPU
+fallback: constructing an :class:`Assembly` without the built library or
+without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libigapgpu.so")
+
+LAW_GRADELAST, LAW_GRADELASTTIME, LAW_LINGRAD = 0, 1, 2
+PREC_FP64, PREC_SPLIT = 0, 1
+LAW_TORDER = {LAW_GRADELAST: 0, LAW_GRADELASTTIME: 2, LAW_LINGRAD: 0}
+# default parameters of the reference plugins (phys/physgradelast.c:21,
+# phys/physgradelasttime.c:21) and of the linear law
+LAW_DEFAULT_PAR = {
+    LAW_GRADELAST: [0.25, 0.50, 360., 180., 0.05, 1.0, 1.0, 1.e-3 * 0.5, 0.0],
+    LAW_GRADELASTTIME: [0.25, 0.50, 500., 250., 0.025, 1.0, 1.0, 1.e-3 * 0.5, 0.0],
+    LAW_LINGRAD: [1.0, 1.0, 0.1, 0, 0, 0, 0, 0, 0],
+}
+
+
+class IgapGpuError(RuntimeError):
+    pass
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("porder", ctypes.c_int), ("nelem", ctypes.c_int * 3),
+                ("knots", ctypes.POINTER(ctypes.c_double) * 3),
+                ("w", ctypes.POINTER(ctypes.c_double)), ("X", ctypes.POINTER(ctypes.c_double))]
+
+
+class PhysDesc(ctypes.Structure):
+    _fields_ = [("law", ctypes.c_int), ("par", ctypes.c_double * 9)]
+
+
+class BCDesc(ctypes.Structure):
+    _fields_ = [("bc_type", ctypes.c_int * 36), ("par_periodic", ctypes.c_double * 9),
+                ("par_dirichlet", ctypes.c_double * 9), ("neumann", ctypes.c_double * 36)]
+
+
+class SolverOpts(ctypes.Structure):
+    _fields_ = [("snes_abstol", ctypes.c_double), ("snes_rtol", ctypes.c_double),
+                ("snes_stol", ctypes.c_double), ("snes_max_it", ctypes.c_int),
+                ("linesearch", ctypes.c_int), ("ksp_restart", ctypes.c_int),
+                ("ksp_rtol", ctypes.c_double), ("ksp_abstol", ctypes.c_double),
+                ("ksp_dtol", ctypes.c_double), ("ksp_max_it", ctypes.c_int), ("pc", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("newton_its", ctypes.c_int), ("ksp_its_total", ctypes.c_int),
+                ("ksp_its_last", ctypes.c_int), ("converged", ctypes.c_int),
+                ("reason", ctypes.c_int), ("fnorm0", ctypes.c_double), ("fnorm", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libigapgpu.so (build it with ``python -m igap4_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise IgapGpuError(f"{LIBPATH} is missing: the CUDA extension must be built "
+                               "(python -m igap4_gb300.build); there is no CPU fallback")
+        L = ctypes.CDLL(LIBPATH)
+        vp = ctypes.c_void_p
+        L.igapgpu_assm_init.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(MeshDesc),
+                                        ctypes.POINTER(PhysDesc), ctypes.POINTER(BCDesc), ctypes.c_int]
+        L.igapgpu_finalize.argtypes = [vp]
+        L.igapgpu_sizes.argtypes = [vp] + [ctypes.c_void_p] * 4
+        L.igapgpu_pattern.argtypes = [vp, vp, vp]
+        for f in ("igapgpu_set_history", "igapgpu_get_history"):
+            getattr(L, f).argtypes = [vp, ctypes.c_int, vp]
+        L.igapgpu_shift_history.argtypes = [vp]
+        for f in ("igapgpu_residual", "igapgpu_tangent", "igapgpu_matmult", "igapgpu_get_diagonal"):
+            getattr(L, f).argtypes = [vp, vp, vp]
+        L.igapgpu_get_diagonal.argtypes = [vp, vp]
+        L.igapgpu_assemble.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_ksp_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverOpts),
+                                        ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+        L.igapgpu_solve.argtypes = [vp, vp, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolveStats)]
+        L.igapgpu_default_solver_opts.argtypes = [ctypes.POINTER(SolverOpts)]
+        L.igapgpu_default_solver_opts.restype = None
+        L.igapgpu_set_precision.argtypes = [vp, ctypes.c_int]
+        L.igapgpu_set_stream.argtypes = [vp, vp]
+        L.igapgpu_synchronize.argtypes = [vp]
+        L.igapgpu_last_error.restype = ctypes.c_char_p
+        L.igapgpu_launch_count.restype = ctypes.c_int64
+        L.igapgpu_profile.argtypes = [vp, ctypes.c_int]
+        L.igapgpu_profile_read.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_measure_fp64_peak.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise IgapGpuError(f"igapgpu error {rc}: {lib().igapgpu_last_error().decode()}")
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array or a CUDA tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise IgapGpuError("tensor must be contiguous")
+        return ctypes.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise IgapGpuError("array must be C-contiguous")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def beam_mesh(nelem, L=(1.0, 1.0, 1.0), porder=2, perturb=False):
+    """Knot vectors, weights and control points of a box beam with a
+    per-direction element count (the formulas of mesh/igabeam.c:34-72 and, with
+    perturb, mesh/igabeamtest.c:68-70)."""
+    knots = []
+    for d in range(3):
+        n = nelem[d]
+        kv = np.empty(n + 1 + 2 * porder)
+        l = 1.0 / n
+        for k in range(len(kv)):
+            kv[k] = 0.0 if k <= porder else ((k - porder) * l if k < n + porder else 1.0)
+        knots.append(kv)
+    nb = [n + porder for n in nelem]
+    i, j, k = np.meshgrid(np.arange(nb[0]), np.arange(nb[1]), np.arange(nb[2]), indexing="ij")
+    X = np.empty(nb + [3])
+    X[..., 0] = (i - 0.5) / (nb[0] - 2) * L[0]
+    X[..., 1] = (j - 0.5) / (nb[1] - 2) * L[1]
+    X[..., 2] = (k - 0.5) / (nb[2] - 2) * L[2]
+    if perturb:
+        inside = ((i > 2) & (j > 2) & (k > 2) & (i < nb[0] - 2) & (j < nb[1] - 2) & (k < nb[2] - 2)).astype(float)
+        ijk = i * k * j
+        X[..., 0] += 0.2 * L[0] / nb[0] * inside * np.sin(3 * ijk)
+        X[..., 1] += 0.2 * L[1] / nb[1] * inside * np.sin(5 * ijk)
+        X[..., 2] += 0.2 * L[2] / nb[2] * inside * np.sin(7 * ijk)
+    w = np.ones(nb[0] * nb[1] * nb[2])
+    return knots, w, np.ascontiguousarray(X.reshape(-1))
+
+
+def clamp_bc(faces=(0,), traction_face=None, traction=(0.0, 0.0, 0.0)):
+    """bc_type / traction tables: listed faces clamped (both orders), others
+    traction-free; optional constant traction on one face."""
+    bct = np.ones(36, np.int32)
+    neu = np.zeros(36)
+    for f in faces:
+        bct[6 * f:6 * f + 6] = 0
+    if traction_face is not None:
+        for d in range(3):
+            neu[6 * traction_face + d] = traction[d]
+    return bct, neu
+
+
+class Assembly:
+    """One GPU assembly context (IGAPAssmInit + the Residual/Tangent callbacks)."""
+
+    def __init__(self, nelem, knots, w, X, law=LAW_GRADELAST, par=None, bc_type=None,
+                 neumann=None, par_dirichlet=None, nquad=4, porder=2):
+        L = lib()
+        self._keep = [np.ascontiguousarray(k, np.float64) for k in knots]
+        self._keep += [np.ascontiguousarray(w, np.float64), np.ascontiguousarray(X, np.float64)]
+        md = MeshDesc()
+        md.porder = porder
+        for d in range(3):
+            md.nelem[d] = int(nelem[d])
+            md.knots[d] = self._keep[d].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        md.w = self._keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        md.X = self._keep[4].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        pd = PhysDesc()
+        pd.law = law
+        p = LAW_DEFAULT_PAR.get(law, [0.0] * 9) if par is None else list(par)
+        for i in range(9):
+            pd.par[i] = float(p[i]) if i < len(p) else 0.0
+        bd = BCDesc()
+        for i in range(36):
+            bd.bc_type[i] = 1 if bc_type is None else int(bc_type[i])
+            bd.neumann[i] = 0.0 if neumann is None else float(neumann[i])
+        for i in range(9):
+            bd.par_dirichlet[i] = 0.0 if par_dirichlet is None else float(par_dirichlet[i])
+        h = ctypes.c_void_p()
+        _check(L.igapgpu_assm_init(ctypes.byref(h), ctypes.byref(md), ctypes.byref(pd),
+                                   ctypes.byref(bd), nquad))
+        self.h = h
+        nd, nz, el = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        to = ctypes.c_int()
+        _check(L.igapgpu_sizes(h, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(to), ctypes.byref(el)))
+        self.ndof, self.nnz, self.torder, self.nelem_total = nd.value, nz.value, to.value, el.value
+        self.nelem = tuple(int(n) for n in nelem)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().igapgpu_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pattern(self):
+        rowptr = np.zeros(self.ndof + 1, np.int64)
+        cols = np.zeros(self.nnz, np.int32)
+        _check(lib().igapgpu_pattern(self.h, _ptr(rowptr), _ptr(cols)))
+        return rowptr, cols
+
+    def set_history(self, level, U):
+        _check(lib().igapgpu_set_history(self.h, level, _ptr(U)))
+
+    def get_history(self, level, out=None):
+        out = np.zeros(self.ndof) if out is None else out
+        _check(lib().igapgpu_get_history(self.h, level, _ptr(out)))
+        return out
+
+    def shift_history(self):
+        _check(lib().igapgpu_shift_history(self.h))
+
+    def set_state(self, U_hist):
+        """U_hist: (torder+1, ndof) array; row 0 is the current iterate."""
+        for lvl in range(self.torder + 1):
+            self.set_history(lvl, np.ascontiguousarray(U_hist[lvl]) if isinstance(U_hist, np.ndarray) else U_hist[lvl])
+
+    def residual(self, U=None, out=None):
+        out = np.zeros(self.ndof) if out is None else out
+        _check(lib().igapgpu_residual(self.h, _ptr(U), _ptr(out)))
+        return out
+
+    def tangent(self, U=None, out=None):
+        out = np.zeros(self.nnz) if out is None else out
+        _check(lib().igapgpu_tangent(self.h, _ptr(U), _ptr(out)))
+        return out
+
+    def assemble(self, U=None, RR=None, vals=None):
+        _check(lib().igapgpu_assemble(self.h, _ptr(U), _ptr(RR), _ptr(vals)))
+        return RR, vals
+
+    def tangent_internal(self, U=None):
+        """Assemble into the context's own matrix (used by matmult / solve)."""
+        _check(lib().igapgpu_tangent(self.h, _ptr(U), None))
+
+    def matmult(self, x, y=None):
+        y = np.zeros(self.ndof) if y is None else y
+        _check(lib().igapgpu_matmult(self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def diagonal(self, out=None):
+        out = np.zeros(self.ndof) if out is None else out
+        _check(lib().igapgpu_get_diagonal(self.h, _ptr(out)))
+        return out
+
+    @staticmethod
+    def default_opts(**kw):
+        o = SolverOpts()
+        lib().igapgpu_default_solver_opts(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    def ksp_solve(self, b, x, **kw):
+        o = self.default_opts(**kw)
+        its = ctypes.c_int()
+        rn = ctypes.c_double()
+        _check(lib().igapgpu_ksp_solve(self.h, _ptr(b), _ptr(x), ctypes.byref(o), ctypes.byref(its),
+                                       ctypes.byref(rn)))
+        return its.value, rn.value
+
+    def solve(self, U, **kw):
+        o = self.default_opts(**kw)
+        st = SolveStats()
+        _check(lib().igapgpu_solve(self.h, _ptr(U), ctypes.byref(o), ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in SolveStats._fields_}
+
+    def set_precision(self, mode):
+        _check(lib().igapgpu_set_precision(self.h, mode))
+
+    def set_stream(self, stream_handle):
+        """stream_handle: an integer cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        _check(lib().igapgpu_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def synchronize(self):
+        _check(lib().igapgpu_synchronize(self.h))
+
+    def profile(self, enable=True):
+        _check(lib().igapgpu_profile(self.h, int(enable)))
+
+    def profile_read(self):
+        ms = ctypes.c_double()
+        nl, ne = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().igapgpu_profile_read(self.h, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ne)))
+        return ms.value, nl.value, ne.value
+
+
+def launch_count() -> int:
+    return int(lib().igapgpu_launch_count())
+
+
+def measure_fp64_peak() -> float:
+    t = ctypes.c_double()
+    _check(lib().igapgpu_measure_fp64_peak(ctypes.byref(t)))
+    return t.value

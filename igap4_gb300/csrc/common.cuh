@@ -1,0 +1,153 @@
+// Internal definitions shared by the translation units of libigapgpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <atomic>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "igapgpu.h"
+
+namespace igap {
+
+constexpr int P = 2;                    // B-spline degree handled on the device
+constexpr int P1 = P + 1;               // basis functions per direction per element
+constexpr int NB = P1 * P1 * P1;        // 27 basis functions per element
+constexpr int NDD = 10;                 // value, 3 first, 6 second derivatives
+constexpr int NE = 3 * NB;              // 81 element DOFs
+constexpr int TAB = 3 * P1 + 2;         // 1-D table entry: N, dN, ddN of 3 functions, xi, h
+constexpr int MAXQ = 6;                 // max Gauss points per direction
+
+// Reference-ABI constants (include/physimpl.h, src/assmcore_iga.c)
+constexpr int NFACE = 6;
+
+void set_error(const char *fmt, ...);
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+#define IGAP_CUDA(call)                                                              \
+  do {                                                                               \
+    cudaError_t _e = (call);                                                         \
+    if (_e != cudaSuccess) {                                                         \
+      ::igap::set_error("CUDA error %s at %s:%d: %s", cudaGetErrorName(_e), __FILE__, \
+                        __LINE__, cudaGetErrorString(_e));                           \
+      return IGAPGPU_ERR_CUDA;                                                       \
+    }                                                                                \
+  } while (0)
+
+#define IGAP_CHECK_LAUNCH() IGAP_CUDA(cudaGetLastError())
+
+// Device-resident problem description used by the element kernels.
+struct DevMesh {
+  int nelem[3];
+  int nbasis[3];           // nelem + P
+  int nquad;
+  int npts;                // nquad^3
+  const double *tab[3];    // [nelem_d][nquad][TAB] 1-D basis tables (with the knot-span MTOL)
+  const double *wq;        // [nquad] Gauss weights on [0,1]
+  const double *w;         // [ncp]
+  const double *X;         // [3*ncp]
+  const int64_t *rowptr;   // [ndof+1]
+  int64_t ndof;
+};
+
+struct DevLaw {
+  int law;
+  int nhist;               // torder + 1
+  double par[9];
+  const double *Dconst;    // 900 constant tangent of a linear law (or null)
+};
+
+struct Context {
+  // problem
+  int law, torder, nquad, prec;
+  double par[9];
+  int nelem[3], nbasis[3];
+  int64_t ndof, nnz, nelem_total, ncp;
+  igapgpu_bc_desc bc;
+  // device buffers
+  double *d_tab[3] = {nullptr, nullptr, nullptr};
+  double *d_tabn[3] = {nullptr, nullptr, nullptr}; // plain Cox-de Boor (face integrals)
+  double *d_knots[3] = {nullptr, nullptr, nullptr};
+  double *d_wq = nullptr, *d_xq = nullptr;
+  double *d_w = nullptr, *d_X = nullptr;
+  double *d_Uhist = nullptr;   // [(torder+1)][ndof]
+  double *d_RR = nullptr;      // [ndof]
+  double *d_vals = nullptr;    // [nnz] the context's matrix
+  int64_t *d_rowptr = nullptr; // [ndof+1]
+  int32_t *d_cols = nullptr;   // [nnz]
+  double *d_Dconst = nullptr;  // [900]
+  double *d_Fneu = nullptr;    // [ndof] Neumann load (state independent)
+  int64_t n_dir = 0;           // Dirichlet rows (unique, last writer wins)
+  int64_t *d_dir_rows = nullptr;
+  double *d_dir_g = nullptr;
+  double *d_stage_a = nullptr, *d_stage_b = nullptr; // host-pointer staging [ndof]
+  double *d_stage_v = nullptr;                       // host-pointer staging [nnz] (lazy)
+  bool matrix_valid = false;
+  // Krylov workspace (lazy)
+  int ksp_restart = 0;
+  double *d_V = nullptr;       // [(restart+1)][ndof]
+  double *d_Z = nullptr;       // [restart][ndof] (right-preconditioned directions)
+  double *d_work = nullptr;    // [4][ndof]
+  double *d_diag = nullptr;    // [ndof]
+  double *d_red = nullptr;     // device scalars (norms, Hessenberg column) [red_cap]
+  double *h_red = nullptr;     // pinned host mirror of d_red [red_cap]
+  double *d_partial = nullptr; // per-block partial sums of the reductions
+  int red_cap = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // element-kernel timing (igapgpu_profile)
+  bool prof = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev;
+  int64_t prof_launches = 0, prof_elements = 0;
+
+  DevMesh devmesh() const {
+    DevMesh m;
+    for (int d = 0; d < 3; d++) {
+      m.nelem[d] = nelem[d];
+      m.nbasis[d] = nbasis[d];
+      m.tab[d] = d_tab[d];
+    }
+    m.nquad = nquad;
+    m.npts = nquad * nquad * nquad;
+    m.wq = d_wq;
+    m.w = d_w;
+    m.X = d_X;
+    m.rowptr = d_rowptr;
+    m.ndof = ndof;
+    return m;
+  }
+  DevLaw devlaw() const {
+    DevLaw l;
+    l.law = law;
+    l.nhist = torder + 1;
+    for (int i = 0; i < 9; i++) l.par[i] = par[i];
+    l.Dconst = d_Dconst;
+    return l;
+  }
+};
+
+// Pointer classification: true if ptr is device (or managed) memory.
+bool is_device_ptr(const void *p);
+
+// assemble.cu
+int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
+int launch_basis_tables(Context *c);
+int launch_lingrad_dconst(Context *c);
+int launch_neumann(Context *c, const double nfac[NFACE][2]);
+int launch_dirichlet_matrix(Context *c, double *vals);
+int launch_dirichlet_residual(Context *c, double *RR);
+int launch_pattern_cols(Context *c);
+// krylov.cu
+int spmv(Context *c, const double *vals, const double *x, double *y);
+int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
+              double *rnorm);
+int dev_norm2(Context *c, const double *x, double *out);
+
+}  // namespace igap
+
+// The opaque handle of the C ABI is the context itself.
+struct igapgpu_ctx : public igap::Context {};

@@ -1,0 +1,178 @@
+/*
+ * igapgpu.h -- C ABI of libigapgpu.so, the GB300 (sm_103a) implementation of
+ * IGAP4's element assembly and Newton-Krylov inner loop on one GPU.
+ *
+ * Plain C types only.  Every array argument may be a host pointer or a CUDA
+ * device pointer; the library inspects it (cudaPointerGetAttributes) and
+ * stages host data through device buffers it owns.  With device pointers the
+ * call is asynchronous on the context's stream; with any host pointer the call
+ * returns after the host data are consumed / produced.
+ *
+ * Numbering follows the reference on one rank: control point
+ *   cp = (ny+p)(nz+p) ix + (nz+p) iy + iz,  DOF = 3 cp + d
+ * (src/interface.c:163-168, src/commcore_iga.c:28-37), state history
+ * U_hist[(torder+1)][ndof] with level 0 the current iterate
+ * (include/coreimpl.h:17, src/assmcore_iga.c:66-80).
+ *
+ * Errors: every entry point returns IGAPGPU_OK (0) or a negative code; the
+ * text of the last error is available from igapgpu_last_error().  There is no
+ * CPU fallback: without a usable GPU, igapgpu_assm_init fails.
+ */
+#ifndef IGAPGPU_H
+#define IGAPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IGAPGPU_OK 0
+#define IGAPGPU_ERR_ARG -1       /* invalid argument / unsupported configuration */
+#define IGAPGPU_ERR_CUDA -2      /* CUDA runtime error */
+#define IGAPGPU_ERR_NOMEM -3     /* device allocation failed */
+#define IGAPGPU_ERR_LAW -4       /* unknown constitutive law: no CPU fallback */
+#define IGAPGPU_ERR_NUMERIC -5   /* non-finite residual norm / breakdown */
+#define IGAPGPU_ERR_STATE -6     /* call order violated (e.g. matmult before tangent) */
+#define IGAPGPU_ERR_TIMEOUT -7   /* a bounded device wait expired */
+
+/* Laws: the reference's two plugins and the project's linear law. */
+#define IGAPGPU_LAW_GRADELAST 0     /* phys/gradelast.c, torder 0, par[9] */
+#define IGAPGPU_LAW_GRADELASTTIME 1 /* phys/gradelasttime.c, torder 2, par[9] */
+#define IGAPGPU_LAW_LINGRAD 2       /* linear isotropic strain gradient, par = {lambda, mu, ell} */
+
+/* Precision of the element contraction (the rest is always FP64). */
+#define IGAPGPU_PREC_FP64 0  /* FP64 everywhere */
+#define IGAPGPU_PREC_SPLIT 1 /* tensor-core split-BF16 products, FP32 accumulate */
+
+typedef struct igapgpu_ctx *igapgpu_t;
+
+/* Mesh of one rank (the global mesh on one GPU), as struct __Mesh holds it
+ * after partitioning (include/meshimpl.h:6-16). */
+typedef struct {
+  int porder;             /* B-spline degree, 2 */
+  int nelem[3];           /* elements per direction */
+  const double *knots[3]; /* knot vectors, nelem[d] + 1 + 2 porder entries */
+  const double *w;        /* weights, prod(nelem+porder) entries, x-major, z fastest */
+  const double *X;        /* control points, 3 per weight */
+} igapgpu_mesh_desc;
+
+/* Law selection and parameters (struct __Phys, include/physimpl.h:13-28). */
+typedef struct {
+  int law;
+  double par[9];
+} igapgpu_phys_desc;
+
+/* Boundary data (struct __BC, include/bcimpl.h:8-15) with the Neumann
+ * callback replaced by a constant traction table.  Index 6*face + 3*order + d;
+ * faces 0/1 = x-min/x-max, 2/3 = y, 4/5 = z; bc_type 1 = Neumann, 0 = Dirichlet. */
+typedef struct {
+  int bc_type[36];
+  double par_periodic[9]; /* affine periodic offset; must be 0 on a non-periodic mesh */
+  double par_dirichlet[9];
+  double neumann[36];
+} igapgpu_bc_desc;
+
+/* Newton-Krylov options (defaults of IGAPSolvInit, src/interface.c:207-250). */
+typedef struct {
+  double snes_abstol;  /* |F| below this: converged (1e-10) */
+  double snes_rtol;    /* relative to |F_0| (1e-20) */
+  double snes_stol;    /* |dU| / |U| step tolerance (1e-20) */
+  int snes_max_it;     /* Newton iterations (the reference loops SNES max_it=1 up to 10000) */
+  int linesearch;      /* 0 = full step, 1 = backtracking (cubic) */
+  int ksp_restart;     /* GMRES restart length */
+  double ksp_rtol;     /* relative residual tolerance of the linear solve */
+  double ksp_abstol;
+  double ksp_dtol;
+  int ksp_max_it;
+  int pc;              /* 0 = none, 1 = Jacobi */
+} igapgpu_solver_opts;
+
+typedef struct {
+  int newton_its;
+  int ksp_its_total;
+  int ksp_its_last;
+  int converged;     /* 1 converged, 0 not (reason < 0) */
+  int reason;        /* PETSc-like SNESConvergedReason value */
+  double fnorm0;
+  double fnorm;
+} igapgpu_solve_stats;
+
+/* IGAPAssmInit (src/interface.c:131-203): upload the mesh, build the CSR
+ * pattern (setnz_iga, src/assmcore_iga.c:1054-1087, plus the columns the
+ * element loop inserts), the element colouring, the Dirichlet row list and the
+ * Neumann load; allocate the state history, residual and matrix.
+ * nquad: Gauss points per direction (4 as the reference, 3 allowed). */
+int igapgpu_assm_init(igapgpu_t *ctx, const igapgpu_mesh_desc *mesh,
+                      const igapgpu_phys_desc *phys, const igapgpu_bc_desc *bc, int nquad);
+/* Frees every device buffer of the context (IGAPFinalize, src/interface.c:362). */
+int igapgpu_finalize(igapgpu_t ctx);
+
+int igapgpu_sizes(igapgpu_t ctx, int64_t *ndof, int64_t *nnz, int *torder, int64_t *nelem);
+/* CSR pattern: rowptr[ndof+1] (int64), cols[nnz] (int32), rows in DOF order,
+ * columns ascending -- the AIJ structure PETSc holds after the first
+ * MatSetValues of Tangent_iga (MAT_KEEP_NONZERO_PATTERN, src/interface.c:196). */
+int igapgpu_pattern(igapgpu_t ctx, int64_t *rowptr, int32_t *cols);
+
+/* State history U_hist[level] (level 0 current, 1 = u_n, 2 = u_{n-1}). */
+int igapgpu_set_history(igapgpu_t ctx, int level, const double *U);
+int igapgpu_get_history(igapgpu_t ctx, int level, double *U);
+/* Time advance of the three-level scheme: u_{n-1} <- u_n, u_n <- U_hist[0].
+ * The reference has no such routine; its callers shift the history. */
+int igapgpu_shift_history(igapgpu_t ctx);
+
+/* Residual_iga (src/assmcore_iga.c:16-502): RR = volume residual + Neumann
+ * load, Dirichlet rows replaced by U - g.  Side effect as in the reference:
+ * U_hist[0] <- U.  U may be NULL (use U_hist[0]). */
+int igapgpu_residual(igapgpu_t ctx, const double *U, double *RR);
+/* Tangent_iga (src/assmcore_iga.c:507-858): CSR values of dRR/dU in the
+ * pattern order, Dirichlet rows and columns zeroed with unit diagonal
+ * (MatZeroRowsColumns).  vals may be NULL: the context's own matrix (used by
+ * igapgpu_matmult / the Newton solver) is assembled.  U may be NULL. */
+int igapgpu_tangent(igapgpu_t ctx, const double *U, double *vals);
+/* Residual and tangent in one fused element pass (same results as the two
+ * calls above).  RR / vals may be NULL as above. */
+int igapgpu_assemble(igapgpu_t ctx, const double *U, double *RR, double *vals);
+
+/* MatMult of the context's matrix (MATSHELL MATOP_MULT): y = K x. */
+int igapgpu_matmult(igapgpu_t ctx, const double *x, double *y);
+/* MatGetDiagonal (MATOP_GET_DIAGONAL, used by Jacobi). */
+int igapgpu_get_diagonal(igapgpu_t ctx, double *diag);
+
+/* KSPSolve on the context's matrix: right-preconditioned GMRES(restart) with
+ * modified Gram-Schmidt (src/interface.c:228-239), FP64, nonzero guess. */
+int igapgpu_ksp_solve(igapgpu_t ctx, const double *b, double *x, const igapgpu_solver_opts *opts,
+                      int *its, double *rnorm);
+/* IGAPSolvSolve (src/interface.c:302-328) on the device: Newton with the
+ * chosen line search, each step assembling the tangent and solving with
+ * GMRES; U is the initial iterate on entry and the solution on exit. */
+int igapgpu_solve(igapgpu_t ctx, double *U, const igapgpu_solver_opts *opts,
+                  igapgpu_solve_stats *stats);
+void igapgpu_default_solver_opts(igapgpu_solver_opts *opts);
+
+int igapgpu_set_precision(igapgpu_t ctx, int mode);
+/* Run on the caller's CUDA stream (cudaStream_t passed as void*); NULL
+ * restores the context's own stream. */
+int igapgpu_set_stream(igapgpu_t ctx, void *stream);
+int igapgpu_synchronize(igapgpu_t ctx);
+const char *igapgpu_last_error(void);
+
+/* Kernel launches issued by this library since load (for accounting). */
+int64_t igapgpu_launch_count(void);
+
+/* Timing of the element-assembly kernels with CUDA events recorded on the
+ * launching stream around each colour batch.  enable=1 resets and starts,
+ * enable=0 stops; igapgpu_profile_read synchronises and returns the summed
+ * kernel time (ms), the number of element-kernel launches and the number of
+ * elements they processed since the last reset. */
+int igapgpu_profile(igapgpu_t ctx, int enable);
+int igapgpu_profile_read(igapgpu_t ctx, double *elem_ms, int64_t *launches, int64_t *elements);
+
+/* Measured FP64 FMA throughput of this GPU (TFLOP/s) from a register-only
+ * kernel; used as the denominator of FP64-bound roofline fractions. */
+int igapgpu_measure_fp64_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,233 @@
+"""GPU parity: the CUDA assembly through the C ABI against the reference.
+
+* golden fixtures made by the reference's own code (tests/golden/) -- FP64
+  mode must agree to 1e-12 relative (norm-wise), sparsity pattern bit-exact;
+* the project's C restatement (oracle/) on larger and edge-case problems;
+* size-independent properties at the benchmark size (linearity, symmetry,
+  rigid-translation invariance).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import igap4_gb300 as ig
+import pyoracle as po
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # FP64 mode, relative in the 2-norm
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def gpu_case(prob: po.Problem):
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L, prob.p, prob.perturb)
+    return ig.Assembly(prob.nelem, knots, w, X, law=prob.law, par=prob.params(),
+                       bc_type=prob.bc_type, neumann=prob.neumann,
+                       par_dirichlet=prob.par_dirichlet, nquad=prob.nquad)
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def problem_from_golden(g):
+    return po.Problem(nelem=tuple(int(x) for x in g["nelem"]), L=tuple(g["L"]), law=int(g["law"]),
+                      perturb=bool(g["perturb"]), par=g["par"], bc_type=g["bc_type"].astype(np.int32),
+                      neumann=g["neumann"])
+
+
+@pytest.mark.parametrize("name", ["g_static_2x2x2", "g_lingrad_4x2x2", "g_transient_3x2x2"])
+def test_golden_full(name):
+    g = load(name)
+    prob = problem_from_golden(g)
+    A = gpu_case(prob)
+    A.set_state(g["U"])
+    RR = A.residual(np.ascontiguousarray(g["U"][0]))
+    assert rel(RR, g["RR"]) <= TOL
+    rowptr, cols = A.pattern()
+    np.testing.assert_array_equal(rowptr, g["rowptr"])
+    np.testing.assert_array_equal(cols, g["cols"])
+    vals = A.tangent(np.ascontiguousarray(g["U"][0]))
+    assert rel(vals, g["vals"]) <= TOL
+
+
+@pytest.mark.parametrize("name", ["g_static_beamtest_4x4x4", "g_lingrad_8x2x2"])
+def test_golden_summary(name):
+    g = load(name)
+    prob = problem_from_golden(g)
+    A = gpu_case(prob)
+    A.set_state(g["U"])
+    RR = A.residual()
+    assert rel(RR, g["RR"]) <= TOL
+    rowptr, cols = A.pattern()
+    np.testing.assert_array_equal(rowptr, g["rowptr"])
+    assert cols.astype(np.int64).sum() == g["cols_sum"]
+    vals = A.tangent()
+    assert abs(np.linalg.norm(vals) - g["vals_norm"]) <= TOL * g["vals_norm"]
+    np.testing.assert_allclose(vals[g["sample_idx"]], g["sample_vals"], rtol=0,
+                               atol=TOL * np.abs(g["sample_vals"]).max())
+
+
+CASES = [
+    # (law, nelem, perturb, L)
+    (po.LAW_LINGRAD, (8, 4, 3), False, (4.0, 1.0, 1.0)),
+    (po.LAW_GRADELAST, (4, 4, 4), True, (1.0, 1.0, 1.0)),
+    (po.LAW_GRADELAST, (5, 3, 4), False, (2.0, 1.0, 1.5)),
+    (po.LAW_GRADELASTTIME, (3, 3, 3), False, (1.0, 1.0, 1.0)),
+    (po.LAW_GRADELASTTIME, (4, 2, 3), True, (1.0, 1.0, 1.0)),
+]
+
+
+@pytest.mark.parametrize("law,nelem,perturb,L", CASES)
+def test_vs_oracle(law, nelem, perturb, L):
+    bct, neu = po.clamp_bc((0, 3), 5, (1e-3, 2e-3, -1e-3))
+    bct[6 * 1 + 3:6 * 1 + 6] = 1
+    neu[6 * 1 + 4] = 5e-4
+    prob = po.Problem(nelem=nelem, L=L, law=law, perturb=perturb, bc_type=bct, neumann=neu,
+                      par_dirichlet=np.linspace(0.01, 0.09, 9))
+    U = po.random_state(prob, 31)
+    orc = po.OracleCase(prob)
+    A = gpu_case(prob)
+    A.set_state(U)
+    assert rel(A.residual(), orc.residual(U)) <= TOL
+    assert rel(A.tangent(), orc.tangent(U)) <= TOL
+    # fused pass gives the same numbers
+    RR = np.zeros(A.ndof)
+    vals = np.zeros(A.nnz)
+    A.assemble(None, RR, vals)
+    assert rel(RR, orc.residual(U)) <= TOL
+    assert rel(vals, orc.tangent(U)) <= TOL
+
+
+def test_nquad3_mode_vs_oracle():
+    """27-point Gauss mode (nquad = 3): pinned by the oracle only."""
+    prob = po.Problem(nelem=(4, 3, 2), law=po.LAW_GRADELAST, nquad=3)
+    U = po.random_state(prob, 4)
+    orc = po.OracleCase(prob)
+    A = gpu_case(prob)
+    A.set_state(U)
+    assert rel(A.residual(), orc.residual(U)) <= TOL
+    assert rel(A.tangent(), orc.tangent(U)) <= TOL
+
+
+def test_device_pointers_and_history_side_effect():
+    torch = pytest.importorskip("torch")
+    prob = po.Problem(nelem=(3, 2, 2), law=po.LAW_GRADELAST)
+    U = po.random_state(prob, 8)
+    A = gpu_case(prob)
+    dU = torch.tensor(U[0], device="cuda")
+    dR = torch.zeros(A.ndof, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(A.nnz, dtype=torch.float64, device="cuda")
+    A.residual(dU, dR)
+    A.tangent(dU, dV)
+    A.synchronize()
+    orc = po.OracleCase(prob)
+    assert rel(dR.cpu().numpy(), orc.residual(U)) <= TOL
+    assert rel(dV.cpu().numpy(), orc.tangent(U)) <= TOL
+    # Residual_iga copies U into U_hist[0] (src/assmcore_iga.c:68)
+    np.testing.assert_array_equal(A.get_history(0), U[0])
+
+
+def test_symmetry_and_rigid_translation_full_size():
+    """Benchmark-size beam (128 x 32 x 32, linear law): the assembled tangent
+    is symmetric, the volume residual of a rigid translation vanishes, and the
+    linear law's residual is linear: R(U) - R(0) = K U on free rows."""
+    torch = pytest.importorskip("torch")
+    nelem = (128, 32, 32)
+    knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0))
+    A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD)  # all faces traction-free
+    rng = np.random.default_rng(2)
+    U = torch.tensor(rng.uniform(-1e-2, 1e-2, A.ndof), device="cuda")
+    R = torch.zeros(A.ndof, dtype=torch.float64, device="cuda")
+    A.tangent_internal(U)
+    A.residual(U, R)
+    KU = torch.zeros_like(R)
+    A.matmult(U, KU)
+    A.synchronize()
+    assert (torch.linalg.norm(R - KU) / torch.linalg.norm(R)).item() <= 1e-12
+    T = torch.tensor(np.tile([0.3, -0.2, 0.1], A.ndof // 3), device="cuda")
+    A.residual(T, R)
+    A.synchronize()
+    assert torch.abs(R).max().item() <= 1e-12 * torch.abs(KU).max().item() * 10
+    # symmetry: x^T K y == y^T K x
+    x = torch.tensor(rng.standard_normal(A.ndof), device="cuda")
+    y = torch.tensor(rng.standard_normal(A.ndof), device="cuda")
+    Kx = torch.zeros_like(x)
+    Ky = torch.zeros_like(x)
+    A.matmult(x, Kx)
+    A.matmult(y, Ky)
+    A.synchronize()
+    a, b = torch.dot(y, Kx).item(), torch.dot(x, Ky).item()
+    assert abs(a - b) <= 1e-12 * abs(a)
+
+
+def test_spmv_and_diagonal_vs_scipy():
+    sp = pytest.importorskip("scipy.sparse")
+    prob = po.Problem(nelem=(6, 3, 3), law=po.LAW_GRADELAST)
+    U = po.random_state(prob, 5)
+    A = gpu_case(prob)
+    A.set_state(U)
+    A.tangent_internal()
+    rowptr, cols = A.pattern()
+    vals = A.tangent()
+    K = sp.csr_matrix((vals, cols, rowptr), shape=(A.ndof, A.ndof))
+    x = np.random.default_rng(1).standard_normal(A.ndof)
+    assert rel(A.matmult(x), K @ x) <= 1e-14
+    np.testing.assert_array_equal(A.diagonal(), K.diagonal())
+
+
+def test_gmres_jacobi_solves():
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(8, 2, 2), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, bc_type=bct, neumann=neu)
+    A = gpu_case(prob)
+    A.tangent_internal(np.zeros(A.ndof))
+    rowptr, cols = A.pattern()
+    K = sp.csr_matrix((A.tangent(), cols, rowptr), shape=(A.ndof, A.ndof))
+    b = np.random.default_rng(3).standard_normal(A.ndof)
+    x = np.zeros(A.ndof)
+    its, rn = A.ksp_solve(b, x, ksp_rtol=1e-10, ksp_restart=200, ksp_max_it=20000)
+    xs = spl.spsolve(K.tocsc(), b)
+    assert np.linalg.norm(K @ x - b) <= 1e-9 * np.linalg.norm(b)
+    assert rel(x, xs) <= 1e-6
+
+
+def test_newton_linear_beam_matches_direct_solve():
+    """Config-1 style: clamped beam, tip traction, linear law; Newton-GMRES on
+    the device converges and agrees with a direct CPU solve."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(16, 4, 4), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, bc_type=bct, neumann=neu)
+    A = gpu_case(prob)
+    U = np.zeros(A.ndof)
+    st = A.solve(U, snes_abstol=1e-10, ksp_rtol=1e-10, ksp_restart=300, ksp_max_it=50000)
+    assert st["converged"] == 1, st
+    orc = po.OracleCase(prob)
+    R0 = orc.residual(np.zeros((1, A.ndof)))
+    rowptr, cols = orc.pattern()
+    K = sp.csr_matrix((orc.tangent(np.zeros((1, A.ndof))), cols, rowptr), shape=(A.ndof, A.ndof))
+    Us = spl.spsolve(K.tocsc(), -R0)
+    assert rel(U, Us) <= 1e-7
+    assert np.linalg.norm(orc.residual(U[None, :])) <= 1e-9
+
+
+def test_unknown_law_is_an_error():
+    knots, w, X = ig.beam_mesh((2, 2, 2))
+    with pytest.raises(ig.IgapGpuError):
+        ig.Assembly((2, 2, 2), knots, w, X, law=7)
+
+
+def test_bad_sizes_are_errors():
+    knots, w, X = ig.beam_mesh((2, 2, 2))
+    with pytest.raises(ig.IgapGpuError):
+        ig.Assembly((1, 2, 2), [np.zeros(6)] + knots[1:], w, X)
+    with pytest.raises(ig.IgapGpuError):
+        ig.Assembly((2, 2, 2), knots, w, X, nquad=9)
