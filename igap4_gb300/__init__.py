@@ -84,6 +84,7 @@ def lib():
         for f in ("igapgpu_residual", "igapgpu_tangent", "igapgpu_matmult", "igapgpu_get_diagonal"):
             getattr(L, f).argtypes = [vp, vp, vp]
         L.igapgpu_get_diagonal.argtypes = [vp, vp]
+        L.igapgpu_norm2.argtypes = [vp, vp, vp]
         L.igapgpu_assemble.argtypes = [vp, vp, vp, vp]
         L.igapgpu_ksp_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverOpts),
                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
@@ -252,6 +253,12 @@ class Assembly:
         y = np.zeros(self.ndof) if y is None else y
         _check(lib().igapgpu_matmult(self.h, _ptr(x), _ptr(y)))
         return y
+
+    def norm2(self, x):
+        """FP64 2-norm of a context-sized vector (host array or CUDA tensor)."""
+        out = ctypes.c_double()
+        _check(lib().igapgpu_norm2(self.h, _ptr(x), ctypes.byref(out)))
+        return out.value
 
     def diagonal(self, out=None):
         out = np.zeros(self.ndof) if out is None else out

@@ -333,6 +333,25 @@ void igapgpu_default_solver_opts(igapgpu_solver_opts *o)
   o->pc = 1;
 }
 
+int igapgpu_norm2(igapgpu_t c, const double *x, double *out)
+{
+  if (!c || !x || !out) return IGAPGPU_ERR_ARG;
+  const double *xd = x;
+  if (!is_device_ptr(x)) {
+    IGAP_CUDA(cudaMemcpyAsync(c->d_stage_a, x, sizeof(double) * c->ndof, cudaMemcpyHostToDevice, c->stream));
+    xd = c->d_stage_a;
+  }
+  double v = 0.0;
+  int r = dev_norm2(c, xd, &v);
+  if (r) return r;
+  if (is_device_ptr(out)) {
+    IGAP_CUDA(cudaMemcpyAsync(out, c->d_red, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  } else {
+    *out = v;
+  }
+  return IGAPGPU_OK;
+}
+
 int igapgpu_get_diagonal(igapgpu_t c, double *diag)
 {
   if (!c || !diag) return IGAPGPU_ERR_ARG;

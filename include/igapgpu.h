@@ -136,6 +136,9 @@ int igapgpu_assemble(igapgpu_t ctx, const double *U, double *RR, double *vals);
 
 /* MatMult of the context's matrix (MATSHELL MATOP_MULT): y = K x. */
 int igapgpu_matmult(igapgpu_t ctx, const double *x, double *y);
+/* VecNorm(NORM_2) of a device or host vector of the context's size, in FP64
+ * (the Newton residual norm, SNESGetFunctionNorm at src/interface.c:322). */
+int igapgpu_norm2(igapgpu_t ctx, const double *x, double *out);
 /* MatGetDiagonal (MATOP_GET_DIAGONAL, used by Jacobi). */
 int igapgpu_get_diagonal(igapgpu_t ctx, double *diag);
 

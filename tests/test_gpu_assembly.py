@@ -219,6 +219,13 @@ def test_newton_linear_beam_matches_direct_solve():
     assert np.linalg.norm(orc.residual(U[None, :])) <= 1e-9
 
 
+def test_norm2_matches_numpy():
+    prob = po.Problem(nelem=(6, 3, 3), law=po.LAW_GRADELAST)
+    A = gpu_case(prob)
+    x = np.random.default_rng(9).standard_normal(A.ndof)
+    assert abs(A.norm2(x) - np.linalg.norm(x)) <= 1e-14 * np.linalg.norm(x)
+
+
 def test_unknown_law_is_an_error():
     knots, w, X = ig.beam_mesh((2, 2, 2))
     with pytest.raises(ig.IgapGpuError):
