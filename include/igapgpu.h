@@ -139,6 +139,21 @@ int igapgpu_matmult(igapgpu_t ctx, const double *x, double *y);
 /* VecNorm(NORM_2) of a device or host vector of the context's size, in FP64
  * (the Newton residual norm, SNESGetFunctionNorm at src/interface.c:322). */
 int igapgpu_norm2(igapgpu_t ctx, const double *x, double *out);
+/* igapgpu_norm2 without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot obtain device memory from cudaMalloc:
+ * applications whose pool allocator already owns the GPU's memory (PyTorch's
+ * caching allocator, a PETSc device pool), and code that must not allocate or
+ * free because cudaMalloc / cudaFree can synchronise the whole device.
+ * x: n doubles in device memory; out: host or device pointer to one double;
+ * stream: cudaStream_t (NULL = default stream).  No context is needed.
+ * Scratch: a fixed 64 KiB array of partial sums compiled into the library,
+ * present on every GPU that loads it until the process exits; hence
+ * n <= 33,554,432 (8192 partial sums of 4096 elements), larger n is rejected
+ * with IGAPGPU_ERR_ARG.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU race; serialise them on one stream. */
+int igapgpu_norm2_noalloc(const double *x, int64_t n, double *out, void *stream);
 /* MatGetDiagonal (MATOP_GET_DIAGONAL, used by Jacobi). */
 int igapgpu_get_diagonal(igapgpu_t ctx, double *diag);
 
