@@ -99,6 +99,7 @@ def lib():
         L.igapgpu_profile.argtypes = [vp, ctypes.c_int]
         L.igapgpu_profile_read.argtypes = [vp, vp, vp, vp]
         L.igapgpu_measure_fp64_peak.argtypes = [vp]
+        L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
         _lib = L
     return _lib
 
@@ -309,6 +310,18 @@ class Assembly:
 
 def launch_count() -> int:
     return int(lib().igapgpu_launch_count())
+
+
+def tc_selftest(variant=0):
+    """Run the tcgen05 self-test GEMM; returns (D, expected) as (128, 32) arrays."""
+    out = np.zeros(128 * 32, np.float32)
+    _check(lib().igapgpu_tc_selftest(variant, _ptr(out)))
+    r = np.arange(128)[:, None]
+    n = np.arange(32)[:, None]
+    k = np.arange(16)[None, :]
+    A = ((r * 3 + k * 5) % 7) - 3
+    B = ((n * 2 + k * 3) % 5) - 2
+    return out.reshape(128, 32), (A @ B.T).astype(np.float32)
 
 
 def measure_fp64_peak() -> float:

@@ -15,13 +15,13 @@
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "laws.cuh"
+#include "element.cuh"
 
 namespace igap {
 
 #define MTOL 1.e-15  // knot-span denominator shift of src/meshcore_iga.c:10,303-307
 
 constexpr int THREADS = 384;
-constexpr int PW = 8;                 // points per chunk (one per warp)
 constexpr int NPAIR = NB * (NB + 1) / 2;  // 378 (b <= c) pairs
 
 __constant__ unsigned char c_pair_b[NPAIR];
@@ -67,24 +67,6 @@ __global__ void basis_table_kernel(const double *knots, int nelem, const double 
 }
 
 // ------------------------------------------------------------ pattern
-__device__ __forceinline__ void cp_coords(int64_t cp, const int nb[3], int &ix, int &iy, int &iz)
-{
-  iz = (int)(cp % nb[2]);
-  int64_t t = cp / nb[2];
-  iy = (int)(t % nb[1]);
-  ix = (int)(t / nb[1]);
-}
-
-// Position of column control point (jx,jy,jz) in the row of (ix,iy,iz).
-__device__ __forceinline__ int64_t stencil_pos(int ix, int iy, int iz, int jx, int jy, int jz,
-                                               const int nb[3])
-{
-  int lox = max(ix - P, 0), loy = max(iy - P, 0), loz = max(iz - P, 0);
-  int cy = min(iy + P, nb[1] - 1) - loy + 1;
-  int cz = min(iz + P, nb[2] - 1) - loz + 1;
-  return ((int64_t)(jx - lox) * cy + (jy - loy)) * cz + (jz - loz);
-}
-
 __global__ void pattern_cols_kernel(const int64_t *rowptr, int32_t *cols, int64_t ndof, int nb0,
                                     int nb1, int nb2)
 {
@@ -115,169 +97,13 @@ __global__ void lingrad_dconst_kernel(const double *par, double *D)
 
 // ------------------------------------------------------ element kernel
 struct ElemSmem {
-  double XV[NB * 3];
-  double wV[NB];
-  double U[3 * NE];          // [nhist][27][3]
+  ElemData E;
+  PointScratch Pt[PW];
   double R[PW][NB * NDD];    // physical basis of the chunk's points
-  double W[PW][NDD];
-  double Xg[PW][3 * NDD];
-  double u[PW][90];
   double rr[PW][30];         // weighted residual integrand
   double Dw[PW][900];        // weighted tangent integrand
   double M[27 * 81];
 };
-
-template <int LAWK>
-struct LawSmem {
-  LawScratch<1> s[1];
-};
-template <>
-struct LawSmem<1> {
-  LawScratch<1> s[PW];
-};
-template <>
-struct LawSmem<2> {
-  LawScratch<4> s[PW];
-};
-
-// Phase A for one point, executed by one warp.
-template <int LAWK, bool RES, bool TAN>
-__device__ void point_setup(ElemSmem &S, LawSmem<LAWK> &LS, const DevMesh &m, const DevLaw &L,
-                            int ex, int ey, int ez, int w, int q, int lane,
-                            const double *__restrict__ Dconst)
-{
-  double *R = S.R[w];
-  const int nq = m.nquad;
-  if (q >= m.npts) {  // padding point of an incomplete chunk: no contribution
-    for (int i = lane; i < NB * NDD; i += 32) R[i] = 0.0;
-    if (RES) for (int i = lane; i < 30; i += 32) S.rr[w][i] = 0.0;
-    if (TAN) for (int i = lane; i < 900; i += 32) S.Dw[w][i] = 0.0;
-    __syncwarp();
-    return;
-  }
-  const int qx = q / (nq * nq), qy = (q / nq) % nq, qz = q % nq;
-  const double *tx = m.tab[0] + ((size_t)ex * nq + qx) * TAB;
-  const double *ty = m.tab[1] + ((size_t)ey * nq + qy) * TAB;
-  const double *tz = m.tab[2] + ((size_t)ez * nq + qz) * TAB;
-  // (a) tensor-product basis, src/meshcore_iga.c:311-326
-  if (lane < NB) {
-    const int i = lane / 9, j = (lane / 3) % 3, l = lane % 3;
-    const double nx = tx[i], dx = tx[P1 + i], ddx = tx[2 * P1 + i];
-    const double ny = ty[j], dy = ty[P1 + j], ddy = ty[2 * P1 + j];
-    const double nz = tz[l], dz = tz[P1 + l], ddz = tz[2 * P1 + l];
-    double *o = R + NDD * lane;
-    o[0] = nx * ny * nz;
-    o[1] = dx * ny * nz;
-    o[2] = nx * dy * nz;
-    o[3] = nx * ny * dz;
-    o[4] = ddx * ny * nz;
-    o[5] = dx * dy * nz;
-    o[6] = dx * ny * dz;
-    o[7] = nx * ddy * nz;
-    o[8] = nx * dy * dz;
-    o[9] = nx * ny * ddz;
-  }
-  __syncwarp();
-  // (b) weight function W and its derivatives
-  if (lane < NDD) {
-    double s = 0.0;
-    for (int b = 0; b < NB; b++) s += S.wV[b] * R[NDD * b + lane];
-    S.W[w][lane] = s;
-  }
-  __syncwarp();
-  // (c) rational basis by the quotient rule, src/assmcore_iga.c:155-165
-  if (lane < NB) {
-    double *r = R + NDD * lane;
-    const double *W = S.W[w];
-    const double wb = S.wV[lane];
-    for (int k = 0; k < NDD; k++) r[k] = r[k] * wb / W[0];
-    for (int k = 1; k < NDD; k++) r[k] -= r[0] * W[k] / W[0];
-    int a = 4;
-    for (int i = 1; i < 4; i++)
-      for (int j = i; j < 4; j++) { r[a] -= (r[j] * W[i] + r[i] * W[j]) / W[0]; a++; }
-  }
-  __syncwarp();
-  // (d) geometry X and its derivatives, src/assmcore_iga.c:166-174
-  if (lane < 30) {
-    const int d = lane / NDD, k = lane % NDD;
-    double s = 0.0;
-    for (int b = 0; b < NB; b++) s += S.XV[3 * b + d] * R[NDD * b + k];
-    S.Xg[w][lane] = s;
-  }
-  __syncwarp();
-  // (e) Jacobian, its determinant and inverse
-  const double *Xg = S.Xg[w];
-  double G[9];
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) G[3 * i + j] = Xg[NDD * i + 1 + j];
-  const double detG = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
-                      G[2] * (G[3] * G[7] - G[4] * G[6]);
-  double Gi[9];
-  {
-    double c0 = G[4] * G[8] - G[5] * G[7], c1 = G[2] * G[7] - G[1] * G[8], c2 = G[1] * G[5] - G[2] * G[4];
-    double c3 = G[5] * G[6] - G[3] * G[8], c4 = G[0] * G[8] - G[2] * G[6], c5 = G[2] * G[3] - G[0] * G[5];
-    double c6 = G[3] * G[7] - G[4] * G[6], c7 = G[1] * G[6] - G[0] * G[7], c8 = G[0] * G[4] - G[1] * G[3];
-    double id = 1.0 / (G[0] * c0 + G[1] * c3 + G[2] * c6);
-    Gi[0] = c0 * id; Gi[1] = c1 * id; Gi[2] = c2 * id;
-    Gi[3] = c3 * id; Gi[4] = c4 * id; Gi[5] = c5 * id;
-    Gi[6] = c6 * id; Gi[7] = c7 * id; Gi[8] = c8 * id;
-  }
-  // (f) physical first and second derivatives, src/assmcore_iga.c:179-208
-  if (lane < NB) {
-    double *r = R + NDD * lane;
-    double n[NDD];
-    for (int k = 0; k < NDD; k++) n[k] = r[k];
-    for (int i = 0; i < 3; i++) {
-      double s = 0.0;
-      for (int j = 0; j < 3; j++) s += n[1 + j] * Gi[3 * j + i];
-      r[1 + i] = s;
-    }
-    for (int k = 4; k < NDD; k++)
-      for (int i = 0; i < 3; i++) n[k] -= r[1 + i] * Xg[NDD * i + k];
-    const double Hs[3][3] = {{n[4], n[5], n[6]}, {n[5], n[7], n[8]}, {n[6], n[8], n[9]}};
-    int a = 4;
-    for (int i = 0; i < 3; i++)
-      for (int j = i; j < 3; j++) {
-        double s = 0.0;
-        for (int mm = 0; mm < 3; mm++) {
-          double t = 0.0;
-          for (int l = 0; l < 3; l++) t += Hs[mm][l] * Gi[3 * l + j];
-          s += Gi[3 * mm + i] * t;
-        }
-        r[a++] = s;
-      }
-  }
-  __syncwarp();
-  // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
-  const int nh = L.nhist;
-  if (lane < 30) {
-    const int d = lane / NDD, k = lane % NDD;
-    for (int h = 0; h < nh; h++) {
-      double s = 0.0;
-      for (int b = 0; b < NB; b++) s += R[NDD * b + k] * S.U[h * NE + 3 * b + d];
-      S.u[w][30 * h + lane] = s;
-    }
-  }
-  __syncwarp();
-  const double wt = m.wq[qx] * m.wq[qy] * m.wq[qz] * tx[3 * P1 + 1] * ty[3 * P1 + 1] *
-                    tz[3 * P1 + 1] * detG;
-  // (h) law
-  if constexpr (LAWK == 0) {
-    const double *u = S.u[w];
-    if (RES && lane < 30) {
-      double s = 0.0;
-      for (int j = 0; j < 30; j++) s += Dconst[30 * lane + j] * u[j];
-      S.rr[w][lane] = wt * s;
-    }
-    if (TAN)
-      for (int i = lane; i < 900; i += 32) S.Dw[w][i] = wt * Dconst[i];
-    __syncwarp();
-  } else if constexpr (LAWK == 1) {
-    gradelast_warp<1, RES, TAN>(S.u[w], L.par, false, wt, S.rr[w], S.Dw[w], LS.s[w], lane);
-  } else {
-    gradelast_warp<4, RES, TAN>(S.u[w], L.par, true, wt, S.rr[w], S.Dw[w], LS.s[w], lane);
-  }
-}
 
 template <int LAWK, bool RES, bool TAN>
 __global__ void __launch_bounds__(THREADS, 1)
@@ -296,14 +122,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
   const int nh = L.nhist;
   // element data: weights, control points, state of every history level
-  for (int t = tid; t < NB; t += THREADS) {
-    const int i = t / 9, j = (t / 3) % 3, l = t % 3;
-    const int64_t cp = ((int64_t)(ex + i) * nb1 + (ey + j)) * nb2 + (ez + l);
-    S.wV[t] = m.w[cp];
-    for (int d = 0; d < 3; d++) S.XV[3 * t + d] = m.X[3 * cp + d];
-    for (int h = 0; h < nh; h++)
-      for (int d = 0; d < 3; d++) S.U[h * NE + 3 * t + d] = Uhist[(int64_t)h * m.ndof + 3 * cp + d];
-  }
+  load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, THREADS);
   __syncthreads();
 
   double acc[9];
@@ -315,7 +134,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   const int nchunk = (m.npts + PW - 1) / PW;
   for (int ch = 0; ch < nchunk; ch++) {
-    if (warp < PW) point_setup<LAWK, RES, TAN>(S, LS, m, L, ex, ey, ez, warp, ch * PW + warp, lane, L.Dconst);
+    if (warp < PW)
+      point_setup<LAWK, RES, TAN, double>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp, ch * PW + warp,
+                                          lane, S.R[warp], S.rr[warp], S.Dw[warp]);
     __syncthreads();
     if (RES && tid < NE) {
       const int bb = tid / 3, d = tid % 3;
@@ -534,15 +355,36 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   if (do_res && do_tan) rc = run_colours<LK, true, true>(c, RR, vals);      \
   else if (do_res) rc = run_colours<LK, true, false>(c, RR, vals);          \
   else rc = run_colours<LK, false, true>(c, RR, vals);
-  if (c->law == IGAPGPU_LAW_LINGRAD) { IGAP_DISPATCH(0) }
-  else if (c->law == IGAPGPU_LAW_GRADELAST) { IGAP_DISPATCH(1) }
-  else if (c->law == IGAPGPU_LAW_GRADELASTTIME) { IGAP_DISPATCH(2) }
-  else {
-    set_error("unknown law %d", c->law);
-    return IGAPGPU_ERR_LAW;
+  // split precision: the residual stays FP64, the tangent goes to the tensor cores
+  const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT;
+  const bool k_res = do_res, k_tan = fp64_tan;
+  if (k_res || k_tan) {
+    const bool do_res_k = k_res, do_tan_k = k_tan;
+    {
+      const bool do_res = do_res_k, do_tan = do_tan_k;
+      if (c->law == IGAPGPU_LAW_LINGRAD) { IGAP_DISPATCH(0) }
+      else if (c->law == IGAPGPU_LAW_GRADELAST) { IGAP_DISPATCH(1) }
+      else if (c->law == IGAPGPU_LAW_GRADELASTTIME) { IGAP_DISPATCH(2) }
+      else {
+        set_error("unknown law %d", c->law);
+        return IGAPGPU_ERR_LAW;
+      }
+    }
   }
 #undef IGAP_DISPATCH
   if (rc) return rc;
+  if (do_tan && !fp64_tan) {
+    IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+    rc = launch_tc_tangent(c, vals);
+    if (rc) return rc;
+    int herr = 0;
+    IGAP_CUDA(cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    IGAP_CUDA(cudaStreamSynchronize(c->stream));
+    if (herr) {
+      set_error("tensor-core tangent: a bounded mbarrier wait expired (code %d)", herr);
+      return IGAPGPU_ERR_TIMEOUT;
+    }
+  }
   if (do_res) {
     rc = launch_dirichlet_residual(c, RR);
     if (rc) return rc;

@@ -81,6 +81,7 @@ struct Context {
   int32_t *d_cols = nullptr;   // [nnz]
   double *d_Dconst = nullptr;  // [900]
   double *d_Fneu = nullptr;    // [ndof] Neumann load (state independent)
+  int *d_err = nullptr;        // device error word (bounded waits that expired)
   int64_t n_dir = 0;           // Dirichlet rows (unique, last writer wins)
   int64_t *d_dir_rows = nullptr;
   double *d_dir_g = nullptr;
@@ -141,6 +142,8 @@ int launch_neumann(Context *c, const double nfac[NFACE][2]);
 int launch_dirichlet_matrix(Context *c, double *vals);
 int launch_dirichlet_residual(Context *c, double *RR);
 int launch_pattern_cols(Context *c);
+// tc_tangent.cu
+int launch_tc_tangent(Context *c, double *vals);
 // krylov.cu
 int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,

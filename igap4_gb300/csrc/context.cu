@@ -162,7 +162,7 @@ static int free_ctx(Context *c)
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
-                  c->d_diag, c->d_red, c->d_partial};
+                  c->d_diag, c->d_red, c->d_partial, c->d_err};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int d = 0; d < 3; d++) {
@@ -261,6 +261,8 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   if ((r = dev_alloc(&c->d_stage_a, c->ndof))) return r;
   if ((r = dev_alloc(&c->d_stage_b, c->ndof))) return r;
   if ((r = dev_alloc(&c->d_Fneu, c->ndof))) return r;
+  if ((r = dev_alloc(&c->d_err, 1))) return r;
+  IGAP_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
   if ((r = dev_alloc(&c->d_red, 64))) return r;
   if ((r = dev_alloc(&c->d_partial, 1024))) return r;
   IGAP_CUDA(cudaMallocHost(&c->h_red, 64 * sizeof(double)));

@@ -1,0 +1,213 @@
+// Per-element data and the per-quadrature-point set-up (phase A) shared by
+// the FP64 element kernel and the tensor-core split-precision kernel.
+#pragma once
+#include "common.cuh"
+#include "laws.cuh"
+
+namespace igap {
+
+constexpr int PW = 8;  // points per chunk (one warp each)
+
+// Element data in shared memory: weights, control points, state levels.
+struct ElemData {
+  double XV[NB * 3];
+  double wV[NB];
+  double U[3 * NE];  // [nhist][27][3]
+};
+
+// Per-warp scratch of one point.
+struct PointScratch {
+  double W[NDD];
+  double Xg[3 * NDD];
+  double u[90];
+};
+
+template <int LAWK>
+struct LawSmem {
+  LawScratch<1> s[1];
+};
+template <>
+struct LawSmem<1> {
+  LawScratch<1> s[PW];
+};
+template <>
+struct LawSmem<2> {
+  LawScratch<4> s[PW];
+};
+
+__device__ __forceinline__ void load_element(ElemData &E, const DevMesh &m, int nh,
+                                             const double *__restrict__ Uhist, int ex, int ey,
+                                             int ez, int tid, int nthreads)
+{
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  for (int t = tid; t < NB; t += nthreads) {
+    const int i = t / 9, j = (t / 3) % 3, l = t % 3;
+    const int64_t cp = ((int64_t)(ex + i) * nb1 + (ey + j)) * nb2 + (ez + l);
+    E.wV[t] = m.w[cp];
+    for (int d = 0; d < 3; d++) E.XV[3 * t + d] = m.X[3 * cp + d];
+    for (int h = 0; h < nh; h++)
+      for (int d = 0; d < 3; d++) E.U[h * NE + 3 * t + d] = Uhist[(int64_t)h * m.ndof + 3 * cp + d];
+  }
+}
+
+__device__ __forceinline__ void cp_coords(int64_t cp, const int nb[3], int &ix, int &iy, int &iz)
+{
+  iz = (int)(cp % nb[2]);
+  int64_t t = cp / nb[2];
+  iy = (int)(t % nb[1]);
+  ix = (int)(t / nb[1]);
+}
+
+// Position of column control point (jx,jy,jz) in the row of (ix,iy,iz).
+__device__ __forceinline__ int64_t stencil_pos(int ix, int iy, int iz, int jx, int jy, int jz,
+                                               const int nb[3])
+{
+  int lox = max(ix - P, 0), loy = max(iy - P, 0), loz = max(iz - P, 0);
+  int cy = min(iy + P, nb[1] - 1) - loy + 1;
+  int cz = min(iz + P, nb[2] - 1) - loz + 1;
+  return ((int64_t)(jx - lox) * cy + (jy - loy)) * cz + (jz - loz);
+}
+
+// Phase A for one point, executed by one warp.
+// Outputs: R[27*10] physical basis, rr[30] weighted residual integrand,
+// D[900] weighted tangent integrand (DT = double, or float for the split mode).
+template <int LAWK, bool RES, bool TAN, typename DT>
+__device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &LS, const DevMesh &m,
+                            const DevLaw &L, int ex, int ey, int ez, int w, int q, int lane,
+                            double *R, double *rr, DT *D)
+{
+  const double *__restrict__ Dconst = L.Dconst;
+  const int nq = m.nquad;
+  if (q >= m.npts) {  // padding point of an incomplete chunk: no contribution
+    for (int i = lane; i < NB * NDD; i += 32) R[i] = 0.0;
+    if (RES) for (int i = lane; i < 30; i += 32) rr[i] = 0.0;
+    if (TAN) for (int i = lane; i < 900; i += 32) D[i] = (DT)0;
+    __syncwarp();
+    return;
+  }
+  const int qx = q / (nq * nq), qy = (q / nq) % nq, qz = q % nq;
+  const double *tx = m.tab[0] + ((size_t)ex * nq + qx) * TAB;
+  const double *ty = m.tab[1] + ((size_t)ey * nq + qy) * TAB;
+  const double *tz = m.tab[2] + ((size_t)ez * nq + qz) * TAB;
+  // (a) tensor-product basis, src/meshcore_iga.c:311-326
+  if (lane < NB) {
+    const int i = lane / 9, j = (lane / 3) % 3, l = lane % 3;
+    const double nx = tx[i], dx = tx[P1 + i], ddx = tx[2 * P1 + i];
+    const double ny = ty[j], dy = ty[P1 + j], ddy = ty[2 * P1 + j];
+    const double nz = tz[l], dz = tz[P1 + l], ddz = tz[2 * P1 + l];
+    double *o = R + NDD * lane;
+    o[0] = nx * ny * nz;
+    o[1] = dx * ny * nz;
+    o[2] = nx * dy * nz;
+    o[3] = nx * ny * dz;
+    o[4] = ddx * ny * nz;
+    o[5] = dx * dy * nz;
+    o[6] = dx * ny * dz;
+    o[7] = nx * ddy * nz;
+    o[8] = nx * dy * dz;
+    o[9] = nx * ny * ddz;
+  }
+  __syncwarp();
+  // (b) weight function W and its derivatives
+  if (lane < NDD) {
+    double s = 0.0;
+    for (int b = 0; b < NB; b++) s += E.wV[b] * R[NDD * b + lane];
+    P.W[lane] = s;
+  }
+  __syncwarp();
+  // (c) rational basis by the quotient rule, src/assmcore_iga.c:155-165
+  if (lane < NB) {
+    double *r = R + NDD * lane;
+    const double *W = P.W;
+    const double wb = E.wV[lane];
+    for (int k = 0; k < NDD; k++) r[k] = r[k] * wb / W[0];
+    for (int k = 1; k < NDD; k++) r[k] -= r[0] * W[k] / W[0];
+    int a = 4;
+    for (int i = 1; i < 4; i++)
+      for (int j = i; j < 4; j++) { r[a] -= (r[j] * W[i] + r[i] * W[j]) / W[0]; a++; }
+  }
+  __syncwarp();
+  // (d) geometry X and its derivatives, src/assmcore_iga.c:166-174
+  if (lane < 30) {
+    const int d = lane / NDD, k = lane % NDD;
+    double s = 0.0;
+    for (int b = 0; b < NB; b++) s += E.XV[3 * b + d] * R[NDD * b + k];
+    P.Xg[lane] = s;
+  }
+  __syncwarp();
+  // (e) Jacobian, its determinant and inverse
+  const double *Xg = P.Xg;
+  double G[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) G[3 * i + j] = Xg[NDD * i + 1 + j];
+  const double detG = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
+                      G[2] * (G[3] * G[7] - G[4] * G[6]);
+  double Gi[9];
+  {
+    double c0 = G[4] * G[8] - G[5] * G[7], c1 = G[2] * G[7] - G[1] * G[8], c2 = G[1] * G[5] - G[2] * G[4];
+    double c3 = G[5] * G[6] - G[3] * G[8], c4 = G[0] * G[8] - G[2] * G[6], c5 = G[2] * G[3] - G[0] * G[5];
+    double c6 = G[3] * G[7] - G[4] * G[6], c7 = G[1] * G[6] - G[0] * G[7], c8 = G[0] * G[4] - G[1] * G[3];
+    double id = 1.0 / (G[0] * c0 + G[1] * c3 + G[2] * c6);
+    Gi[0] = c0 * id; Gi[1] = c1 * id; Gi[2] = c2 * id;
+    Gi[3] = c3 * id; Gi[4] = c4 * id; Gi[5] = c5 * id;
+    Gi[6] = c6 * id; Gi[7] = c7 * id; Gi[8] = c8 * id;
+  }
+  // (f) physical first and second derivatives, src/assmcore_iga.c:179-208
+  if (lane < NB) {
+    double *r = R + NDD * lane;
+    double n[NDD];
+    for (int k = 0; k < NDD; k++) n[k] = r[k];
+    for (int i = 0; i < 3; i++) {
+      double s = 0.0;
+      for (int j = 0; j < 3; j++) s += n[1 + j] * Gi[3 * j + i];
+      r[1 + i] = s;
+    }
+    for (int k = 4; k < NDD; k++)
+      for (int i = 0; i < 3; i++) n[k] -= r[1 + i] * Xg[NDD * i + k];
+    const double Hs[3][3] = {{n[4], n[5], n[6]}, {n[5], n[7], n[8]}, {n[6], n[8], n[9]}};
+    int a = 4;
+    for (int i = 0; i < 3; i++)
+      for (int j = i; j < 3; j++) {
+        double s = 0.0;
+        for (int mm = 0; mm < 3; mm++) {
+          double t = 0.0;
+          for (int l = 0; l < 3; l++) t += Hs[mm][l] * Gi[3 * l + j];
+          s += Gi[3 * mm + i] * t;
+        }
+        r[a++] = s;
+      }
+  }
+  __syncwarp();
+  // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
+  const int nh = L.nhist;
+  if (lane < 30) {
+    const int d = lane / NDD, k = lane % NDD;
+    for (int h = 0; h < nh; h++) {
+      double s = 0.0;
+      for (int b = 0; b < NB; b++) s += R[NDD * b + k] * E.U[h * NE + 3 * b + d];
+      P.u[30 * h + lane] = s;
+    }
+  }
+  __syncwarp();
+  const double wt = m.wq[qx] * m.wq[qy] * m.wq[qz] * tx[3 * P1 + 1] * ty[3 * P1 + 1] *
+                    tz[3 * P1 + 1] * detG;
+  // (h) law
+  if constexpr (LAWK == 0) {
+    const double *u = P.u;
+    if (RES && lane < 30) {
+      double s = 0.0;
+      for (int j = 0; j < 30; j++) s += Dconst[30 * lane + j] * u[j];
+      rr[lane] = wt * s;
+    }
+    if (TAN)
+      for (int i = lane; i < 900; i += 32) D[i] = (DT)(wt * Dconst[i]);
+    __syncwarp();
+  } else if constexpr (LAWK == 1) {
+    gradelast_warp<1, RES, TAN, DT>(P.u, L.par, false, wt, rr, D, LS.s[w], lane);
+  } else {
+    gradelast_warp<4, RES, TAN, DT>(P.u, L.par, true, wt, rr, D, LS.s[w], lane);
+  }
+}
+
+
+}  // namespace igap

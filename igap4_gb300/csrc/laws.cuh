@@ -108,9 +108,9 @@ __device__ __forceinline__ void landau(const double *par, double &A, double &B, 
 
 // Finite-strain gradient elasticity, NJ = 1 (static point) or 4 (transient
 // segment jets).  u: nhist*30 (smem), rr/D outputs scaled by wt.
-template <int NJ, bool RES, bool TAN>
+template <int NJ, bool RES, bool TAN, typename DT = double>
 __device__ void gradelast_warp(const double *u, const double *par, bool transient, double wt,
-                               double *rr, double *D, LawScratch<NJ> &S, int lane)
+                               double *rr, DT *D, LawScratch<NJ> &S, int lane)
 {
   // segment: static -> m = u, delta = 0
   if (lane < 30) {
@@ -241,8 +241,8 @@ __device__ void gradelast_warp(const double *u, const double *par, bool transien
   // tangent rows: lane i owns row i of D
   if (TAN && lane < 30) {
     const int i = lane;
-    double *row = D + 30 * i;
-    for (int j = 0; j < 30; j++) row[j] = 0.0;
+    DT *row = D + 30 * i;
+    for (int j = 0; j < 30; j++) row[j] = (DT)0;
     // collapse of an s-jet of the static tangent to the discrete-gradient Jacobian
     auto collapse = [&](const Jet<NJ> &t) -> double {
       if constexpr (NJ == 1) return t.c[0];
@@ -270,7 +270,7 @@ __device__ void gradelast_warp(const double *u, const double *par, bool transien
           for (int e2 = 0; e2 < S.cnt[d]; e2++) {
             Jet<NJ> gd = jconst<NJ>(S.g0[d][e2]);
             if constexpr (NJ > 1) gd.c[1] = S.g1[d][e2];
-            row[S.idx[d][e2]] += collapse(jmul(dcoef[t], gd));
+            row[S.idx[d][e2]] += (DT)collapse(jmul(dcoef[t], gd));
           }
         }
       }
@@ -281,18 +281,18 @@ __device__ void gradelast_warp(const double *u, const double *par, bool transien
       if (i % 10 == 0 || i % 10 > 3) continue;
       int k = i / 10, col = i % 10 - 1;
       double h = collapse(S.d1[c]);
-      if (col == a) row[10 * k + 1 + b] += 0.5 * h;
-      if (col == b) row[10 * k + 1 + a] += 0.5 * h;
+      if (col == a) row[10 * k + 1 + b] += (DT)(0.5 * h);
+      if (col == b) row[10 * k + 1 + a] += (DT)(0.5 * h);
     }
     for (int c = 6; c < NQM; c++) {
       int a = (c - 6) / 3, mm = (c - 6) % 3;
       double h = collapse(S.d1[c]);
       int k = i / 10, r10 = i % 10;
-      if (r10 == 1 + a) row[10 * k + 4 + sym6(a, mm)] += h;
-      if (r10 == 4 + sym6(a, mm)) row[10 * k + 1 + a] += h;
+      if (r10 == 1 + a) row[10 * k + 4 + sym6(a, mm)] += (DT)h;
+      if (r10 == 4 + sym6(a, mm)) row[10 * k + 1 + a] += (DT)h;
     }
-    if (transient && (i % 10) == 0) row[i] += damp / (2.0 * dt) + rho_m / (dt * dt);
-    for (int j = 0; j < 30; j++) row[j] *= wt;
+    if (transient && (i % 10) == 0) row[i] += (DT)(damp / (2.0 * dt) + rho_m / (dt * dt));
+    for (int j = 0; j < 30; j++) row[j] = (DT)(row[j] * wt);
   }
   __syncwarp();
 }

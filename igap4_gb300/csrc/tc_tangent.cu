@@ -1,0 +1,335 @@
+// Split-precision tangent assembly on the tensor cores (tcgen05, TF32x3).
+//
+// For one element the tangent block of SURVEY's K6 loop,
+//   K[(b,d),(c,e)] = sum_q sum_{k,l} R_q[b,k] w_q D_q[(d,k),(e,l)] R_q[c,l]
+// (src/assmcore_iga.c:722-750), is evaluated as one GEMM per element
+//   K^T[(d,c,e), b] = sum_{(q,k)} A[(d,c,e),(q,k)] B[b,(q,k)]
+//   A[(d,c,e),(q,k)] = sum_l w_q D_q[(d,k),(e,l)] R_q[c,l]      (stage 1, FP32 CUDA cores)
+//   B[b,(q,k)]       = R_q[b,k]
+// with the 243 rows (d,c,e) in two M=128 tiles, N = 32 >= 27 columns b, and
+// the reduction over 64 points x 10 derivative slots in chunks of K = 40
+// (8 points x 5 slots).  Each operand is split into TF32 hi + lo parts and
+// the three products hi.hi + hi.lo + lo.hi accumulate in FP32 in tensor
+// memory; the epilogue reads TMEM and adds into the FP64 CSR values.
+// The residual is not touched here (the FP64 element kernel computes it).
+//
+// One persistent CTA per SM walks the elements of one colour, so the CSR
+// scatter is conflict-free as in the FP64 kernel.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "element.cuh"
+#include "tcgen05.cuh"
+
+namespace igap {
+
+namespace {
+constexpr int TC_THREADS = 256;
+constexpr int KCH = 40;                    // K per chunk: 8 points x 5 slots
+constexpr int NKT = KCH / 8;               // tf32 MMA K-steps per chunk (K = 8 each)
+constexpr int A_TILE = 128 * 8 * 4;        // one (K-step, M-tile) block: 4096 B
+constexpr int A_PIECE = NKT * 2 * A_TILE;  // 40960 B
+constexpr int B_TILE = 32 * 8 * 4;         // 1024 B
+constexpr int B_PIECE = NKT * B_TILE;      // 5120 B
+constexpr uint32_t WAIT_LIMIT = 1u << 26;  // bounded polls of an mbarrier
+constexpr uint32_t TMEM_COLS = 64;
+
+// byte offset of (row r, k index kk8 in [0,8)) inside one 128-row (or 32-row)
+// block of a K-step: K-major, no swizzle, LBO = 128 B, SBO = 256 B
+__device__ __forceinline__ uint32_t kmajor_off(int r, int kk8)
+{
+  return (uint32_t)((r >> 3) * 256 + (kk8 >> 2) * 128 + (r & 7) * 16 + (kk8 & 3) * 4);
+}
+}  // namespace
+
+struct TcSmem {
+  unsigned char A[2 * A_PIECE];  // [piece][kstep][mtile][block]
+  unsigned char B[2 * B_PIECE];  // [piece][kstep][block]
+  uint64_t mbar;
+  uint32_t taddr;
+  int abort;
+  ElemData E;
+  PointScratch Pt[PW];
+  double R[PW][NB * NDD];
+  float Rf[PW][NB * NDD];
+  float Dwf[PW][900];
+};
+
+// ------------------------------------------------------------ self-test
+// D (128 x 32) = A (128 x 16) . B (32 x 16)^T with small integers, two K-steps;
+// variant 0: LBO = 128 / SBO = 256, variant 1: swapped.
+__global__ void tc_selftest_kernel(int variant, float *out, int *err)
+{
+  __shared__ __align__(1024) float sA[2][128 * 8];
+  __shared__ __align__(1024) float sB[2][32 * 8];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t taddr_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(&taddr_s, 32);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  for (int i = tid; i < 128 * 16; i += blockDim.x) {
+    const int r = i / 16, kk = i % 16;
+    sA[kk / 8][kmajor_off(r, kk % 8) / 4] = (float)(((r * 3 + kk * 5) % 7) - 3);
+  }
+  for (int i = tid; i < 32 * 16; i += blockDim.x) {
+    const int n = i / 16, kk = i % 16;
+    sB[kk / 8][kmajor_off(n, kk % 8) / 4] = (float)(((n * 2 + kk * 3) % 5) - 2);
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = taddr_s;
+  const uint32_t lbo = variant == 0 ? 128 : 256, sbo = variant == 0 ? 256 : 128;
+  if (tid == 0) {
+    for (int kt = 0; kt < 2; kt++)
+      tc::mma_tf32(taddr, tc::smem_desc(tc::smem_u32(sA[kt]), lbo, sbo),
+                   tc::smem_desc(tc::smem_u32(sB[kt]), lbo, sbo), tc::instr_desc(2, 128, 32), kt > 0);
+    tc::mma_commit(&mbar);
+  }
+  if (!tc::mbar_wait(&mbar, 0, WAIT_LIMIT)) atomicExch(err, 1);
+  tc::fence_after_sync();
+  if (warp < 4) {
+    uint32_t v[32];
+    tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16), v);
+    for (int j = 0; j < 32; j++) out[(warp * 32 + lane) * 32 + j] = __uint_as_float(v[j]);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, 32);
+}
+
+// ------------------------------------------------------ split tangent
+template <int LAWK>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_tangent_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz,
+                      const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(TcSmem));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&S.mbar, 1);
+    S.abort = 0;
+  }
+  // padding rows (243..255 of A, 27..31 of B) stay zero for the whole kernel
+  for (int i = tid; i < (int)(sizeof(S.A) / 4); i += TC_THREADS) reinterpret_cast<float *>(S.A)[i] = 0.f;
+  for (int i = tid; i < (int)(sizeof(S.B) / 4); i += TC_THREADS) reinterpret_cast<float *>(S.B)[i] = 0.f;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = S.taddr;
+  const uint32_t idesc = tc::instr_desc(2, 128, 32);
+  const uint32_t a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
+  uint32_t commits = 0;  // commits issued so far (uniform across the CTA)
+  const int nh = L.nhist;
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  const int nbv[3] = {m.nbasis[0], nb1, nb2};
+  const int nelem_c = ncx * ncy * ncz;
+  const int nchunk = (m.npts + PW - 1) / PW;
+
+  for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    const int ex = cx + 3 * ix, ey = cy + 3 * iy, ez = cz + 3 * iz;
+    load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, TC_THREADS);
+    __syncthreads();
+    bool first = true;
+    for (int ch = 0; ch < nchunk; ch++) {
+      // phase A: 8 points, one warp each (FP64 geometry, FP32 tangent integrand)
+      point_setup<LAWK, false, true, float>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp,
+                                            ch * PW + warp, lane, S.R[warp], nullptr, S.Dwf[warp]);
+      for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = (float)S.R[warp][i];
+      __syncthreads();
+      for (int kg = 0; kg < 2; kg++) {
+        // the previous chunk's MMAs must be done before A/B are overwritten
+        if (commits > 0) {
+          if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
+        }
+        __syncthreads();
+        if (S.abort) goto done;
+        // stage 1 (rows (d,c,e)) and B (rows b); columns kk = kq*8 + pt
+        if (tid < 243) {
+          const int d = tid / 81, c = (tid % 81) / 3, e = tid % 3;
+          for (int kq = 0; kq < 5; kq++) {
+            const int k = kg * 5 + kq;
+            for (int half = 0; half < 2; half++) {
+              float4 hi, lo;
+              float *ph = &hi.x, *pl = &lo.x;
+              for (int j = 0; j < 4; j++) {
+                const int pt = half * 4 + j;
+                const float *drow = S.Dwf[pt] + 30 * (10 * d + k) + 10 * e;
+                const float *rc = S.Rf[pt] + NDD * c;
+                float s = 0.f;
+#pragma unroll
+                for (int l = 0; l < NDD; l++) s = fmaf(drow[l], rc[l], s);
+                const float h = tc::to_tf32(s);
+                ph[j] = h;
+                pl[j] = tc::to_tf32(s - h);
+              }
+              const int r = tid, mt = r >> 7;
+              const uint32_t off = (uint32_t)((kq * 2 + mt) * A_TILE) + kmajor_off(r & 127, half * 4);
+              *reinterpret_cast<float4 *>(S.A + off) = hi;
+              *reinterpret_cast<float4 *>(S.A + A_PIECE + off) = lo;
+            }
+          }
+        }
+        if (tid < NB) {
+          const int b = tid;
+          for (int kq = 0; kq < 5; kq++) {
+            const int k = kg * 5 + kq;
+            for (int half = 0; half < 2; half++) {
+              float4 hi, lo;
+              float *ph = &hi.x, *pl = &lo.x;
+              for (int j = 0; j < 4; j++) {
+                const float s = S.Rf[half * 4 + j][NDD * b + k];
+                const float h = tc::to_tf32(s);
+                ph[j] = h;
+                pl[j] = tc::to_tf32(s - h);
+              }
+              const uint32_t off = (uint32_t)(kq * B_TILE) + kmajor_off(b, half * 4);
+              *reinterpret_cast<float4 *>(S.B + off) = hi;
+              *reinterpret_cast<float4 *>(S.B + B_PIECE + off) = lo;
+            }
+          }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+          tc::fence_after_sync();
+          for (int kt = 0; kt < NKT; kt++)
+            for (int mt = 0; mt < 2; mt++)
+              for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
+                const int pa = (pp == 2) ? 1 : 0, pb = (pp == 1) ? 1 : 0;
+                const uint64_t ad = tc::smem_desc(a_base + pa * A_PIECE + (kt * 2 + mt) * A_TILE, 128, 256);
+                const uint64_t bd = tc::smem_desc(b_base + pb * B_PIECE + kt * B_TILE, 128, 256);
+                const uint32_t acc = (first && kt == 0 && pp == 0) ? 0u : 1u;
+                tc::mma_tf32(taddr + (uint32_t)(mt * 32), ad, bd, idesc, acc);
+              }
+          tc::mma_commit(&S.mbar);
+        }
+        commits++;
+        first = false;
+      }
+      __syncthreads();  // Rf / Dwf of this chunk are no longer read after the next wait
+    }
+    // epilogue: wait for the element's last MMAs, read TMEM, scatter
+    if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
+    tc::fence_after_sync();
+    __syncthreads();
+    if (S.abort) goto done;
+    if (warp < 4) {
+      for (int mt = 0; mt < 2; mt++) {
+        uint32_t v[32];
+        tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * 32), v);
+        const int r = mt * 128 + warp * 32 + lane;
+        if (r < 243) {
+          const int d = r / 81, c = (r % 81) / 3, e = r % 3;
+          const int sx = ex + c / 9, sy = ey + (c / 3) % 3, sz = ez + c % 3;
+          const int64_t cpc = ((int64_t)sx * nb1 + sy) * nb2 + sz;
+          for (int b = 0; b < NB; b++) {
+            const int rx = ex + b / 9, ry = ey + (b / 3) % 3, rz = ez + b % 3;
+            const int64_t cpb = ((int64_t)rx * nb1 + ry) * nb2 + rz;
+            const int64_t pos = stencil_pos(rx, ry, rz, sx, sy, sz, nbv);
+            vals[m.rowptr[3 * cpb + d] + 3 * pos + e] += (double)__uint_as_float(v[b]);
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+done:
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort && tid == 0) atomicExch(err, 2);
+  if (warp == 0) tc::tmem_dealloc(taddr, TMEM_COLS);
+}
+
+template <int LAWK>
+static int run_tc(Context *c, double *vals)
+{
+  const DevMesh m = c->devmesh();
+  const DevLaw L = c->devlaw();
+  const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
+  auto kern = tc_tangent_kernel<LAWK>;
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  for (int cx = 0; cx < 3; cx++)
+    for (int cy = 0; cy < 3; cy++)
+      for (int cz = 0; cz < 3; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        const int nel = ncx * ncy * ncz;
+        if (nel <= 0) continue;
+        const int grid = nel < nsm ? nel : nsm;
+        kern<<<grid, TC_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, c->d_Uhist, vals,
+                                                    c->d_err);
+        count_launch();
+        IGAP_CHECK_LAUNCH();
+        if (c->prof) {
+          c->prof_launches++;
+          c->prof_elements += nel;
+        }
+      }
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev.emplace_back(e0, e1);
+  }
+  return IGAPGPU_OK;
+}
+
+int launch_tc_tangent(Context *c, double *vals)
+{
+  if (c->law == IGAPGPU_LAW_LINGRAD) return run_tc<0>(c, vals);
+  if (c->law == IGAPGPU_LAW_GRADELAST) return run_tc<1>(c, vals);
+  if (c->law == IGAPGPU_LAW_GRADELASTTIME) return run_tc<2>(c, vals);
+  set_error("unknown law %d", c->law);
+  return IGAPGPU_ERR_LAW;
+}
+
+}  // namespace igap
+
+using namespace igap;
+
+extern "C" int igapgpu_tc_selftest(int variant, float *out)
+{
+  float *d_out = nullptr;
+  int *d_err = nullptr;
+  IGAP_CUDA(cudaMalloc(&d_out, sizeof(float) * 128 * 32));
+  IGAP_CUDA(cudaMalloc(&d_err, sizeof(int)));
+  IGAP_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+  tc_selftest_kernel<<<1, 128>>>(variant, d_out, d_err);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  int herr = 0;
+  IGAP_CUDA(cudaMemcpy(out, d_out, sizeof(float) * 128 * 32, cudaMemcpyDeviceToHost));
+  IGAP_CUDA(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  cudaFree(d_out);
+  cudaFree(d_err);
+  if (herr) {
+    set_error("tcgen05 self-test: mbarrier wait timed out");
+    return IGAPGPU_ERR_TIMEOUT;
+  }
+  return IGAPGPU_OK;
+}

@@ -186,6 +186,12 @@ int64_t igapgpu_launch_count(void);
 int igapgpu_profile(igapgpu_t ctx, int enable);
 int igapgpu_profile_read(igapgpu_t ctx, double *elem_ms, int64_t *launches, int64_t *elements);
 
+/* Tensor-core self-test: D (128 x 32) = A (128 x 16) . B (32 x 16)^T of small
+ * integers through tcgen05.mma kind::tf32 with the operand layout of the
+ * split-precision tangent (variant 0) or with LBO/SBO swapped (variant 1).
+ * out: 4096 floats on the host, row-major. */
+int igapgpu_tc_selftest(int variant, float *out);
+
 /* Measured FP64 FMA throughput of this GPU (TFLOP/s) from a register-only
  * kernel; used as the denominator of FP64-bound roofline fractions. */
 int igapgpu_measure_fp64_peak(double *tflops);

@@ -1,0 +1,70 @@
+"""Tensor-core (tcgen05, TF32x3) split-precision tangent.
+
+* the tcgen05 self-test GEMM reproduces an exact integer product;
+* the split tangent agrees with the FP64 tangent within the stated bound
+  (relative 2-norm error <= 2e-6; TF32 hi+lo operands keep ~21 bits, the
+  FP32 tensor-memory accumulation adds ~1e-7), for all three laws;
+* the residual of the split mode is the FP64 residual, unchanged.
+"""
+import numpy as np
+import pytest
+
+import igap4_gb300 as ig
+import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_TOL = 2e-6
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_tcgen05_selftest_exact():
+    D, E = ig.tc_selftest(0)
+    assert np.array_equal(D, E), f"max |D-E| = {np.abs(D - E).max()}"
+
+
+@pytest.mark.parametrize("law,nelem,perturb", [
+    (po.LAW_LINGRAD, (8, 4, 3), False),
+    (po.LAW_GRADELAST, (4, 4, 4), True),
+    (po.LAW_GRADELASTTIME, (3, 3, 4), False),
+])
+def test_split_tangent_vs_fp64(law, nelem, perturb):
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=nelem, law=law, perturb=perturb, bc_type=bct, neumann=neu)
+    U = po.random_state(prob, 77)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L, prob.p, prob.perturb)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=law, par=prob.params(), bc_type=bct, neumann=neu)
+    A.set_state(U)
+    K64 = A.tangent()
+    R64 = A.residual()
+    A.set_precision(ig.PREC_SPLIT)
+    Ks = A.tangent()
+    Rs = A.residual()
+    e = rel(Ks, K64)
+    print(f"split tangent rel err {e:.3e}")
+    assert e <= SPLIT_TOL
+    np.testing.assert_array_equal(Rs, R64)
+    # fused assemble in split mode = FP64 residual + split tangent
+    RR = np.zeros(A.ndof)
+    V = np.zeros(A.nnz)
+    A.assemble(None, RR, V)
+    np.testing.assert_array_equal(RR, R64)
+    assert rel(V, K64) <= SPLIT_TOL
+
+
+def test_split_newton_converges_to_fp64_tolerance():
+    """Inexact (split) Jacobian, exact FP64 residual: Newton still reaches the
+    FP64 residual tolerance."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=(16, 4, 4), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, bc_type=bct, neumann=neu)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=prob.law, par=prob.params(), bc_type=bct, neumann=neu)
+    A.set_precision(ig.PREC_SPLIT)
+    U = np.zeros(A.ndof)
+    st = A.solve(U, snes_abstol=1e-10, ksp_rtol=1e-10, ksp_restart=300, ksp_max_it=50000, snes_max_it=20)
+    assert st["converged"] == 1, st
+    orc = po.OracleCase(prob)
+    assert np.linalg.norm(orc.residual(U[None, :])) <= 1e-9
