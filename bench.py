@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--nelem", default="128,32,32")
-    ap.add_argument("--prec", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--prec", default="both", choices=["fp64", "split", "both"],
+                    help="both: FP64 headline plus the split (tensor-core) mode")
     ap.add_argument("--spmv", type=int, default=200, help="SpMV repetitions")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -130,6 +131,13 @@ def run_reference(a):
 
 
 # ------------------------------------------------------------------ GPU
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
 class ClockSampler:
     def __init__(self, path=None):
         self.samples = []
@@ -210,7 +218,6 @@ def main():
     bct, neu = ig.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     knots, w, X = ig.beam_mesh(nelem, LBEAM)
     A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD, par=LAW_PAR, bc_type=bct, neumann=neu)
-    A.set_precision(ig.PREC_SPLIT if a.prec == "split" else ig.PREC_FP64)
     stream = torch.cuda.Stream(device=dev)
     A.set_stream(stream.cuda_stream)
     rng = np.random.default_rng(SEED + rank)
@@ -221,41 +228,78 @@ def main():
     def step():
         A.assemble(U, RR, None)  # residual + tangent into the context matrix
 
-    with torch.cuda.stream(stream):
-        for _ in range(a.warmup):
-            step()
-    torch.cuda.synchronize()
+    def measure(prec, steps, warmup):
+        A.set_precision(prec)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                step()
+        torch.cuda.synchronize()
+        launches0 = ig.launch_count()
+        A.profile(True)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                flush.fill_(float(k))  # L2 flush, outside the events
+                evs[k][0].record(stream)
+                step()
+                evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        launches = ig.launch_count() - launches0
+        kinds = {kd: A.profile_read(kd) for kd in (0, 1)}
+        A.profile(False)
+        step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+        dev_ms = sum(step_ms)
+        if world > 1:
+            t = torch.tensor([dev_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            dev_ms = t.item()
+        return dev_ms / steps, step_ms, kinds, launches
 
     sampler = ClockSampler()
     sampler.start()
-    launches0 = ig.launch_count()
-    A.profile(True)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     t_wall0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for k in range(a.steps):
-            flush.fill_(float(k))  # L2 flush, outside the events
-            evs[k][0].record(stream)
-            step()
-            evs[k][1].record(stream)
-    torch.cuda.synchronize()
+    fp64_prec = ig.PREC_FP64
+    headline_prec = ig.PREC_SPLIT if a.prec == "split" else fp64_prec
+    ms_per_step, step_ms, kinds, launches = measure(headline_prec, a.steps, a.warmup)
     t_wall = time.perf_counter() - t_wall0
-    if world > 1:
-        torch.distributed.barrier()
-    launches = ig.launch_count() - launches0
-    elem_ms, elem_launches, elem_count = A.profile_read()
-    A.profile(False)
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    dev_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([dev_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = t.item()
-    ms_per_step = dev_ms / a.steps
     value = world * A.nelem_total / (ms_per_step * 1e-3)
+    elem_ms, elem_launches, elem_count = kinds[0] if headline_prec == fp64_prec else kinds[1]
+    dev_ms = ms_per_step * a.steps
+
+    split = None
+    if a.prec == "both":
+        # split mode: same step, tangent on the tensor cores; error vs FP64 at full size
+        sms, sstep, skinds, slaunch = measure(ig.PREC_SPLIT, a.steps, max(1, a.warmup - 1))
+        A.set_precision(ig.PREC_FP64)
+        K64 = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
+        A.tangent(U, K64)
+        A.set_precision(ig.PREC_SPLIT)
+        Ks = torch.zeros_like(K64)
+        A.tangent(U, Ks)
+        A.synchronize()
+        err = (torch.linalg.norm(Ks - K64) / torch.linalg.norm(K64)).item()
+        del K64, Ks
+        tc_ms, tc_l, tc_e = skinds[1]
+        res_ms, res_l, res_e = skinds[0]
+        tc_flop = TAN_FLOP_PER_ELEM * tc_e / max(tc_l, 1)
+        tc_ach = tc_flop / (tc_ms / max(tc_l, 1) * 1e-3) / 1e12
+        bf16_peak = peaks.get("bf16_tflops", 1900.0) if (peaks := _peaks()) else 1900.0
+        split = {"value": world * A.nelem_total / (sms * 1e-3), "unit": "elements/s",
+                 "ms_per_step": sms, "step_ms": sstep, "gpu_launches": slaunch,
+                 "tangent_rel_err_vs_fp64": err, "dtype": "tf32x3/f32-acc tangent, f64 residual",
+                 "tc_kernel_ms_per_step": tc_ms / a.steps, "fp64_residual_kernel_ms_per_step": res_ms / a.steps,
+                 "roofline": {"bound": "tensor", "kernel": "tc_tangent_kernel (tcgen05.mma kind::tf32, TF32x3)",
+                              "achieved": tc_ach, "peak": bf16_peak, "unit": "TFLOP/s",
+                              "frac": tc_ach / bf16_peak,
+                              "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense TF32 is half of it)",
+                              "algorithmic_flop_per_element": TAN_FLOP_PER_ELEM}}
+        A.set_precision(headline_prec)
 
     # e2e through the C ABI with pinned host buffers
     Uh = torch.empty(A.ndof, dtype=torch.float64, pin_memory=True)
@@ -286,17 +330,14 @@ def main():
     spmv_bytes = A.nnz * (8 + 4) + (A.ndof + 1) * 8 + 2 * A.ndof * 8
     sampler.stop()
 
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = _peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = ig.measure_fp64_peak()
     elem_kernel_ms = elem_ms / max(elem_launches, 1)
     flop_per_launch = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) * elem_count / max(elem_launches, 1)
     achieved = flop_per_launch / (elem_kernel_ms * 1e-3) / 1e12
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "traffic_note": "FP64-bound: DRAM traffic is negligible (see profiles/)",
                 "frac": achieved / fp64_peak, "traffic": None,
                 "kernel": "element_kernel (fused residual+tangent, FP64)",
                 "peak_source": "measured in-run FP64 FMA throughput (MEASURED_PEAKS.json has no FP64 figure)",
@@ -309,14 +350,15 @@ def main():
             "metric": "assembled elements/s (tangent+residual)", "value": value, "unit": "elements/s",
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if a.prec == "fp64" else "bf16x3-split/f32-acc+f64",
+            "dtype": "f64" if a.prec != "split" else "tf32x3/f32-acc tangent, f64 residual",
             "data": "synthetic",
             "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} "
                                    f"({A.nelem_total} elements, {A.ndof} DOF, nnz {A.nnz}) "
                                    "residual Vec + CSR tangent assembly",
                        "law": "linear isotropic strain gradient lambda=1 mu=1 ell=0.1",
                        "quadrature": "4x4x4 Gauss", "bc": "clamped x=0, traction 1e-3 in -z at x=4",
-                       "state": "seeded uniform [-1e-2,1e-2] per DOF", "precision": a.prec,
+                       "state": "seeded uniform [-1e-2,1e-2] per DOF",
+                       "precision": "fp64" if a.prec != "split" else "split",
                        "l2": "flushed (256 MiB write) before every timed step; the 1.25 GB CSR output also exceeds L2",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": A.ndof * 8,
@@ -328,6 +370,7 @@ def main():
                      "frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / hbm_peak, "bytes": spmv_bytes,
                      "repetitions": a.spmv},
             "cpu_baseline": cpu,
+            "split": split,
             "clocks": sampler.summary(local),
             "step_ms": step_ms,
             "wall_s": t_wall,

@@ -92,12 +92,14 @@ def lib():
         L.igapgpu_default_solver_opts.argtypes = [ctypes.POINTER(SolverOpts)]
         L.igapgpu_default_solver_opts.restype = None
         L.igapgpu_set_precision.argtypes = [vp, ctypes.c_int]
+        L.igapgpu_set_neumann.argtypes = [vp, vp]
         L.igapgpu_set_stream.argtypes = [vp, vp]
         L.igapgpu_synchronize.argtypes = [vp]
         L.igapgpu_last_error.restype = ctypes.c_char_p
         L.igapgpu_launch_count.restype = ctypes.c_int64
         L.igapgpu_profile.argtypes = [vp, ctypes.c_int]
         L.igapgpu_profile_read.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_profile_read_kind.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.igapgpu_measure_fp64_peak.argtypes = [vp]
         L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
         _lib = L
@@ -288,6 +290,11 @@ class Assembly:
         _check(lib().igapgpu_solve(self.h, _ptr(U), ctypes.byref(o), ctypes.byref(st)))
         return {f: getattr(st, f) for f, _ in SolveStats._fields_}
 
+    def set_neumann(self, table):
+        """New constant traction table (36 entries); recomputes the Neumann load."""
+        t = np.ascontiguousarray(table, np.float64)
+        _check(lib().igapgpu_set_neumann(self.h, _ptr(t)))
+
     def set_precision(self, mode):
         _check(lib().igapgpu_set_precision(self.h, mode))
 
@@ -301,10 +308,13 @@ class Assembly:
     def profile(self, enable=True):
         _check(lib().igapgpu_profile(self.h, int(enable)))
 
-    def profile_read(self):
+    def profile_read(self, kind=-1):
+        """(ms, launches, elements) of the timed element kernels; kind 0 = FP64
+        element kernel, 1 = tensor-core tangent kernel, -1 = both."""
         ms = ctypes.c_double()
         nl, ne = ctypes.c_int64(), ctypes.c_int64()
-        _check(lib().igapgpu_profile_read(self.h, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ne)))
+        _check(lib().igapgpu_profile_read_kind(self.h, kind, ctypes.byref(ms), ctypes.byref(nl),
+                                               ctypes.byref(ne)))
         return ms.value, nl.value, ne.value
 
 

@@ -212,6 +212,57 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// ------------------------------------------------------ geometry cache
+// State-independent per-point geometry: physical basis R (value, gradient,
+// Hessian of the 27 rational basis functions) and the quadrature weight.
+__global__ void __launch_bounds__(256) geometry_cache_kernel(DevMesh m, double *geo)
+{
+  __shared__ ElemData E;
+  __shared__ PointScratch Pt[8];
+  __shared__ double R[8][NB * NDD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t e = blockIdx.x;
+  const int ez = (int)(e % m.nelem[2]), ey = (int)((e / m.nelem[2]) % m.nelem[1]),
+            ex = (int)(e / ((int64_t)m.nelem[1] * m.nelem[2]));
+  load_element(E, m, 0, nullptr, ex, ey, ez, tid, 256);
+  __syncthreads();
+  for (int q = warp; q < m.npts; q += 8) {
+    const double wt = point_geometry(E, Pt[warp], m, ex, ey, ez, q, lane, R[warp]);
+    double *g = geo + (e * m.npts + q) * GEO_STRIDE;
+    for (int i = lane; i < NB * NDD; i += 32) g[i] = R[warp][i];
+    if (lane == 0) {
+      g[NB * NDD] = wt;
+      g[NB * NDD + 1] = 0.0;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void geometry_f32_kernel(const double *geo, float *geof, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    geof[i] = (float)geo[i];
+}
+
+int launch_geometry_cache_f32(Context *c)
+{
+  const int64_t n = c->nelem_total * (int64_t)c->nquad * c->nquad * c->nquad * GEO_STRIDE;
+  geometry_f32_kernel<<<152 * 16, 256, 0, c->stream>>>(c->d_geo, c->d_geof, n);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+int launch_geometry_cache(Context *c)
+{
+  DevMesh m = c->devmesh();
+  m.geo = nullptr;
+  geometry_cache_kernel<<<(unsigned)c->nelem_total, 256, 0, c->stream>>>(m, c->d_geo);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
 // ----------------------------------------------------------- Neumann
 // One thread per face control point of one face; both orders and all dofs.
 __global__ void neumann_kernel(int face, const int *bc_type, const double *neumann,
@@ -317,13 +368,13 @@ static int run_colours(Context *c, double *RR, double *vals)
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
-          c->prof_launches++;
-          c->prof_elements += nblk;
+          c->prof_launches[0]++;
+          c->prof_elements[0] += nblk;
         }
       }
   if (c->prof) {
     IGAP_CUDA(cudaEventRecord(e1, c->stream));
-    c->prof_ev.emplace_back(e0, e1);
+    c->prof_ev[0].emplace_back(e0, e1);
   }
   return IGAPGPU_OK;
 }
@@ -435,10 +486,12 @@ int launch_pattern_cols(Context *c)
 
 int launch_neumann(Context *c, const double nfac[NFACE][2])
 {
-  int *d_bct = nullptr;
-  double *d_neu = nullptr;
-  IGAP_CUDA(cudaMalloc(&d_bct, 36 * sizeof(int)));
-  IGAP_CUDA(cudaMalloc(&d_neu, 36 * sizeof(double)));
+  if (!c->d_bct) {
+    IGAP_CUDA(cudaMalloc(&c->d_bct, 36 * sizeof(int)));
+    IGAP_CUDA(cudaMalloc(&c->d_neu, 36 * sizeof(double)));
+  }
+  int *d_bct = c->d_bct;
+  double *d_neu = c->d_neu;
   IGAP_CUDA(cudaMemcpyAsync(d_bct, c->bc.bc_type, 36 * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   IGAP_CUDA(cudaMemcpyAsync(d_neu, c->bc.neumann, 36 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   IGAP_CUDA(cudaMemsetAsync(c->d_Fneu, 0, sizeof(double) * c->ndof, c->stream));
@@ -460,8 +513,6 @@ int launch_neumann(Context *c, const double nfac[NFACE][2])
     IGAP_CHECK_LAUNCH();
   }
   IGAP_CUDA(cudaStreamSynchronize(c->stream));
-  IGAP_CUDA(cudaFree(d_bct));
-  IGAP_CUDA(cudaFree(d_neu));
   return IGAPGPU_OK;
 }
 

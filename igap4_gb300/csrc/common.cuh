@@ -52,6 +52,8 @@ struct DevMesh {
   const double *X;         // [3*ncp]
   const int64_t *rowptr;   // [ndof+1]
   int64_t ndof;
+  const double *geo;       // geometry cache [nelem][npts][272] or null
+  const float *geof;       // FP32 copy of the geometry cache (split tangent) or null
 };
 
 struct DevLaw {
@@ -59,6 +61,15 @@ struct DevLaw {
   int nhist;               // torder + 1
   double par[9];
   const double *Dconst;    // 900 constant tangent of a linear law (or null)
+  // sparse form of Dconst: rows (CSR) for the residual, and per (d,k,e)
+  // segments (entries l with D[(d,k),(e,l)] != 0) for the split tangent
+  const int *dptr;         // [31]
+  const int *dcol;         // [nnz]
+  const double *dval;      // [nnz]
+  const int *sptr;         // [91]
+  const int *sl;           // [nnz]
+  const float *sval;       // [nnz]
+  int dnnz;
 };
 
 struct Context {
@@ -68,6 +79,8 @@ struct Context {
   int nelem[3], nbasis[3];
   int64_t ndof, nnz, nelem_total, ncp;
   igapgpu_bc_desc bc;
+  std::vector<double> h_knots[3];  // host copies of the knot vectors (boundary data)
+  double nfac[6][2];               // Neumann normal-derivative factors of the two boundary layers
   // device buffers
   double *d_tab[3] = {nullptr, nullptr, nullptr};
   double *d_tabn[3] = {nullptr, nullptr, nullptr}; // plain Cox-de Boor (face integrals)
@@ -82,6 +95,14 @@ struct Context {
   double *d_Dconst = nullptr;  // [900]
   double *d_Fneu = nullptr;    // [ndof] Neumann load (state independent)
   int *d_err = nullptr;        // device error word (bounded waits that expired)
+  int *d_bct = nullptr;        // bc_type table on the device [36]
+  double *d_neu = nullptr;     // traction table on the device [36]
+  double *d_geo = nullptr;     // geometry cache (physical basis + weight per point)
+  float *d_geof = nullptr;     // FP32 copy for the split-precision tangent
+  int *d_dsparse = nullptr;    // sparse constant tangent: dptr | dcol | sptr | sl
+  double *d_dval = nullptr;
+  float *d_sval = nullptr;
+  int dnnz = 0;
   int64_t n_dir = 0;           // Dirichlet rows (unique, last writer wins)
   int64_t *d_dir_rows = nullptr;
   double *d_dir_g = nullptr;
@@ -102,8 +123,9 @@ struct Context {
   cudaStream_t stream = nullptr;
   // element-kernel timing (igapgpu_profile)
   bool prof = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev;
-  int64_t prof_launches = 0, prof_elements = 0;
+  // per kernel kind: 0 = FP64 element kernel, 1 = tensor-core tangent kernel
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[2];
+  int64_t prof_launches[2] = {0, 0}, prof_elements[2] = {0, 0};
 
   DevMesh devmesh() const {
     DevMesh m;
@@ -119,6 +141,8 @@ struct Context {
     m.X = d_X;
     m.rowptr = d_rowptr;
     m.ndof = ndof;
+    m.geo = d_geo;
+    m.geof = d_geof;
     return m;
   }
   DevLaw devlaw() const {
@@ -127,6 +151,13 @@ struct Context {
     l.nhist = torder + 1;
     for (int i = 0; i < 9; i++) l.par[i] = par[i];
     l.Dconst = d_Dconst;
+    l.dnnz = dnnz;
+    l.dptr = d_dsparse;
+    l.dcol = d_dsparse ? d_dsparse + 31 : nullptr;
+    l.sptr = d_dsparse ? d_dsparse + 31 + dnnz : nullptr;
+    l.sl = d_dsparse ? d_dsparse + 31 + dnnz + 91 : nullptr;
+    l.dval = d_dval;
+    l.sval = d_sval;
     return l;
   }
 };
@@ -142,6 +173,8 @@ int launch_neumann(Context *c, const double nfac[NFACE][2]);
 int launch_dirichlet_matrix(Context *c, double *vals);
 int launch_dirichlet_residual(Context *c, double *RR);
 int launch_pattern_cols(Context *c);
+int launch_geometry_cache(Context *c);
+int launch_geometry_cache_f32(Context *c);
 // tc_tangent.cu
 int launch_tc_tangent(Context *c, double *vals);
 // krylov.cu

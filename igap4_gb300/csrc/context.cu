@@ -162,7 +162,7 @@ static int free_ctx(Context *c)
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
-                  c->d_diag, c->d_red, c->d_partial, c->d_err};
+                  c->d_diag, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int d = 0; d < 3; d++) {
@@ -231,6 +231,33 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   IGAP_CUDA(cudaMemcpy(c->d_xq, xq, sizeof(double) * c->nquad, cudaMemcpyHostToDevice));
   IGAP_CUDA(cudaMemcpy(c->d_wq, wq, sizeof(double) * c->nquad, cudaMemcpyHostToDevice));
   if ((r = launch_basis_tables(c))) return r;
+  // geometry cache: built once when it fits (leaving headroom for the matrix
+  // and the Krylov workspace); IGAPGPU_GEOMETRY_CACHE=0 disables it
+  {
+    const char *env = getenv("IGAPGPU_GEOMETRY_CACHE");
+    const bool want = !(env && env[0] == '0');
+    const size_t npts = (size_t)c->nquad * c->nquad * c->nquad;
+    const size_t bytes = sizeof(double) * (size_t)c->nelem_total * npts * (NB * NDD + 2);
+    size_t freeb = 0, totb = 0;
+    IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
+    const size_t need_other = (size_t)(3 * c->ncp) * 8 * 400;  // matrix, pattern, workspace (rough)
+    if (want && bytes + need_other + ((size_t)4 << 30) < freeb) {
+      if (cudaMalloc(&c->d_geo, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        c->d_geo = nullptr;
+      } else if ((r = launch_geometry_cache(c))) {
+        return r;
+      } else if (bytes / 2 + need_other + ((size_t)4 << 30) < freeb - bytes) {
+        // FP32 copy used by the split-precision tangent
+        if (cudaMalloc(&c->d_geof, bytes / 2) != cudaSuccess) {
+          cudaGetLastError();
+          c->d_geof = nullptr;
+        } else if ((r = launch_geometry_cache_f32(c))) {
+          return r;
+        }
+      }
+    }
+  }
   // CSR row offsets (setnz_iga, src/assmcore_iga.c:1074-1086, one rank)
   std::vector<int64_t> rowptr(c->ndof + 1);
   rowptr[0] = 0;
@@ -271,10 +298,40 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   if (c->law == IGAPGPU_LAW_LINGRAD) {
     if ((r = dev_alloc(&c->d_Dconst, 900))) return r;
     if ((r = launch_lingrad_dconst(c))) return r;
+    // sparse form of the constant tangent (exact zeros skipped)
+    double D[900];
+    IGAP_CUDA(cudaMemcpy(D, c->d_Dconst, sizeof D, cudaMemcpyDeviceToHost));
+    std::vector<int> dptr(31, 0), dcol, sptr(91, 0), sl;
+    std::vector<double> dval;
+    std::vector<float> sval;
+    for (int i = 0; i < 30; i++) {
+      for (int j = 0; j < 30; j++)
+        if (D[30 * i + j] != 0.0) { dcol.push_back(j); dval.push_back(D[30 * i + j]); }
+      dptr[i + 1] = (int)dcol.size();
+    }
+    for (int i = 0; i < 30; i++)
+      for (int e = 0; e < 3; e++) {
+        for (int l = 0; l < 10; l++)
+          if (D[30 * i + 10 * e + l] != 0.0) { sl.push_back(l); sval.push_back((float)D[30 * i + 10 * e + l]); }
+        sptr[3 * i + e + 1] = (int)sl.size();
+      }
+    c->dnnz = (int)dcol.size();
+    std::vector<int> packed;
+    packed.insert(packed.end(), dptr.begin(), dptr.end());
+    packed.insert(packed.end(), dcol.begin(), dcol.end());
+    packed.insert(packed.end(), sptr.begin(), sptr.end());
+    packed.insert(packed.end(), sl.begin(), sl.end());
+    if ((r = dev_alloc(&c->d_dsparse, packed.size()))) return r;
+    if ((r = dev_alloc(&c->d_dval, dval.size()))) return r;
+    if ((r = dev_alloc(&c->d_sval, sval.size()))) return r;
+    IGAP_CUDA(cudaMemcpy(c->d_dsparse, packed.data(), sizeof(int) * packed.size(), cudaMemcpyHostToDevice));
+    IGAP_CUDA(cudaMemcpy(c->d_dval, dval.data(), sizeof(double) * dval.size(), cudaMemcpyHostToDevice));
+    IGAP_CUDA(cudaMemcpy(c->d_sval, sval.data(), sizeof(float) * sval.size(), cudaMemcpyHostToDevice));
   }
   // Neumann load (state independent): normal-derivative factors of the two
   // boundary layers, evalN(k=1) at the face coordinate (src/assmcore_iga.c:384-387)
-  double nfac[NFACE][2];
+  double (&nfac)[NFACE][2] = c->nfac;
+  for (int d = 0; d < 3; d++) c->h_knots[d] = kn[d];
   for (int face = 0; face < NFACE; face++) {
     int da, db, dn;
     face_dirs(face, da, db, dn);
@@ -550,6 +607,13 @@ int igapgpu_matmult(igapgpu_t c, const double *x, double *y)
   return IGAPGPU_OK;
 }
 
+int igapgpu_set_neumann(igapgpu_t c, const double *table)
+{
+  if (!c || !table) return IGAPGPU_ERR_ARG;
+  for (int i = 0; i < 36; i++) c->bc.neumann[i] = table[i];
+  return launch_neumann(c, c->nfac);
+}
+
 int igapgpu_set_precision(igapgpu_t c, int mode)
 {
   if (!c) return IGAPGPU_ERR_ARG;
@@ -573,31 +637,45 @@ int igapgpu_profile(igapgpu_t c, int enable)
   if (!c) return IGAPGPU_ERR_ARG;
   if (enable) {
     IGAP_CUDA(cudaStreamSynchronize(c->stream));
-    for (auto &p : c->prof_ev) {
-      cudaEventDestroy(p.first);
-      cudaEventDestroy(p.second);
+    for (int k = 0; k < 2; k++) {
+      for (auto &p : c->prof_ev[k]) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+      }
+      c->prof_ev[k].clear();
+      c->prof_launches[k] = c->prof_elements[k] = 0;
     }
-    c->prof_ev.clear();
-    c->prof_launches = c->prof_elements = 0;
   }
   c->prof = enable != 0;
   return IGAPGPU_OK;
 }
 
-int igapgpu_profile_read(igapgpu_t c, double *elem_ms, int64_t *launches, int64_t *elements)
+int igapgpu_profile_read_kind(igapgpu_t c, int kind, double *elem_ms, int64_t *launches,
+                              int64_t *elements)
 {
-  if (!c) return IGAPGPU_ERR_ARG;
+  if (!c || kind < -1 || kind > 1) return IGAPGPU_ERR_ARG;
   IGAP_CUDA(cudaStreamSynchronize(c->stream));
   double ms = 0.0;
-  for (auto &p : c->prof_ev) {
-    float t = 0.f;
-    IGAP_CUDA(cudaEventElapsedTime(&t, p.first, p.second));
-    ms += t;
+  int64_t nl = 0, ne = 0;
+  for (int k = 0; k < 2; k++) {
+    if (kind >= 0 && k != kind) continue;
+    for (auto &p : c->prof_ev[k]) {
+      float t = 0.f;
+      IGAP_CUDA(cudaEventElapsedTime(&t, p.first, p.second));
+      ms += t;
+    }
+    nl += c->prof_launches[k];
+    ne += c->prof_elements[k];
   }
   if (elem_ms) *elem_ms = ms;
-  if (launches) *launches = c->prof_launches;
-  if (elements) *elements = c->prof_elements;
+  if (launches) *launches = nl;
+  if (elements) *elements = ne;
   return IGAPGPU_OK;
+}
+
+int igapgpu_profile_read(igapgpu_t c, double *elem_ms, int64_t *launches, int64_t *elements)
+{
+  return igapgpu_profile_read_kind(c, -1, elem_ms, launches, elements);
 }
 
 int igapgpu_synchronize(igapgpu_t c)

@@ -7,6 +7,7 @@
 namespace igap {
 
 constexpr int PW = 8;  // points per chunk (one warp each)
+constexpr int GEO_STRIDE = NB * NDD + 2;  // cached R (270), weight, pad
 
 // Element data in shared memory: weights, control points, state levels.
 struct ElemData {
@@ -69,22 +70,13 @@ __device__ __forceinline__ int64_t stencil_pos(int ix, int iy, int iz, int jx, i
 }
 
 // Phase A for one point, executed by one warp.
-// Outputs: R[27*10] physical basis, rr[30] weighted residual integrand,
-// D[900] weighted tangent integrand (DT = double, or float for the split mode).
-template <int LAWK, bool RES, bool TAN, typename DT>
-__device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &LS, const DevMesh &m,
-                            const DevLaw &L, int ex, int ey, int ez, int w, int q, int lane,
-                            double *R, double *rr, DT *D)
+// Geometry of one quadrature point q (< npts) of element (ex,ey,ez), by one
+// warp: physical basis R[27*10] (value, gradient, Hessian of every rational
+// basis function) and the returned quadrature weight w_q * |span| * detG.
+__device__ inline double point_geometry(const ElemData &E, PointScratch &P, const DevMesh &m, int ex,
+                                        int ey, int ez, int q, int lane, double *R)
 {
-  const double *__restrict__ Dconst = L.Dconst;
   const int nq = m.nquad;
-  if (q >= m.npts) {  // padding point of an incomplete chunk: no contribution
-    for (int i = lane; i < NB * NDD; i += 32) R[i] = 0.0;
-    if (RES) for (int i = lane; i < 30; i += 32) rr[i] = 0.0;
-    if (TAN) for (int i = lane; i < 900; i += 32) D[i] = (DT)0;
-    __syncwarp();
-    return;
-  }
   const int qx = q / (nq * nq), qy = (q / nq) % nq, qz = q % nq;
   const double *tx = m.tab[0] + ((size_t)ex * nq + qx) * TAB;
   const double *ty = m.tab[1] + ((size_t)ey * nq + qy) * TAB;
@@ -178,9 +170,39 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
       }
   }
   __syncwarp();
+  return m.wq[qx] * m.wq[qy] * m.wq[qz] * tx[3 * P1 + 1] * ty[3 * P1 + 1] * tz[3 * P1 + 1] * detG;
+}
+
+// Outputs: R[27*10] physical basis, rr[30] weighted residual integrand,
+// D[900] weighted tangent integrand (DT = double, or float for the split mode).
+// With a geometry cache (m.geo) R and the weight are read, not recomputed.
+template <int LAWK, bool RES, bool TAN, typename DT>
+__device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &LS, const DevMesh &m,
+                            const DevLaw &L, int ex, int ey, int ez, int w, int q, int lane,
+                            double *R, double *rr, DT *D)
+{
+  const double *__restrict__ Dconst = L.Dconst;
+  if (q >= m.npts) {  // padding point of an incomplete chunk: no contribution
+    for (int i = lane; i < NB * NDD; i += 32) R[i] = 0.0;
+    if (RES) for (int i = lane; i < 30; i += 32) rr[i] = 0.0;
+    if (TAN) for (int i = lane; i < 900; i += 32) D[i] = (DT)0;
+    __syncwarp();
+    return;
+  }
+  double wt;
+  if (m.geo) {
+    const int64_t e = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+    const double *g = m.geo + (e * m.npts + q) * GEO_STRIDE;
+    for (int i = lane; i < NB * NDD; i += 32) R[i] = g[i];
+    wt = g[NB * NDD];
+    __syncwarp();
+  } else {
+    wt = point_geometry(E, P, m, ex, ey, ez, q, lane, R);
+  }
   // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
   const int nh = L.nhist;
-  if (lane < 30) {
+  constexpr bool NEED_U = RES || LAWK != 0;
+  if (NEED_U && lane < 30) {
     const int d = lane / NDD, k = lane % NDD;
     for (int h = 0; h < nh; h++) {
       double s = 0.0;
@@ -189,14 +211,16 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
     }
   }
   __syncwarp();
-  const double wt = m.wq[qx] * m.wq[qy] * m.wq[qz] * tx[3 * P1 + 1] * ty[3 * P1 + 1] *
-                    tz[3 * P1 + 1] * detG;
   // (h) law
   if constexpr (LAWK == 0) {
     const double *u = P.u;
     if (RES && lane < 30) {
       double s = 0.0;
-      for (int j = 0; j < 30; j++) s += Dconst[30 * lane + j] * u[j];
+      if (L.dptr) {  // sparse constant tangent
+        for (int j = L.dptr[lane]; j < L.dptr[lane + 1]; j++) s += L.dval[j] * u[L.dcol[j]];
+      } else {
+        for (int j = 0; j < 30; j++) s += Dconst[30 * lane + j] * u[j];
+      }
       rr[lane] = wt * s;
     }
     if (TAN)

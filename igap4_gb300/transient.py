@@ -1,0 +1,110 @@
+"""Time stepping of the three-level transient law on the device.
+
+The reference library has no time loop: its callers set the history levels
+U_hist[1] = u_n, U_hist[2] = u_{n-1} (include/coreimpl.h:17,
+phys/gradelasttime.c:9-11), call IGAPSolvSolve and shift the levels.  This
+module is that caller for the transient runs: a seeded tip traction
+(sum of sinusoids), one Newton solve per step with u_n as the initial
+iterate (or a predictor's guess), then the history shift.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class TipLoad:
+    """Traction on one face: sum_i a_i sin(2 pi f_i t) along one direction,
+    amplitudes uniform in [0, amax], frequencies uniform in [fmin, fmax]."""
+
+    seed: int
+    n: int = 4
+    amax: float = 1e-3
+    fmin: float = 0.5
+    fmax: float = 5.0
+    face: int = 1        # x = L (the tip of the beam)
+    dof: int = 2         # z component
+    sign: float = -1.0
+    amp: np.ndarray = field(init=False)
+    freq: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        rng = np.random.default_rng(self.seed)
+        self.amp = rng.uniform(0.0, self.amax, self.n)
+        self.freq = rng.uniform(self.fmin, self.fmax, self.n)
+
+    def value(self, t: float) -> float:
+        return self.sign * float(np.sum(self.amp * np.sin(2.0 * np.pi * self.freq * t)))
+
+    def table(self, t: float) -> np.ndarray:
+        tab = np.zeros(36)
+        tab[6 * self.face + self.dof] = self.value(t)  # order 0 (plain traction)
+        return tab
+
+
+@dataclass
+class StepRecord:
+    t: float
+    newton_its: int
+    ksp_its: int
+    fnorm0: float
+    fnorm: float
+    converged: int
+    seconds: float
+    used_prediction: bool = False
+
+
+def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts=None,
+                  record_states: bool = True, device=None):
+    """Advance `nsteps` steps of size dt (dt must equal the law's par[7]).
+
+    A: igap4_gb300.Assembly with the transient law.  predictor: optional
+    callable (u_n, u_nm1, dload) -> guess for u_{n+1}; its guess is kept only
+    if it lowers the residual norm below that of u_n (plain Newton fallback).
+    Returns (states [nsteps+1, ndof] or None, list of StepRecord)."""
+    import torch
+
+    dev = device or torch.device("cuda")
+    o = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30)
+    if opts:
+        o.update(opts)
+    zero = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+    A.set_history(1, zero)
+    A.set_history(2, zero)
+    states = [np.zeros(A.ndof)] if record_states else None
+    recs = []
+    u_n = zero.clone()
+    u_nm1 = zero.clone()
+    F = torch.zeros_like(zero)
+    prev_load = 0.0
+    for n in range(nsteps):
+        t = (n + 1) * dt
+        A.set_neumann(load.table(t))
+        t0 = time.perf_counter()
+        U = u_n.clone()
+        used = False
+        if predictor is not None:
+            guess = predictor(u_n, u_nm1, load.value(t) - prev_load)
+            A.residual(U, F)
+            f_plain = torch.linalg.norm(F).item()
+            A.residual(guess, F)
+            f_pred = torch.linalg.norm(F).item()
+            if f_pred < f_plain:
+                U = guess.clone().contiguous()
+                used = True
+        st = A.solve(U, **o)
+        A.synchronize()
+        dtm = time.perf_counter() - t0
+        recs.append(StepRecord(t, st["newton_its"], st["ksp_its_total"], st["fnorm0"], st["fnorm"],
+                               st["converged"], dtm, used))
+        # history shift: u_{n-1} <- u_n, u_n <- u_{n+1}
+        A.set_history(0, U)
+        A.shift_history()
+        u_nm1, u_n = u_n, U
+        prev_load = load.value(t)
+        if record_states:
+            states.append(U.cpu().numpy())
+    return (np.array(states) if record_states else None), recs

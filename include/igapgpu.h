@@ -168,6 +168,12 @@ int igapgpu_solve(igapgpu_t ctx, double *U, const igapgpu_solver_opts *opts,
                   igapgpu_solve_stats *stats);
 void igapgpu_default_solver_opts(igapgpu_solver_opts *opts);
 
+/* Replace the constant traction table (index 6*face + 3*order + d) and
+ * recompute the Neumann load on the device; bc_type is unchanged.  Used by
+ * time-dependent loading (the reference's neumann callback may depend on
+ * par_neumann, include/bcimpl.h:6). */
+int igapgpu_set_neumann(igapgpu_t ctx, const double *table);
+
 int igapgpu_set_precision(igapgpu_t ctx, int mode);
 /* Run on the caller's CUDA stream (cudaStream_t passed as void*); NULL
  * restores the context's own stream. */
@@ -185,6 +191,10 @@ int64_t igapgpu_launch_count(void);
  * elements they processed since the last reset. */
 int igapgpu_profile(igapgpu_t ctx, int enable);
 int igapgpu_profile_read(igapgpu_t ctx, double *elem_ms, int64_t *launches, int64_t *elements);
+/* The same for one kernel kind: 0 = FP64 element kernel (residual and/or
+ * FP64 tangent), 1 = tensor-core split-precision tangent kernel. */
+int igapgpu_profile_read_kind(igapgpu_t ctx, int kind, double *elem_ms, int64_t *launches,
+                              int64_t *elements);
 
 /* Tensor-core self-test: D (128 x 32) = A (128 x 16) . B (32 x 16)^T of small
  * integers through tcgen05.mma kind::tf32 with the operand layout of the

@@ -219,6 +219,21 @@ def test_newton_linear_beam_matches_direct_solve():
     assert np.linalg.norm(orc.residual(U[None, :])) <= 1e-9
 
 
+def test_geometry_cache_on_off_identical(monkeypatch):
+    """The state-independent geometry cache gives bit-identical assembly."""
+    prob = po.Problem(nelem=(5, 3, 4), law=po.LAW_GRADELASTTIME, perturb=False)
+    U = po.random_state(prob, 12)
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("IGAPGPU_GEOMETRY_CACHE", flag)
+        A = gpu_case(prob)
+        A.set_state(U)
+        out.append((A.residual(), A.tangent()))
+        A.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_norm2_matches_numpy():
     prob = po.Problem(nelem=(6, 3, 3), law=po.LAW_GRADELAST)
     A = gpu_case(prob)
