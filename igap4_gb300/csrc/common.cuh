@@ -72,6 +72,8 @@ struct DevLaw {
   int dnnz;
 };
 
+struct GraphWork;
+
 struct Context {
   // problem
   int law, torder, nquad, prec;
@@ -121,6 +123,11 @@ struct Context {
   int red_cap = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // CUDA graphs (graph.cu)
+  GraphWork *gmres_graph = nullptr;
+  cudaGraphExec_t asm_graph[8] = {};
+  int64_t asm_graph_nodes[8] = {};
+  bool capturing = false;
   // element-kernel timing (igapgpu_profile)
   bool prof = false;
   // per kernel kind: 0 = FP64 element kernel, 1 = tensor-core tangent kernel
@@ -182,6 +189,11 @@ int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
               double *rnorm);
 int dev_norm2(Context *c, const double *x, double *out);
+// graph.cu
+int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
+                    double *rnorm);
+int assembly_graph(Context *c, bool do_res, bool do_tan);
+void graph_release(Context *c);
 
 }  // namespace igap
 

@@ -159,6 +159,7 @@ static void dirichlet_face(const Context *c, const std::vector<double> kn[3], in
 static int free_ctx(Context *c)
 {
   if (!c) return IGAPGPU_OK;
+  graph_release(c);
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,

@@ -331,6 +331,7 @@ void igapgpu_default_solver_opts(igapgpu_solver_opts *o)
   o->ksp_dtol = 1e8;
   o->ksp_max_it = 10000;
   o->pc = 1;
+  o->use_graphs = 1;
 }
 
 int igapgpu_norm2(igapgpu_t c, const double *x, double *out)
@@ -417,7 +418,8 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
   else if (U != Ud) IGAP_CUDA(cudaMemcpyAsync(Ud, U, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
   double *F = c->d_RR, *dx = c->d_work + 2 * n, *Ubak = c->d_stage_a, *negF = c->d_stage_b;
   const unsigned vb = vec_blocks(n);
-  if ((r = launch_assembly(c, true, false, F, nullptr))) return r;
+  auto residual = [&]() { return o.use_graphs ? assembly_graph(c, true, false) : launch_assembly(c, true, false, F, nullptr); };
+  if ((r = residual())) return r;
   double fnorm;
   if ((r = dev_norm2(c, F, &fnorm))) return r;
   S.fnorm0 = fnorm;
@@ -428,14 +430,15 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
     if (fnorm <= o.snes_abstol) { S.reason = 2; break; }
     if (fnorm <= o.snes_rtol * S.fnorm0) { S.reason = 3; break; }
     // J dx = -F
-    if ((r = launch_assembly(c, false, true, nullptr, c->d_vals))) return r;
+    if ((r = o.use_graphs ? assembly_graph(c, false, true) : launch_assembly(c, false, true, nullptr, c->d_vals)))
+      return r;
     c->matrix_valid = true;
     IGAP_CUDA(cudaMemsetAsync(dx, 0, sizeof(double) * n, c->stream));
     axpby_kernel<<<vb, 256, 0, c->stream>>>(negF, F, -1.0, 0.0, n);
     count_launch();
     int kits = 0;
     double kr = 0.0;
-    r = ksp_gmres(c, negF, dx, &o, &kits, &kr);
+    r = o.use_graphs ? ksp_gmres_graph(c, negF, dx, &o, &kits, &kr) : ksp_gmres(c, negF, dx, &o, &kits, &kr);
     if (r == IGAPGPU_ERR_NUMERIC) { S.reason = -3; break; }
     if (r) return r;
     S.ksp_its_last = kits;
@@ -449,7 +452,7 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
       IGAP_CUDA(cudaMemcpyAsync(Ud, Ubak, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
       axpby_kernel<<<vb, 256, 0, c->stream>>>(Ud, dx, lam, 1.0, n);
       count_launch();
-      if ((r = launch_assembly(c, true, false, F, nullptr))) return r;
+      if ((r = residual())) return r;
       if ((r = dev_norm2(c, F, &fn))) return r;
       const double fl = 0.5 * fn * fn;
       if (o.linesearch == 0 || (isfinite(fl) && fl <= f0 + 1e-4 * lam * slope)) { ok = true; break; }

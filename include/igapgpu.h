@@ -86,6 +86,7 @@ typedef struct {
   double ksp_dtol;
   int ksp_max_it;
   int pc;              /* 0 = none, 1 = Jacobi */
+  int use_graphs;      /* 1: assembly and GMRES cycles replayed as CUDA graphs */
 } igapgpu_solver_opts;
 
 typedef struct {

@@ -253,3 +253,25 @@ def test_bad_sizes_are_errors():
         ig.Assembly((1, 2, 2), [np.zeros(6)] + knots[1:], w, X)
     with pytest.raises(ig.IgapGpuError):
         ig.Assembly((2, 2, 2), knots, w, X, nquad=9)
+
+
+@pytest.mark.parametrize("prec", [ig.PREC_FP64, ig.PREC_SPLIT])
+def test_newton_with_graphs_matches_without(prec):
+    """Graph-replayed Newton step (captured assembly + device-resident GMRES
+    cycles) gives the same iterates as the step-by-step path."""
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(12, 3, 3), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, bc_type=bct, neumann=neu)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L)
+    res = []
+    for graphs in (0, 1):
+        A = ig.Assembly(prob.nelem, knots, w, X, law=prob.law, par=prob.params(), bc_type=bct, neumann=neu)
+        A.set_precision(prec)
+        U = np.zeros(A.ndof)
+        st = A.solve(U, snes_abstol=1e-10, ksp_rtol=1e-10, ksp_restart=40, ksp_max_it=40000,
+                     snes_max_it=15, use_graphs=graphs)
+        res.append((U, st))
+        A.close()
+    (U0, s0), (U1, s1) = res
+    assert s0["converged"] == 1 and s1["converged"] == 1, (s0, s1)
+    assert np.linalg.norm(U1 - U0) <= 1e-8 * np.linalg.norm(U0)
+    assert s1["newton_its"] == s0["newton_its"]
