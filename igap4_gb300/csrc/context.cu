@@ -413,11 +413,6 @@ static int set_current(Context *c, const double *U)
   return IGAPGPU_OK;
 }
 
-static int ensure_stage_v(Context *c)
-{
-  if (c->d_stage_v) return IGAPGPU_OK;
-  return dev_alloc(&c->d_stage_v, c->nnz);
-}
 
 }  // namespace igap
 

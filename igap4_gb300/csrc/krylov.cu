@@ -424,7 +424,6 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
   if ((r = dev_norm2(c, F, &fnorm))) return r;
   S.fnorm0 = fnorm;
   S.reason = 0;
-  double unorm_prev = 0.0;
   for (int it = 0; it < o.snes_max_it; it++) {
     if (!isfinite(fnorm)) { S.reason = -4; break; }
     if (fnorm <= o.snes_abstol) { S.reason = 2; break; }
@@ -480,7 +479,6 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
     double dxn, un;
     if ((r = dev_norm2(c, dx, &dxn))) return r;
     if ((r = dev_norm2(c, Ud, &un))) return r;
-    (void)unorm_prev;
     if (lam * dxn <= o.snes_stol * un) { S.reason = 4; break; }
   }
   if (S.reason == 0) S.reason = (fnorm <= o.snes_abstol) ? 2 : -5;

@@ -1,0 +1,161 @@
+"""Learned Newton predictor for the transient runs (no counterpart in the
+reference; a spec addition).
+
+A 3-D convolutional network on the control-point lattice predicts the next
+displacement increment from (u_n, u_{n-1}, load increment).  It is a
+correction to linear extrapolation,
+
+    guess = u_n + (u_n - u_{n-1}) + s_out * net([u_n / s_u, u_{n-1} / s_u, dload / s_l]),
+
+with the last layer initialised to zero, so an untrained network reproduces
+the extrapolation.  The network's forward, backward and Adam step are the
+library's own kernels (igapgpu_net_*); torch is used here only to hold device
+buffers and to pack the 9 input channels.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _check, _ptr, lib
+
+CIN = (9, 32, 32, 32)
+COUT = (32, 32, 32, 3)
+NPARAM = sum(co * 27 * ci for ci, co in zip(CIN, COUT)) + sum(COUT)
+
+
+def _bind():
+    L = lib()
+    if getattr(L, "_net_bound", False):
+        return L
+    vp = ctypes.c_void_p
+    L.igapgpu_net_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int]
+    L.igapgpu_net_destroy.argtypes = [vp]
+    L.igapgpu_net_num_params.argtypes = [vp]
+    L.igapgpu_net_num_params.restype = ctypes.c_int64
+    L.igapgpu_net_set_stream.argtypes = [vp, vp]
+    for f in ("igapgpu_net_set_params", "igapgpu_net_get_params", "igapgpu_net_get_grads"):
+        getattr(L, f).argtypes = [vp, vp]
+    L.igapgpu_net_forward.argtypes = [vp, vp, vp, ctypes.c_int]
+    L.igapgpu_net_train_step.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_float,
+                                         ctypes.POINTER(ctypes.c_float)]
+    L._net_bound = True
+    return L
+
+
+def init_params(seed: int, zero_last: bool = True) -> np.ndarray:
+    """He-normal weights for the ReLU layers; the output layer starts at zero."""
+    rng = np.random.default_rng(seed)
+    ws = []
+    for l, (ci, co) in enumerate(zip(CIN, COUT)):
+        std = np.sqrt(2.0 / (27 * ci))
+        w = rng.standard_normal((co, 27, ci)) * std
+        if l == 3 and zero_last:
+            w[:] = 0.0
+        ws.append(w.ravel())
+    bs = [np.zeros(co) for co in COUT]
+    return np.concatenate(ws + bs).astype(np.float32)
+
+
+class ConvNet:
+    """Device network over a lattice (nx, ny, nz); storage 'bf16' or 'f32'."""
+
+    def __init__(self, lattice, batch_max=1, storage="bf16", params=None, seed=0):
+        L = _bind()
+        h = ctypes.c_void_p()
+        _check(L.igapgpu_net_create(ctypes.byref(h), int(lattice[0]), int(lattice[1]), int(lattice[2]),
+                                    int(batch_max), 1 if storage == "bf16" else 0))
+        self.h = h
+        self.lattice = tuple(int(v) for v in lattice)
+        self.P = int(np.prod(self.lattice))
+        self.batch_max = batch_max
+        self.set_params(init_params(seed) if params is None else params)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().igapgpu_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == NPARAM
+        _check(lib().igapgpu_net_set_params(self.h, _ptr(p)))
+
+    def get_params(self):
+        p = np.zeros(NPARAM, np.float32)
+        _check(lib().igapgpu_net_get_params(self.h, _ptr(p)))
+        return p
+
+    def get_grads(self):
+        g = np.zeros(NPARAM, np.float32)
+        _check(lib().igapgpu_net_get_grads(self.h, _ptr(g)))
+        return g
+
+    def forward(self, x, out):
+        """x: CUDA float32 [B, P, 9]; out: CUDA float32 [B, P, 3]."""
+        _check(lib().igapgpu_net_forward(self.h, _ptr(x), _ptr(out), int(x.shape[0])))
+        return out
+
+    def train_step(self, x, target, lr):
+        loss = ctypes.c_float()
+        _check(lib().igapgpu_net_train_step(self.h, _ptr(x), _ptr(target), int(x.shape[0]), float(lr),
+                                            ctypes.byref(loss)))
+        return float(loss.value)
+
+
+@dataclass
+class Scales:
+    u: float = 1.0
+    load: float = 1.0
+    out: float = 1.0
+
+
+def features(u_n, u_nm1, dload, scales: Scales):
+    """[P, 9] float32 input channels from device DOF vectors (3 per point)."""
+    import torch
+
+    P = u_n.numel() // 3
+    x = torch.empty((P, 9), dtype=torch.float32, device=u_n.device)
+    x[:, 0:3] = (u_n.view(P, 3) / scales.u).float()
+    x[:, 3:6] = (u_nm1.view(P, 3) / scales.u).float()
+    x[:, 6:9] = torch.as_tensor(np.asarray(dload, np.float32) / scales.load, device=u_n.device)
+    return x
+
+
+class LearnedPredictor:
+    """Callable (u_n, u_{n-1}, dload) -> guess for u_{n+1} (device float64)."""
+
+    def __init__(self, net: ConvNet, scales: Scales, dload_dir=(0.0, 0.0, 1.0)):
+        import torch
+
+        self.net = net
+        self.scales = scales
+        self.dir = np.asarray(dload_dir, np.float64)
+        self.out = torch.empty((1, net.P, 3), dtype=torch.float32, device="cuda")
+
+    def __call__(self, u_n, u_nm1, dload_scalar):
+        x = features(u_n, u_nm1, self.dir * dload_scalar, self.scales)[None]
+        self.net.forward(x, self.out)
+        corr = self.out.view(-1).double() * self.scales.out
+        return u_n + (u_n - u_nm1) + corr
+
+
+def make_samples(states, loads, lattice_points):
+    """Training pairs from one trajectory: inputs (u_n, u_{n-1}, dload) and
+    targets = (u_{n+1} - u_n) - (u_n - u_{n-1}) for n = 1 .. N-1."""
+    X, Y = [], []
+    for n in range(1, len(states) - 1):
+        un, unm1, unp1 = states[n], states[n - 1], states[n + 1]
+        dl = np.array([0.0, 0.0, loads[n + 1] - loads[n]])
+        X.append((un, unm1, dl))
+        Y.append((unp1 - un) - (un - unm1))
+    return X, Y

@@ -1,0 +1,151 @@
+"""Train the learned Newton predictor on trajectories of the plain method and
+measure what it gains (spec config 5, scaled to the sizes given on the
+command line).
+
+    python -m igap4_gb300.train_predictor --nelem 16,4,4 --train 6 --steps 60 --test 2
+
+1. Plain-method trajectories (transient law, seeded tip loads) on the device.
+2. Samples (u_n, u_{n-1}, load increment) -> correction to linear extrapolation.
+3. Adam training with the library's own BF16 network kernels.
+4. Unseen load histories: Newton iterations and wall time per step, plain
+   Newton (guess u_n) vs the predictor (kept only when it lowers |F|).
+Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def transient_problem(nelem, dt=1e-2, rho=1.0):
+    import igap4_gb300 as ig
+
+    par = np.array(ig.LAW_DEFAULT_PAR[ig.LAW_GRADELASTTIME], dtype=float)
+    par[5], par[7] = rho, dt
+    bct, _ = ig.clamp_bc((0,))
+    knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0))
+    A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_GRADELASTTIME, par=par, bc_type=bct)
+    return A, par
+
+
+def generate(A, seeds, nsteps, dt, amax, opts=None):
+    from .transient import TipLoad, run_transient
+
+    trajs = []
+    for s in seeds:
+        load = TipLoad(seed=int(s), amax=amax)
+        states, recs = run_transient(A, load, nsteps, dt, opts=opts)
+        loads = np.array([0.0] + [load.value((n + 1) * dt) for n in range(nsteps)])
+        trajs.append((states, loads, recs))
+    return trajs
+
+
+def build_dataset(trajs):
+    from .predictor import make_samples
+
+    X, Y = [], []
+    for states, loads, _ in trajs:
+        x, y = make_samples(states, loads, None)
+        X += x
+        Y += y
+    return X, Y
+
+
+def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None):
+    import torch
+
+    from .predictor import ConvNet, Scales, features
+
+    lattice = tuple(n + 2 for n in A.nelem)
+    su = max(1e-30, max(np.abs(x[0]).max() for x in X))
+    sl = max(1e-30, max(np.abs(x[2]).max() for x in X))
+    so = max(1e-30, max(np.abs(y).max() for y in Y))
+    scales = Scales(u=su, load=sl, out=so)
+    P = int(np.prod(lattice))
+    dev = torch.device("cuda")
+    feats = torch.stack([features(torch.tensor(x[0], device=dev), torch.tensor(x[1], device=dev), x[2], scales)
+                         for x in X])
+    targ = torch.stack([torch.tensor(y / so, dtype=torch.float32, device=dev).view(P, 3) for y in Y])
+    net = ConvNet(lattice, batch_max=batch, storage=storage, seed=seed)
+    rng = np.random.default_rng(seed)
+    n = len(X)
+    hist = []
+    for ep in range(epochs):
+        order = rng.permutation(n)
+        tot = 0.0
+        for i in range(0, n - batch + 1, batch):
+            idx = torch.tensor(order[i:i + batch], device=dev)
+            tot += net.train_step(feats[idx].contiguous(), targ[idx].contiguous(), lr) * batch
+        hist.append(tot / max(1, (n // batch) * batch))
+        if log:
+            log(f"epoch {ep}: loss {hist[-1]:.4e}")
+    return net, scales, hist
+
+
+def evaluate(A, seeds, nsteps, dt, amax, predictor=None, opts=None):
+    from .transient import TipLoad, run_transient
+
+    its, times, used = [], [], []
+    for s in seeds:
+        load = TipLoad(seed=int(s), amax=amax)
+        _, recs = run_transient(A, load, nsteps, dt, predictor=predictor, opts=opts, record_states=False)
+        its += [r.newton_its for r in recs]
+        times += [r.seconds for r in recs]
+        used += [r.used_prediction for r in recs]
+    return {"newton_its_per_step": float(np.mean(its)), "seconds_per_step": float(np.mean(times)),
+            "prediction_used_fraction": float(np.mean(used)) if predictor else 0.0}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nelem", default="16,4,4")
+    ap.add_argument("--train", type=int, default=6, help="training trajectories")
+    ap.add_argument("--test", type=int, default=2, help="unseen evaluation trajectories")
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--dt", type=float, default=1e-2)
+    ap.add_argument("--amax", type=float, default=1e-3)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--eval-nelem", default=None, help="evaluate on another mesh (default: same)")
+    a = ap.parse_args()
+    import torch  # noqa: F401
+
+    from .predictor import LearnedPredictor
+
+    nelem = tuple(int(v) for v in a.nelem.split(","))
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30)
+    A, _ = transient_problem(nelem, a.dt)
+    t0 = time.perf_counter()
+    trajs = generate(A, range(1000, 1000 + a.train), a.steps, a.dt, a.amax, opts)
+    t_gen = time.perf_counter() - t0
+    X, Y = build_dataset(trajs)
+    t0 = time.perf_counter()
+    net, scales, hist = train(A, X, Y, epochs=a.epochs)
+    t_train = time.perf_counter() - t0
+    if a.eval_nelem:
+        A.close()
+        A, _ = transient_problem(tuple(int(v) for v in a.eval_nelem.split(",")), a.dt)
+        from .predictor import ConvNet
+
+        lattice = tuple(n + 2 for n in A.nelem)
+        net = ConvNet(lattice, batch_max=1, storage="bf16", params=net.get_params())
+    seeds = range(5000, 5000 + a.test)
+    plain = evaluate(A, seeds, a.steps, a.dt, a.amax, None, opts)
+    from .predictor import init_params
+
+    extrap_net = type(net)(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
+    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, scales), opts)
+    learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales), opts)
+    out = {"train_mesh": list(nelem), "eval_mesh": list(A.nelem), "train_trajectories": a.train,
+           "steps": a.steps, "samples": len(X), "generation_s": t_gen, "training_s": t_train,
+           "loss_first": hist[0], "loss_last": hist[-1], "plain": plain,
+           "extrapolation_only": extrap, "learned": learned,
+           "time_ratio_learned_vs_plain": learned["seconds_per_step"] / plain["seconds_per_step"],
+           "its_ratio_learned_vs_plain": learned["newton_its_per_step"] / plain["newton_its_per_step"]}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -207,6 +207,27 @@ int igapgpu_tc_selftest(int variant, float *out);
  * kernel; used as the denominator of FP64-bound roofline fractions. */
 int igapgpu_measure_fp64_peak(double *tflops);
 
+/* ---- learned Newton predictor (no counterpart in the reference) --------
+ * 3-D convolutional network on the control-point lattice (nx, ny, nz):
+ * channels 9 -> 32 -> 32 -> 32 -> 3, 3x3x3 kernels, zero padding, ReLU after
+ * the first three layers.  storage 1 = bfloat16 weights and activations,
+ * 0 = float (gradient checks); FP32 accumulation; FP32 master weights and Adam.
+ * Parameter layout: weights layer by layer [Co][27][Ci] (tap t = 9(dx+1) +
+ * 3(dy+1) + dz+1), then biases.  Tensors are device FP32, [B][nx][ny][nz][C]. */
+typedef struct igapgpu_net igapgpu_net;
+int igapgpu_net_create(igapgpu_net **net, int nx, int ny, int nz, int batch_max, int storage);
+int igapgpu_net_destroy(igapgpu_net *net);
+int64_t igapgpu_net_num_params(igapgpu_net *net);
+int igapgpu_net_set_stream(igapgpu_net *net, void *stream);
+int igapgpu_net_set_params(igapgpu_net *net, const float *params);
+int igapgpu_net_get_params(igapgpu_net *net, float *params);
+int igapgpu_net_get_grads(igapgpu_net *net, float *grads);
+int igapgpu_net_forward(igapgpu_net *net, const float *in, float *out, int batch);
+/* forward + mean-square loss against target + backward (gradients zeroed
+ * first); lr > 0 then applies one Adam step.  loss: host float. */
+int igapgpu_net_train_step(igapgpu_net *net, const float *in, const float *target, int batch, float lr,
+                           float *loss);
+
 #ifdef __cplusplus
 }
 #endif
