@@ -79,6 +79,8 @@ def lib():
         L.igapgpu_finalize.argtypes = [vp]
         L.igapgpu_sizes.argtypes = [vp] + [ctypes.c_void_p] * 4
         L.igapgpu_pattern.argtypes = [vp, vp, vp]
+        L.igapgpu_dirichlet.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_impose_dirichlet.argtypes = [vp, vp]
         for f in ("igapgpu_set_history", "igapgpu_get_history"):
             getattr(L, f).argtypes = [vp, ctypes.c_int, vp]
         L.igapgpu_shift_history.argtypes = [vp]
@@ -105,6 +107,9 @@ def lib():
         L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
         _lib = L
     return _lib
+
+
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 
 
 def _check(rc):
@@ -219,6 +224,21 @@ class Assembly:
         _check(lib().igapgpu_pattern(self.h, _ptr(rowptr), _ptr(cols)))
         return rowptr, cols
 
+    def dirichlet(self):
+        """(rows int64, prescribed values float64) of the Dirichlet DOFs."""
+        n = ctypes.c_int64()
+        _check(lib().igapgpu_dirichlet(self.h, ctypes.byref(n), None, None))
+        rows = np.zeros(n.value, np.int64)
+        vals = np.zeros(n.value)
+        if n.value:
+            _check(lib().igapgpu_dirichlet(self.h, ctypes.byref(n), _ptr(rows), _ptr(vals)))
+        return rows, vals
+
+    def impose_dirichlet(self, U):
+        """U[r] = g_r on the Dirichlet rows, in place (host array or CUDA tensor)."""
+        _check(lib().igapgpu_impose_dirichlet(self.h, _ptr(U)))
+        return U
+
     def set_history(self, level, U):
         _check(lib().igapgpu_set_history(self.h, level, _ptr(U)))
 
@@ -300,8 +320,15 @@ class Assembly:
         _check(lib().igapgpu_set_precision(self.h, mode))
 
     def set_stream(self, stream_handle):
-        """stream_handle: an integer cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
-        _check(lib().igapgpu_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+        """stream_handle: an integer cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream),
+        or None for the context's own stream.  0 is the legacy default stream
+        (torch's default stream) and is passed as cudaStreamLegacy, because a
+        NULL handle selects the context's own stream."""
+        if stream_handle is None:
+            h = None
+        else:
+            h = ctypes.c_void_p(int(stream_handle) or CUDA_STREAM_LEGACY)
+        _check(lib().igapgpu_set_stream(self.h, h))
 
     def synchronize(self):
         _check(lib().igapgpu_synchronize(self.h))

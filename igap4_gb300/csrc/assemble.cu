@@ -528,6 +528,22 @@ int launch_dirichlet_residual(Context *c, double *RR)
   return IGAPGPU_OK;
 }
 
+__global__ void impose_dirichlet_kernel(const int64_t *rows, const double *g, int64_t n, double *U)
+{
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) U[rows[t]] = g[t];
+}
+
+int launch_impose_dirichlet(Context *c, double *U)
+{
+  if (c->n_dir == 0) return IGAPGPU_OK;
+  impose_dirichlet_kernel<<<(unsigned)((c->n_dir + 255) / 256), 256, 0, c->stream>>>(c->d_dir_rows, c->d_dir_g,
+                                                                                     c->n_dir, U);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
 int launch_dirichlet_matrix(Context *c, double *vals)
 {
   if (c->n_dir == 0) return IGAPGPU_OK;

@@ -179,6 +179,7 @@ int launch_lingrad_dconst(Context *c);
 int launch_neumann(Context *c, const double nfac[NFACE][2]);
 int launch_dirichlet_matrix(Context *c, double *vals);
 int launch_dirichlet_residual(Context *c, double *RR);
+int launch_impose_dirichlet(Context *c, double *U);
 int launch_pattern_cols(Context *c);
 int launch_geometry_cache(Context *c);
 int launch_geometry_cache_f32(Context *c);

@@ -515,6 +515,37 @@ int igapgpu_pattern(igapgpu_t c, int64_t *rowptr, int32_t *cols)
   return IGAPGPU_OK;
 }
 
+int igapgpu_dirichlet(igapgpu_t c, int64_t *count, int64_t *rows, double *values)
+{
+  if (!c) return IGAPGPU_ERR_ARG;
+  if (count) *count = c->n_dir;
+  if (c->n_dir == 0) return IGAPGPU_OK;
+  if (rows) {
+    cudaMemcpyKind k = is_device_ptr(rows) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    IGAP_CUDA(cudaMemcpyAsync(rows, c->d_dir_rows, sizeof(int64_t) * c->n_dir, k, c->stream));
+  }
+  if (values) {
+    cudaMemcpyKind k = is_device_ptr(values) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    IGAP_CUDA(cudaMemcpyAsync(values, c->d_dir_g, sizeof(double) * c->n_dir, k, c->stream));
+  }
+  IGAP_CUDA(cudaStreamSynchronize(c->stream));
+  return IGAPGPU_OK;
+}
+
+int igapgpu_impose_dirichlet(igapgpu_t c, double *U)
+{
+  if (!c || !U) return IGAPGPU_ERR_ARG;
+  if (c->n_dir == 0) return IGAPGPU_OK;
+  if (is_device_ptr(U)) return launch_impose_dirichlet(c, U);
+  // host vector: round trip through the residual scratch
+  IGAP_CUDA(cudaMemcpyAsync(c->d_RR, U, sizeof(double) * c->ndof, cudaMemcpyHostToDevice, c->stream));
+  int r = launch_impose_dirichlet(c, c->d_RR);
+  if (r) return r;
+  IGAP_CUDA(cudaMemcpyAsync(U, c->d_RR, sizeof(double) * c->ndof, cudaMemcpyDeviceToHost, c->stream));
+  IGAP_CUDA(cudaStreamSynchronize(c->stream));
+  return IGAPGPU_OK;
+}
+
 int igapgpu_set_history(igapgpu_t c, int level, const double *U)
 {
   if (!c || !U || level < 0 || level > c->torder) {

@@ -214,6 +214,15 @@ void graph_release(Context *c)
   }
 }
 
+
+// Capture cannot begin on the legacy default stream; there the graph is
+// recorded on the context's own stream (recording runs nothing) and later
+// launched on the caller's stream.
+static cudaStream_t capture_stream(const Context *c)
+{
+  return (c->stream == nullptr || c->stream == cudaStreamLegacy) ? c->own_stream : c->stream;
+}
+
 static int build_gmres_graph(Context *c, int m, int pc)
 {
   free_graph(c->gmres_graph);
@@ -236,7 +245,7 @@ static int build_gmres_graph(Context *c, int m, int pc)
   gw->pc = pc;
   const unsigned vb = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
   const unsigned sb = (unsigned)((n * 32 + 255) / 256);
-  cudaStream_t s = c->stream;
+  cudaStream_t s = capture_stream(c);
   int64_t nodes = 0;
   IGAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   gm_reset<<<1, 1, 0, s>>>(gw->st);
@@ -354,11 +363,14 @@ int assembly_graph(Context *c, bool do_res, bool do_tan)
     const bool prof = c->prof;
     c->prof = false;
     c->capturing = true;
+    cudaStream_t user = c->stream;
+    c->stream = capture_stream(c);
     IGAP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t l0 = g_launches.load();
     int r = launch_assembly(c, do_res, do_tan, c->d_RR, c->d_vals);
     cudaGraph_t graph;
     cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    c->stream = user;
     c->capturing = false;
     c->prof = prof;
     if (r) return r;

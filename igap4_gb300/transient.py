@@ -68,6 +68,9 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     import torch
 
     dev = device or torch.device("cuda")
+    # the context works on torch's current stream, so residuals read by torch
+    # (the predictor's acceptance test) are ordered after the kernels
+    A.set_stream(torch.cuda.current_stream(dev).cuda_stream)
     o = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30)
     if opts:
         o.update(opts)
@@ -87,13 +90,16 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         U = u_n.clone()
         used = False
         if predictor is not None:
-            guess = predictor(u_n, u_nm1, load.value(t) - prev_load)
+            # the Newton correction leaves Dirichlet DOFs where the initial
+            # iterate puts them (their columns are cleared), so the guess
+            # carries the prescribed values exactly
+            guess = A.impose_dirichlet(predictor(u_n, u_nm1, load.value(t) - prev_load).contiguous())
             A.residual(U, F)
-            f_plain = torch.linalg.norm(F).item()
+            f_plain = A.norm2(F)
             A.residual(guess, F)
-            f_pred = torch.linalg.norm(F).item()
+            f_pred = A.norm2(F)
             if f_pred < f_plain:
-                U = guess.clone().contiguous()
+                U = guess.clone()
                 used = True
         st = A.solve(U, **o)
         A.synchronize()

@@ -115,6 +115,14 @@ int igapgpu_sizes(igapgpu_t ctx, int64_t *ndof, int64_t *nnz, int *torder, int64
  * MatSetValues of Tangent_iga (MAT_KEEP_NONZERO_PATTERN, src/interface.c:196). */
 int igapgpu_pattern(igapgpu_t ctx, int64_t *rowptr, int32_t *cols);
 
+/* Dirichlet rows (unique) and their prescribed values g: the rows
+ * Residual_iga sets to U - g (src/assmcore_iga.c:451-495) and Tangent_iga
+ * clears with MatZeroRowsColumns (src/assmcore_iga.c:844).  rows / values may be NULL, host or device. */
+int igapgpu_dirichlet(igapgpu_t ctx, int64_t *count, int64_t *rows, double *values);
+/* U[r] = g_r on every Dirichlet row (U host or device), so that an initial
+ * iterate meets the constraints the Newton correction does not move. */
+int igapgpu_impose_dirichlet(igapgpu_t ctx, double *U);
+
 /* State history U_hist[level] (level 0 current, 1 = u_n, 2 = u_{n-1}). */
 int igapgpu_set_history(igapgpu_t ctx, int level, const double *U);
 int igapgpu_get_history(igapgpu_t ctx, int level, double *U);
@@ -177,7 +185,8 @@ int igapgpu_set_neumann(igapgpu_t ctx, const double *table);
 
 int igapgpu_set_precision(igapgpu_t ctx, int mode);
 /* Run on the caller's CUDA stream (cudaStream_t passed as void*); NULL
- * restores the context's own stream. */
+ * restores the context's own (non-blocking) stream, so the legacy default
+ * stream is selected with cudaStreamLegacy. */
 int igapgpu_set_stream(igapgpu_t ctx, void *stream);
 int igapgpu_synchronize(igapgpu_t ctx);
 const char *igapgpu_last_error(void);

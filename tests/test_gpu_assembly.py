@@ -275,3 +275,27 @@ def test_newton_with_graphs_matches_without(prec):
     assert s0["converged"] == 1 and s1["converged"] == 1, (s0, s1)
     assert np.linalg.norm(U1 - U0) <= 1e-8 * np.linalg.norm(U0)
     assert s1["newton_its"] == s0["newton_its"]
+
+
+def test_dirichlet_rows_match_reference_tangent():
+    """The Dirichlet rows the context reports are exactly the rows the
+    reference's tangent reduced to identity rows (MatZeroRowsColumns), and
+    impose_dirichlet writes g there and nothing elsewhere."""
+    g = load("g_static_2x2x2")
+    A = gpu_case(problem_from_golden(g))
+    rows, vals = A.dirichlet()
+    rowptr, cols, v = g["rowptr"], g["cols"], g["vals"]
+    ident = []
+    for r in range(len(rowptr) - 1):
+        c, x = cols[rowptr[r]:rowptr[r + 1]], v[rowptr[r]:rowptr[r + 1]]
+        if np.all(x[c != r] == 0.0) and np.all(x[c == r] == 1.0):
+            ident.append(r)
+    np.testing.assert_array_equal(np.sort(rows), np.array(ident))
+    U = np.random.default_rng(3).standard_normal(A.ndof)
+    V = A.impose_dirichlet(U.copy())
+    np.testing.assert_array_equal(V[rows], vals)
+    keep = np.ones(A.ndof, bool)
+    keep[rows] = False
+    np.testing.assert_array_equal(V[keep], U[keep])
+    RR = A.residual(V)
+    assert np.all(RR[rows] == 0.0)

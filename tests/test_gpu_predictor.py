@@ -1,5 +1,6 @@
 """Learned predictor kernels: forward pass and gradients against the FP64
-numpy oracle (float storage: 1e-4 relative; bf16 storage: 3e-2), and a
+numpy oracle (float storage: 1e-4 relative; bf16 storage: 6e-2, four layers of
+BF16 activation rounding over 864-term sums), and a
 few Adam steps reduce the loss."""
 import numpy as np
 import pytest
@@ -20,7 +21,7 @@ def _case(seed=0, lattice=(5, 4, 3), B=2):
     return params, x, y
 
 
-@pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("bf16", 3e-2)])
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("bf16", 6e-2)])
 def test_forward_and_gradients_vs_oracle(storage, tol):
     torch = pytest.importorskip("torch")
     lattice, B = (5, 4, 3), 2
