@@ -105,6 +105,13 @@ def lib():
         L.igapgpu_profile_read_kind.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.igapgpu_measure_fp64_peak.argtypes = [vp]
         L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
+        L.igapgpu_batch_init.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(MeshDesc),
+                                         ctypes.POINTER(PhysDesc), ctypes.POINTER(BCDesc), ctypes.c_int]
+        L.igapgpu_batch_info.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_batch_norms.argtypes = [vp, vp, vp]
+        L.igapgpu_batch_set_schedule.argtypes = [vp, vp]
+        L.igapgpu_batch_get_schedule.argtypes = [vp, vp]
+        L.igapgpu_batch_autotune.argtypes = [vp, ctypes.c_int, ctypes.c_double, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -171,41 +178,54 @@ def clamp_bc(faces=(0,), traction_face=None, traction=(0.0, 0.0, 0.0)):
     return bct, neu
 
 
+def _descs(keep, nelem, knots, w, X, law, par, bc_type, neumann, par_dirichlet, porder=2):
+    """ctypes descriptors of one instance; the arrays they point to go to keep."""
+    arrs = [np.ascontiguousarray(k, np.float64) for k in knots]
+    arrs += [np.ascontiguousarray(w, np.float64), np.ascontiguousarray(X, np.float64)]
+    keep += arrs
+    dp = ctypes.POINTER(ctypes.c_double)
+    md = MeshDesc()
+    md.porder = porder
+    for d in range(3):
+        md.nelem[d] = int(nelem[d])
+        md.knots[d] = arrs[d].ctypes.data_as(dp)
+    md.w = arrs[3].ctypes.data_as(dp)
+    md.X = arrs[4].ctypes.data_as(dp)
+    pd = PhysDesc()
+    pd.law = law
+    p = LAW_DEFAULT_PAR.get(law, [0.0] * 9) if par is None else list(par)
+    for i in range(9):
+        pd.par[i] = float(p[i]) if i < len(p) else 0.0
+    bd = BCDesc()
+    for i in range(36):
+        bd.bc_type[i] = 1 if bc_type is None else int(bc_type[i])
+        bd.neumann[i] = 0.0 if neumann is None else float(neumann[i])
+    for i in range(9):
+        bd.par_dirichlet[i] = 0.0 if par_dirichlet is None else float(par_dirichlet[i])
+    return md, pd, bd
+
+
 class Assembly:
     """One GPU assembly context (IGAPAssmInit + the Residual/Tangent callbacks)."""
 
     def __init__(self, nelem, knots, w, X, law=LAW_GRADELAST, par=None, bc_type=None,
                  neumann=None, par_dirichlet=None, nquad=4, porder=2):
         L = lib()
-        self._keep = [np.ascontiguousarray(k, np.float64) for k in knots]
-        self._keep += [np.ascontiguousarray(w, np.float64), np.ascontiguousarray(X, np.float64)]
-        md = MeshDesc()
-        md.porder = porder
-        for d in range(3):
-            md.nelem[d] = int(nelem[d])
-            md.knots[d] = self._keep[d].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        md.w = self._keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        md.X = self._keep[4].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        pd = PhysDesc()
-        pd.law = law
-        p = LAW_DEFAULT_PAR.get(law, [0.0] * 9) if par is None else list(par)
-        for i in range(9):
-            pd.par[i] = float(p[i]) if i < len(p) else 0.0
-        bd = BCDesc()
-        for i in range(36):
-            bd.bc_type[i] = 1 if bc_type is None else int(bc_type[i])
-            bd.neumann[i] = 0.0 if neumann is None else float(neumann[i])
-        for i in range(9):
-            bd.par_dirichlet[i] = 0.0 if par_dirichlet is None else float(par_dirichlet[i])
+        self._keep = []
+        md, pd, bd = _descs(self._keep, nelem, knots, w, X, law, par, bc_type, neumann, par_dirichlet, porder)
         h = ctypes.c_void_p()
         _check(L.igapgpu_assm_init(ctypes.byref(h), ctypes.byref(md), ctypes.byref(pd),
                                    ctypes.byref(bd), nquad))
         self.h = h
+        self._sizes()
+        self.nelem = tuple(int(n) for n in nelem)
+
+    def _sizes(self):
         nd, nz, el = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         to = ctypes.c_int()
-        _check(L.igapgpu_sizes(h, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(to), ctypes.byref(el)))
+        _check(lib().igapgpu_sizes(self.h, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(to),
+                                   ctypes.byref(el)))
         self.ndof, self.nnz, self.torder, self.nelem_total = nd.value, nz.value, to.value, el.value
-        self.nelem = tuple(int(n) for n in nelem)
 
     def close(self):
         if getattr(self, "h", None):
@@ -366,3 +386,93 @@ def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     _check(lib().igapgpu_measure_fp64_peak(ctypes.byref(t)))
     return t.value
+
+
+class BatchSchedule(ctypes.Structure):
+    """Work-queue schedule of the batched kernels (igapgpu_batch_schedule)."""
+    _fields_ = [("grab_fp64", ctypes.c_int), ("ctas_per_sm_fp64", ctypes.c_int),
+                ("grab_tc", ctypes.c_int), ("order", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class BatchAssembly(Assembly):
+    """Independent instances (beams of different sizes and parameters, one law)
+    assembled by one persistent launch per kernel.  The object behaves as an
+    :class:`Assembly` of the block-diagonal union: DOFs of instance i occupy
+    ``dof_off[i]:dof_off[i+1]``.
+
+    instances: sequence of dicts with keys nelem, knots, w, X and optionally
+    par, bc_type, neumann, par_dirichlet."""
+
+    def __init__(self, instances, law=LAW_LINGRAD, nquad=4):
+        L = lib()
+        n = len(instances)
+        self._keep = []
+        mds, pds, bds = (MeshDesc * n)(), (PhysDesc * n)(), (BCDesc * n)()
+        for i, inst in enumerate(instances):
+            md, pd, bd = _descs(self._keep, inst["nelem"], inst["knots"], inst["w"], inst["X"], law,
+                                inst.get("par"), inst.get("bc_type"), inst.get("neumann"),
+                                inst.get("par_dirichlet"))
+            mds[i], pds[i], bds[i] = md, pd, bd
+        h = ctypes.c_void_p()
+        _check(L.igapgpu_batch_init(ctypes.byref(h), n, mds, pds, bds, nquad))
+        self.h = h
+        self._sizes()
+        self.ninst = n
+        self.dof_off = np.zeros(n + 1, np.int64)
+        self.elem_off = np.zeros(n + 1, np.int64)
+        ni = ctypes.c_int()
+        _check(L.igapgpu_batch_info(h, ctypes.byref(ni), _ptr(self.dof_off), _ptr(self.elem_off)))
+        self.nelem = None
+        self.instance_nelem = [tuple(int(v) for v in inst["nelem"]) for inst in instances]
+
+    def norms(self, x):
+        """FP64 2-norm of every instance's segment of x (host array or CUDA tensor)."""
+        out = np.zeros(self.ninst)
+        _check(lib().igapgpu_batch_norms(self.h, _ptr(x), _ptr(out)))
+        return out
+
+    def segment(self, x, i):
+        return x[self.dof_off[i]:self.dof_off[i + 1]]
+
+    @property
+    def schedule(self):
+        s = BatchSchedule()
+        _check(lib().igapgpu_batch_get_schedule(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    @schedule.setter
+    def schedule(self, d):
+        s = BatchSchedule(**{k: int(v) for k, v in d.items()})
+        _check(lib().igapgpu_batch_set_schedule(self.h, ctypes.byref(s)))
+
+    def autotune(self, reps=2, frac=0.1):
+        """Time the candidate schedules, keep the fastest; returns
+        (schedule dict, best FP64-kernel ms, best tensor-core-kernel ms) on
+        the timed queue prefix."""
+        s = BatchSchedule()
+        m64, mtc = ctypes.c_double(), ctypes.c_double()
+        _check(lib().igapgpu_batch_autotune(self.h, int(reps), float(frac), ctypes.byref(s),
+                                            ctypes.byref(m64), ctypes.byref(mtc)))
+        return s.as_dict(), m64.value, mtc.value
+
+
+def batch_instances(n=256, seed=0, nx=(8, 64), nyz=(2, 16), lam=(0.5, 2.0), mu=(0.5, 2.0),
+                    ell=(0.02, 0.2), L=(4.0, 1.0, 1.0), traction=1e-3, clamp=True):
+    """Seeded uneven beam instances of the linear strain-gradient law: nx
+    uniform in nx[0]..nx[1], ny = nz uniform in nyz[0]..nyz[1], lambda, mu,
+    length scale uniform in their ranges; clamped at x = 0, uniform traction
+    in -z at x = L (the 16x4x4 beam problem's boundary conditions)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    bct, neu = clamp_bc((0,) if clamp else (), traction_face=1, traction=(0.0, 0.0, -traction))
+    for _ in range(n):
+        ex = int(rng.integers(nx[0], nx[1] + 1))
+        eyz = int(rng.integers(nyz[0], nyz[1] + 1))
+        nelem = (ex, eyz, eyz)
+        knots, w, X = beam_mesh(nelem, L)
+        par = [rng.uniform(*lam), rng.uniform(*mu), rng.uniform(*ell), 0, 0, 0, 0, 0, 0]
+        out.append(dict(nelem=nelem, knots=knots, w=w, X=X, par=par, bc_type=bct, neumann=neu))
+    return out

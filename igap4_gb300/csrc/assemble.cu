@@ -19,6 +19,8 @@
 
 namespace igap {
 
+constexpr uint32_t BATCH_WAIT_LIMIT = 1u << 24;  // polls of a colour counter (~2 s)
+
 #define MTOL 1.e-15  // knot-span denominator shift of src/meshcore_iga.c:10,303-307
 
 constexpr int THREADS = 384;
@@ -68,7 +70,7 @@ __global__ void basis_table_kernel(const double *knots, int nelem, const double 
 
 // ------------------------------------------------------------ pattern
 __global__ void pattern_cols_kernel(const int64_t *rowptr, int32_t *cols, int64_t ndof, int nb0,
-                                    int nb1, int nb2)
+                                    int nb1, int nb2, int64_t coff)
 {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= ndof) return;
@@ -80,7 +82,7 @@ __global__ void pattern_cols_kernel(const int64_t *rowptr, int32_t *cols, int64_
     for (int jy = max(iy - P, 0); jy <= min(iy + P, nb1 - 1); jy++)
       for (int jz = max(iz - P, 0); jz <= min(iz + P, nb2 - 1); jz++) {
         int64_t cp = ((int64_t)jx * nb1 + jy) * nb2 + jz;
-        for (int e = 0; e < 3; e++) cols[s++] = (int32_t)(3 * cp + e);
+        for (int e = 0; e < 3; e++) cols[s++] = (int32_t)(coff + 3 * cp + e);
       }
 }
 
@@ -105,20 +107,16 @@ struct ElemSmem {
   double M[27 * 81];
 };
 
-template <int LAWK, bool RES, bool TAN>
-__global__ void __launch_bounds__(THREADS, 1)
-    element_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncy, int ncz,
-                   const double *__restrict__ Uhist, double *__restrict__ RR,
-                   double *__restrict__ vals)
+// One element: load, quadrature (phase A, B1, B2) and the scatter into RR /
+// vals.  COH: the read-modify-write of RR / vals bypasses L1 (a batched
+// launch orders colours inside one kernel, through L2).
+template <int LAWK, bool RES, bool TAN, bool COH>
+__device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, const DevMesh &m,
+                                             const DevLaw &L, int ex, int ey, int ez,
+                                             const double *__restrict__ Uhist, double *__restrict__ RR,
+                                             double *__restrict__ vals)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
-  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // element of this colour
-  const int b = blockIdx.x;
-  const int iz = b % ncz, iy = (b / ncz) % ncy, ix = b / (ncz * ncy);
-  const int ex = cx + 3 * ix, ey = cy + 3 * iy, ez = cz + 3 * iz;
   const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
   const int nh = L.nhist;
   // element data: weights, control points, state of every history level
@@ -193,7 +191,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int bb = tid / 3, d = tid % 3;
     const int i = bb / 9, j = (bb / 3) % 3, l = bb % 3;
     const int64_t cp = ((int64_t)(ex + i) * nb1 + (ey + j)) * nb2 + (ez + l);
-    RR[3 * cp + d] += racc;
+    double *dst = RR + m.dof_off + 3 * cp + d;
+    *dst = (COH ? __ldcg(dst) : *dst) + racc;
   }
   if (TAN && tid < NPAIR) {
     const int bi = pb / 9, bj = (pb / 3) % 3, bl = pb % 3;
@@ -206,9 +205,96 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int64_t pos_cb = stencil_pos(sx, sy, sz, rx, ry, rz, nbv);
     for (int d = 0; d < 3; d++)
       for (int e = 0; e < 3; e++) {
-        vals[m.rowptr[3 * cpb + d] + 3 * pos_bc + e] += acc[3 * d + e];
-        if (pb != pc) vals[m.rowptr[3 * cpc + e] + 3 * pos_cb + d] += acc[3 * d + e];
+        double *p1 = vals + m.rowptr[3 * cpb + d] + 3 * pos_bc + e;
+        *p1 = (COH ? __ldcg(p1) : *p1) + acc[3 * d + e];
+        if (pb != pc) {
+          double *p2 = vals + m.rowptr[3 * cpc + e] + 3 * pos_cb + d;
+          *p2 = (COH ? __ldcg(p2) : *p2) + acc[3 * d + e];
+        }
       }
+  }
+}
+
+template <int LAWK, bool RES, bool TAN>
+__global__ void __launch_bounds__(THREADS, 1)
+    element_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncy, int ncz,
+                   const double *__restrict__ Uhist, double *__restrict__ RR,
+                   double *__restrict__ vals)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
+  // element of this colour
+  const int b = blockIdx.x;
+  const int iz = b % ncz, iy = (b / ncz) % ncy, ix = b / (ncz * ncy);
+  element_body<LAWK, RES, TAN, false>(S, LS, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, Uhist, RR, vals);
+}
+
+// ------------------------------------------------- batched (persistent)
+// Waits (bounded) until *p >= target; acquire at GPU scope.
+__device__ __forceinline__ bool wait_count_ge(const int *p, int target)
+{
+  for (uint32_t i = 0; i < BATCH_WAIT_LIMIT; i++) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v >= target) return true;
+    __nanosleep(128);
+  }
+  return false;
+}
+
+// Persistent CTAs take elements of every instance from one colour-major
+// queue.  An element of colour k of instance i starts only after all its
+// instance's elements of colours < k are finished (a per-instance count
+// reaching the number of those elements); they sit earlier in the queue and
+// were taken by running CTAs, so every wait ends.  Each CSR slot and residual
+// row therefore receives its element contributions in colour order, exactly
+// as with one launch per colour.
+template <int LAWK, bool RES, bool TAN>
+__global__ void __launch_bounds__(THREADS, 1)
+    element_batch_kernel(BatchArgs a, const double *__restrict__ Uhist, double *__restrict__ RR,
+                         double *__restrict__ vals)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
+  __shared__ DevMesh sm;
+  __shared__ DevLaw sl;
+  __shared__ int64_t s_base;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x;
+  int cur = -1;
+  if (tid == 0) s_abort = 0;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_base = atomicAdd(a.head, a.grab);
+    __syncthreads();
+    const int64_t base = s_base;
+    if (base >= a.nitems || s_abort) break;
+    const int64_t end = base + a.grab < a.nitems ? base + a.grab : a.nitems;
+    for (int64_t it = base; it < end; it++) {
+      const BatchItem w = a.items[it];
+      if (w.inst != cur) {
+        __syncthreads();
+        if (tid == 0) {
+          sm = a.meshes[w.inst];
+          sl = a.laws[w.inst];
+        }
+        cur = w.inst;
+      }
+      if (tid == 0 && w.col > 0) {
+        if (!wait_count_ge(a.done + w.inst, a.need[27 * w.inst + w.col])) {
+          s_abort = 1;
+          atomicExch(a.err, 3);
+        }
+      }
+      __syncthreads();
+      if (s_abort) break;
+      element_body<LAWK, RES, TAN, true>(S, LS, sm, sl, w.ex, w.eyz >> 16, w.eyz & 0xffff, Uhist, RR, vals);
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) atomicAdd(a.done + w.inst, 1);
+    }
   }
 }
 
@@ -338,6 +424,53 @@ __global__ void dirichlet_matrix_kernel(const int64_t *rows, int64_t n, const in
   }
 }
 
+// MatZeroRowsColumns on the block-diagonal matrix of a batch: rows carry
+// their instance (inst), whose lattice is nbs[3*inst..] and first DOF dof_off[inst].
+__global__ void dirichlet_matrix_batch_kernel(const int64_t *rows, const int *inst, int64_t n,
+                                              const int64_t *rowptr, const int32_t *cols, const int *nbs,
+                                              const int64_t *dof_off, double *vals)
+{
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = inst[t];
+  const int nb[3] = {nbs[3 * i], nbs[3 * i + 1], nbs[3 * i + 2]};
+  const int64_t off = dof_off[i];
+  const int64_t r = rows[t], rl = r - off;
+  int ix, iy, iz;
+  cp_coords(rl / 3, nb, ix, iy, iz);
+  const int dr = (int)(rl % 3);
+  for (int64_t s = rowptr[r]; s < rowptr[r + 1]; s++) {
+    const int32_t c = cols[s];
+    vals[s] = (c == r) ? 1.0 : 0.0;
+    if (c == r) continue;
+    int jx, jy, jz;
+    cp_coords((c - off) / 3, nb, jx, jy, jz);
+    const int64_t pos = stencil_pos(jx, jy, jz, ix, iy, iz, nb);
+    vals[rowptr[c] + 3 * pos + dr] = 0.0;
+  }
+}
+
+int launch_dirichlet_matrix_batch(Context *c, const int *d_inst, const int *d_nbs, const int64_t *d_off,
+                                  double *vals)
+{
+  if (c->n_dir == 0) return IGAPGPU_OK;
+  dirichlet_matrix_batch_kernel<<<(unsigned)((c->n_dir + 127) / 128), 128, 0, c->stream>>>(
+      c->d_dir_rows, d_inst, c->n_dir, c->d_rowptr, c->d_cols, d_nbs, d_off, vals);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+int launch_pattern_cols_at(Context *c, const int64_t *rowptr, int32_t *cols, int64_t coff)
+{
+  const int64_t n = c->ndof;
+  pattern_cols_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
+      rowptr, cols, n, c->nbasis[0], c->nbasis[1], c->nbasis[2], coff);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
 // ------------------------------------------------------------ launches
 template <int LAWK, bool RES, bool TAN>
 static int run_colours(Context *c, double *RR, double *vals)
@@ -393,10 +526,70 @@ static int init_pairs()
   return IGAPGPU_OK;
 }
 
+template <int LAWK, bool RES, bool TAN>
+static int run_batch(Context *c, const BatchArgs &a, int grid, const double *Uhist, double *RR, double *vals)
+{
+  const size_t smem = sizeof(ElemSmem) + sizeof(LawSmem<LAWK>);
+  auto kern = element_batch_kernel<LAWK, RES, TAN>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  kern<<<grid, THREADS, smem, c->stream>>>(a, Uhist, RR, vals);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+template <int LAWK, bool RES, bool TAN>
+static int batch_occ(int *nb)
+{
+  const size_t smem = sizeof(ElemSmem) + sizeof(LawSmem<LAWK>);
+  auto kern = element_batch_kernel<LAWK, RES, TAN>;
+  IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  IGAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, kern, THREADS, smem));
+  return IGAPGPU_OK;
+}
+
+#define IGAP_BATCH_DISPATCH(FN, ...)                                                       \
+  switch (law) {                                                                         \
+  case IGAPGPU_LAW_LINGRAD:                                                              \
+    if (do_res && do_tan) return FN<0, true, true>(__VA_ARGS__);                         \
+    if (do_res) return FN<0, true, false>(__VA_ARGS__);                                  \
+    return FN<0, false, true>(__VA_ARGS__);                                              \
+  case IGAPGPU_LAW_GRADELAST:                                                            \
+    if (do_res && do_tan) return FN<1, true, true>(__VA_ARGS__);                         \
+    if (do_res) return FN<1, true, false>(__VA_ARGS__);                                  \
+    return FN<1, false, true>(__VA_ARGS__);                                              \
+  case IGAPGPU_LAW_GRADELASTTIME:                                                        \
+    if (do_res && do_tan) return FN<2, true, true>(__VA_ARGS__);                         \
+    if (do_res) return FN<2, true, false>(__VA_ARGS__);                                  \
+    return FN<2, false, true>(__VA_ARGS__);                                              \
+  default:                                                                               \
+    set_error("unknown law %d", law);                                                    \
+    return IGAPGPU_ERR_LAW;                                                              \
+  }
+
+int launch_element_batch(Context *c, const BatchArgs &a, int law, bool do_res, bool do_tan, int grid,
+                         const double *Uhist, double *RR, double *vals)
+{
+  int rc = init_pairs();
+  if (rc) return rc;
+  IGAP_BATCH_DISPATCH(run_batch, c, a, grid, Uhist, RR, vals)
+}
+
+int element_batch_occupancy(int law, bool do_res, bool do_tan, int *blocks_per_sm)
+{
+  IGAP_BATCH_DISPATCH(batch_occ, blocks_per_sm)
+}
+#undef IGAP_BATCH_DISPATCH
+
 int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals)
 {
   int rc = init_pairs();
   if (rc) return rc;
+  if (c->batch) return launch_batch_assembly(c, do_res, do_tan, RR, vals);
   if (do_res) {
     IGAP_CUDA(cudaMemcpyAsync(RR, c->d_Fneu, sizeof(double) * c->ndof, cudaMemcpyDeviceToDevice,
                               c->stream));
@@ -480,7 +673,7 @@ int launch_pattern_cols(Context *c)
 {
   const int64_t n = c->ndof;
   pattern_cols_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
-      c->d_rowptr, c->d_cols, n, c->nbasis[0], c->nbasis[1], c->nbasis[2]);
+      c->d_rowptr, c->d_cols, n, c->nbasis[0], c->nbasis[1], c->nbasis[2], 0);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;

@@ -50,8 +50,9 @@ struct DevMesh {
   const double *wq;        // [nquad] Gauss weights on [0,1]
   const double *w;         // [ncp]
   const double *X;         // [3*ncp]
-  const int64_t *rowptr;   // [ndof+1]
-  int64_t ndof;
+  const int64_t *rowptr;   // [ndof+1] (global CSR positions; a batch instance's rows)
+  int64_t ndof;            // stride between history levels of the state
+  int64_t dof_off;         // first DOF of this mesh in the state / residual vectors
   const double *geo;       // geometry cache [nelem][npts][272] or null
   const float *geof;       // FP32 copy of the geometry cache (split tangent) or null
 };
@@ -73,6 +74,29 @@ struct DevLaw {
 };
 
 struct GraphWork;
+struct Batch;
+
+// One work item of a batched launch: element (ex, ey, ez) of instance inst,
+// whose colour (ex mod 3, ey mod 3, ez mod 3) is col.
+struct BatchItem {
+  int inst;
+  int col;
+  int ex;
+  int eyz;  // ey << 16 | ez
+};
+
+// Arguments of the persistent batched kernels.
+struct BatchArgs {
+  const DevMesh *meshes;   // [ninst]
+  const DevLaw *laws;      // [ninst]
+  const BatchItem *items;  // colour-major work queue
+  int64_t nitems;
+  int *head;               // queue head (reset before each launch)
+  int *done;               // [ninst] finished items per instance
+  const int *need;         // [ninst*27] items of the instance in colours before each colour
+  int grab;                // items taken per fetch
+  int *err;                // device error word
+};
 
 struct Context {
   // problem
@@ -128,6 +152,11 @@ struct Context {
   cudaGraphExec_t asm_graph[8] = {};
   int64_t asm_graph_nodes[8] = {};
   bool capturing = false;
+  // batched instances (batch.cu): this context is then their block-diagonal union
+  Batch *batch = nullptr;
+  bool sub = false;  // an instance of a batch (no matrix or state of its own)
+  int geo_mode = -1;  // geometry cache: -1 by free memory, 0 none, 1 FP64, 2 FP64 + FP32
+  std::vector<int64_t> h_rowptr;  // host CSR offsets (kept for instances of a batch)
   // element-kernel timing (igapgpu_profile)
   bool prof = false;
   // per kernel kind: 0 = FP64 element kernel, 1 = tensor-core tangent kernel
@@ -148,6 +177,7 @@ struct Context {
     m.X = d_X;
     m.rowptr = d_rowptr;
     m.ndof = ndof;
+    m.dof_off = 0;
     m.geo = d_geo;
     m.geof = d_geof;
     return m;
@@ -172,6 +202,14 @@ struct Context {
 // Pointer classification: true if ptr is device (or managed) memory.
 bool is_device_ptr(const void *p);
 
+// context.cu
+int check_instance_args(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
+                        const igapgpu_bc_desc *bc, int nquad);
+Context *new_context(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
+                     const igapgpu_bc_desc *bc, int nquad);
+int context_init(Context *c, const igapgpu_mesh_desc *mesh);
+int context_free(Context *c);
+
 // assemble.cu
 int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
 int launch_basis_tables(Context *c);
@@ -181,6 +219,9 @@ int launch_dirichlet_matrix(Context *c, double *vals);
 int launch_dirichlet_residual(Context *c, double *RR);
 int launch_impose_dirichlet(Context *c, double *U);
 int launch_pattern_cols(Context *c);
+int launch_pattern_cols_at(Context *c, const int64_t *rowptr, int32_t *cols, int64_t coff);
+int launch_dirichlet_matrix_batch(Context *c, const int *d_inst, const int *d_nbs, const int64_t *d_off,
+                                  double *vals);
 int launch_geometry_cache(Context *c);
 int launch_geometry_cache_f32(Context *c);
 // tc_tangent.cu
@@ -190,6 +231,15 @@ int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
               double *rnorm);
 int dev_norm2(Context *c, const double *x, double *out);
+// batch.cu
+int launch_batch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
+void batch_release(Context *c);
+int batch_set_neumann(Context *c, const double *table);
+// element kernels over a batch work queue (assemble.cu, tc_tangent.cu)
+int launch_element_batch(Context *c, const BatchArgs &a, int law, bool do_res, bool do_tan, int grid,
+                         const double *Uhist, double *RR, double *vals);
+int launch_tc_batch(Context *c, const BatchArgs &a, int law, int grid, const double *Uhist, double *vals);
+int element_batch_occupancy(int law, bool do_res, bool do_tan, int *blocks_per_sm);
 // graph.cu
 int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
                     double *rnorm);

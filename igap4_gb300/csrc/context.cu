@@ -160,6 +160,7 @@ static int free_ctx(Context *c)
 {
   if (!c) return IGAPGPU_OK;
   graph_release(c);
+  batch_release(c);
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
@@ -206,8 +207,10 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
     set_error("no CUDA device: the GPU assembly has no CPU fallback");
     return IGAPGPU_ERR_CUDA;
   }
-  IGAP_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
-  c->stream = c->own_stream;
+  if (!c->sub) {  // an instance of a batch runs on the batch's stream
+    IGAP_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+  }
   // mesh
   std::vector<double> kn[3];
   for (int d = 0; d < 3; d++) {
@@ -242,13 +245,21 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
     size_t freeb = 0, totb = 0;
     IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
     const size_t need_other = (size_t)(3 * c->ncp) * 8 * 400;  // matrix, pattern, workspace (rough)
-    if (want && bytes + need_other + ((size_t)4 << 30) < freeb) {
+    bool use64, use32;
+    if (c->geo_mode >= 0) {  // decided by the caller (the instances of a batch)
+      use64 = want && c->geo_mode >= 1;
+      use32 = use64 && c->geo_mode >= 2;
+    } else {
+      use64 = want && bytes + need_other + ((size_t)4 << 30) < freeb;
+      use32 = use64 && bytes / 2 + need_other + ((size_t)4 << 30) < freeb - bytes;
+    }
+    if (use64) {
       if (cudaMalloc(&c->d_geo, bytes) != cudaSuccess) {
         cudaGetLastError();
         c->d_geo = nullptr;
       } else if ((r = launch_geometry_cache(c))) {
         return r;
-      } else if (bytes / 2 + need_other + ((size_t)4 << 30) < freeb - bytes) {
+      } else if (use32) {
         // FP32 copy used by the split-precision tangent
         if (cudaMalloc(&c->d_geof, bytes / 2) != cudaSuccess) {
           cudaGetLastError();
@@ -277,6 +288,12 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
     set_error("matrix too large");
     return IGAPGPU_ERR_ARG;
   }
+  if (c->sub) {  // the batch owns matrix, pattern and state
+    c->h_rowptr.swap(rowptr);
+    if ((r = dev_alloc(&c->d_Fneu, c->ndof))) return r;
+    if ((r = dev_alloc(&c->d_err, 1))) return r;
+    IGAP_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
+  } else {
   if ((r = dev_alloc(&c->d_rowptr, c->ndof + 1))) return r;
   if ((r = dev_alloc(&c->d_cols, c->nnz))) return r;
   if ((r = dev_alloc(&c->d_vals, c->nnz))) return r;
@@ -295,6 +312,7 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   if ((r = dev_alloc(&c->d_partial, 1024))) return r;
   IGAP_CUDA(cudaMallocHost(&c->h_red, 64 * sizeof(double)));
   c->red_cap = 64;
+  }
   // law constants
   if (c->law == IGAPGPU_LAW_LINGRAD) {
     if ((r = dev_alloc(&c->d_Dconst, 900))) return r;
@@ -416,21 +434,15 @@ static int set_current(Context *c, const double *U)
 
 }  // namespace igap
 
-using namespace igap;
+namespace igap {
 
-extern "C" {
-
-const char *igapgpu_last_error(void) { return g_err; }
-int64_t igapgpu_launch_count(void) { return g_launches.load(); }
-
-int igapgpu_assm_init(igapgpu_t *out, const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
-                      const igapgpu_bc_desc *bc, int nquad)
+int check_instance_args(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
+                        const igapgpu_bc_desc *bc, int nquad)
 {
-  if (!out || !mesh || !phys || !bc) {
+  if (!mesh || !phys || !bc) {
     set_error("null argument");
     return IGAPGPU_ERR_ARG;
   }
-  *out = nullptr;
   if (mesh->porder != P) {
     set_error("porder %d unsupported: the device basis is quadratic (as eval_Bspline)", mesh->porder);
     return IGAPGPU_ERR_ARG;
@@ -463,6 +475,12 @@ int igapgpu_assm_init(igapgpu_t *out, const igapgpu_mesh_desc *mesh, const igapg
       set_error("bc_type[%d] = %d; expected 0 (Dirichlet) or 1 (Neumann)", i, bc->bc_type[i]);
       return IGAPGPU_ERR_ARG;
     }
+  return IGAPGPU_OK;
+}
+
+Context *new_context(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
+                     const igapgpu_bc_desc *bc, int nquad)
+{
   igapgpu_ctx *c = new igapgpu_ctx();
   c->law = phys->law;
   c->torder = phys->law == IGAPGPU_LAW_GRADELASTTIME ? 2 : 0;
@@ -479,8 +497,34 @@ int igapgpu_assm_init(igapgpu_t *out, const igapgpu_mesh_desc *mesh, const igapg
     c->nelem_total *= c->nelem[d];
   }
   c->ndof = 3 * c->ncp;
+  return c;
+}
+
+int context_init(Context *c, const igapgpu_mesh_desc *mesh) { return init_impl(c, mesh); }
+int context_free(Context *c) { return free_ctx(c); }
+
+}  // namespace igap
+
+using namespace igap;
+
+extern "C" {
+
+const char *igapgpu_last_error(void) { return g_err; }
+int64_t igapgpu_launch_count(void) { return g_launches.load(); }
+
+int igapgpu_assm_init(igapgpu_t *out, const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phys,
+                      const igapgpu_bc_desc *bc, int nquad)
+{
+  if (!out) {
+    set_error("null argument");
+    return IGAPGPU_ERR_ARG;
+  }
+  *out = nullptr;
+  int r = check_instance_args(mesh, phys, bc, nquad);
+  if (r) return r;
+  Context *c = new_context(mesh, phys, bc, nquad);
   IGAP_TRY(init_impl(c, mesh));
-  *out = c;
+  *out = static_cast<igapgpu_ctx *>(c);
   return IGAPGPU_OK;
 }
 
@@ -637,6 +681,7 @@ int igapgpu_matmult(igapgpu_t c, const double *x, double *y)
 int igapgpu_set_neumann(igapgpu_t c, const double *table)
 {
   if (!c || !table) return IGAPGPU_ERR_ARG;
+  if (c->batch) return batch_set_neumann(c, table);
   for (int i = 0; i < 36; i++) c->bc.neumann[i] = table[i];
   return launch_neumann(c, c->nfac);
 }

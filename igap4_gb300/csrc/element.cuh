@@ -47,7 +47,7 @@ __device__ __forceinline__ void load_element(ElemData &E, const DevMesh &m, int 
     E.wV[t] = m.w[cp];
     for (int d = 0; d < 3; d++) E.XV[3 * t + d] = m.X[3 * cp + d];
     for (int h = 0; h < nh; h++)
-      for (int d = 0; d < 3; d++) E.U[h * NE + 3 * t + d] = Uhist[(int64_t)h * m.ndof + 3 * cp + d];
+      for (int d = 0; d < 3; d++) E.U[h * NE + 3 * t + d] = Uhist[(int64_t)h * m.ndof + m.dof_off + 3 * cp + d];
   }
 }
 

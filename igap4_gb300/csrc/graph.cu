@@ -389,11 +389,14 @@ int assembly_graph(Context *c, bool do_res, bool do_tan)
     }
     return IGAPGPU_OK;
   }
-  if (c->prec == IGAPGPU_PREC_SPLIT && do_tan) IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+  // the error word is cleared inside the graph; it is read after the replay
+  // when a kernel of the graph has bounded waits
+  const bool waits = c->batch || (c->prec == IGAPGPU_PREC_SPLIT && do_tan);
+  if (waits) IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
   IGAP_CUDA(cudaGraphLaunch(c->asm_graph[key], c->stream));
   count_launch((int)c->asm_graph_nodes[key]);
   if (do_tan) c->matrix_valid = true;
-  if (c->prec == IGAPGPU_PREC_SPLIT && do_tan) {
+  if (waits) {
     int herr = 0;
     IGAP_CUDA(cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     IGAP_CUDA(cudaStreamSynchronize(c->stream));

@@ -34,6 +34,18 @@ constexpr int B_PIECE = NKT * B_TILE;      // 5120 B
 constexpr uint32_t WAIT_LIMIT = 1u << 26;  // bounded polls of an mbarrier
 constexpr uint32_t TMEM_COLS = 64;
 
+// bounded acquire-wait until *p >= target (batched queue dependencies)
+__device__ __forceinline__ bool tc_wait_count_ge(const int *p, int target)
+{
+  for (uint32_t i = 0; i < (1u << 24); i++) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v >= target) return true;
+    __nanosleep(128);
+  }
+  return false;
+}
+
 // byte offset of (row r, k index kk8 in [0,8)) inside one 128-row (or 32-row)
 // block of a K-step: K-major, no swizzle, LBO = 128 B, SBO = 256 B
 __device__ __forceinline__ uint32_t kmajor_off(int r, int kk8)
@@ -56,6 +68,9 @@ struct TcSmem {
   int64_t rowp[NE];          // CSR row offsets of the element's 81 rows (b,d)
   float wtf[PW];             // quadrature weights (constant-tangent path)
   float Dc[900];             // constant tangent (FP32) of the linear law
+  DevMesh m;                 // mesh and law of the current element
+  DevLaw L;
+  int64_t base;              // batched launch: first queue item of this fetch
 };
 
 // ------------------------------------------------------------ self-test
@@ -106,14 +121,18 @@ __global__ void tc_selftest_kernel(int variant, float *out, int *err)
 }
 
 // ------------------------------------------------------ split tangent
-template <int LAWK>
+// BATCH: elements come from the colour-major queue of a batch (see
+// element_batch_kernel); otherwise the CTAs stride over one colour.
+template <int LAWK, bool BATCH>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_tangent_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz,
-                      const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
+    tc_tangent_kernel(DevMesh m_arg, DevLaw L_arg, int cx, int cy, int cz, int ncx, int ncy, int ncz,
+                      BatchArgs ba, const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
   LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(TcSmem));
+  const DevMesh &m = S.m;
+  const DevLaw &L = S.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (warp == 0) {
     tc::tmem_alloc(&S.taddr, TMEM_COLS);
@@ -122,6 +141,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (tid == 0) {
     tc::mbar_init(&S.mbar, 1);
     S.abort = 0;
+    if (!BATCH) {
+      S.m = m_arg;
+      S.L = L_arg;
+    }
   }
   // padding rows (243..255 of A, 27..31 of B) stay zero for the whole kernel
   for (int i = tid; i < (int)(sizeof(S.A) / 4); i += TC_THREADS) reinterpret_cast<float *>(S.A)[i] = 0.f;
@@ -133,20 +156,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t idesc = tc::instr_desc(2, 128, 32);
   const uint32_t a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
   uint32_t commits = 0;  // commits issued so far (uniform across the CTA)
-  const int nh = L.nhist;
-  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
-  const int nbv[3] = {m.nbasis[0], nb1, nb2};
   const int nelem_c = ncx * ncy * ncz;
-  const int nchunk = (m.npts + PW - 1) / PW;
-  // constant sparse tangent (linear law) with the FP32 geometry cache
-  const bool const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
-  if (const_d)
-    for (int i = tid; i < 900; i += TC_THREADS) S.Dc[i] = (float)L.Dconst[i];
+  bool const_d = false;
+  int cur = -1;             // batch instance whose mesh and law are loaded
+  int64_t it = 0, it_end = 0;
+  BatchItem w{};
+  if (!BATCH) {
+    __syncthreads();
+    // constant sparse tangent (linear law) with the FP32 geometry cache
+    const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
+    if (const_d)
+      for (int i = tid; i < 900; i += TC_THREADS) S.Dc[i] = (float)L.Dconst[i];
+  }
   __syncthreads();
 
-  for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
-    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
-    const int ex = cx + 3 * ix, ey = cy + 3 * iy, ez = cz + 3 * iz;
+  for (int ei = blockIdx.x;; ei += gridDim.x) {
+    int ex, ey, ez;
+    if (!BATCH) {
+      if (ei >= nelem_c) break;
+      const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+      ex = cx + 3 * ix;
+      ey = cy + 3 * iy;
+      ez = cz + 3 * iz;
+    } else {
+      if (it >= it_end) {  // next fetch from the queue
+        if (tid == 0) S.base = atomicAdd(ba.head, ba.grab);
+        __syncthreads();
+        it = S.base;
+        __syncthreads();
+        if (it >= ba.nitems) break;
+        it_end = it + ba.grab < ba.nitems ? it + ba.grab : ba.nitems;
+      }
+      w = ba.items[it++];
+      if (w.inst != cur) {
+        if (tid == 0) {
+          S.m = ba.meshes[w.inst];
+          S.L = ba.laws[w.inst];
+        }
+        __syncthreads();
+        cur = w.inst;
+        const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
+        if (const_d)
+          for (int i = tid; i < 900; i += TC_THREADS) S.Dc[i] = (float)L.Dconst[i];
+      }
+      if (tid == 0 && w.col > 0) {
+        if (!tc_wait_count_ge(ba.done + w.inst, ba.need[27 * w.inst + w.col])) {
+          S.abort = 1;
+          atomicExch(err, 3);
+        }
+      }
+      __syncthreads();
+      if (S.abort) goto done;
+      ex = w.ex;
+      ey = w.eyz >> 16;
+      ez = w.eyz & 0xffff;
+    }
+    const int nh = L.nhist;
+    const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+    const int nbv[3] = {m.nbasis[0], nb1, nb2};
+    const int nchunk = (m.npts + PW - 1) / PW;
     load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, TC_THREADS);
     if (tid < NE) {
       const int b = tid / 3, dd = tid % 3;
@@ -312,19 +380,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             slot[t] = S.rowp[3 * b + d] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
           }
 #pragma unroll
-          for (int t = 0; t < 9; t++) old[t] = vals[slot[t]];
+          for (int t = 0; t < 9; t++) old[t] = BATCH ? __ldcg(vals + slot[t]) : vals[slot[t]];
 #pragma unroll
           for (int t = 0; t < 9; t++) vals[slot[t]] = old[t] + (double)__uint_as_float(v[9 * bi + t]);
         }
       }
     }
+    if (BATCH) __threadfence();
     tc::fence_before_sync();
     __syncthreads();
+    if (BATCH && tid == 0) atomicAdd(ba.done + w.inst, 1);
   }
 done:
   tc::fence_before_sync();
   __syncthreads();
-  if (S.abort && tid == 0) atomicExch(err, 2);
+  if (S.abort && tid == 0) atomicCAS(err, 0, 2);
   if (warp == 0) tc::tmem_dealloc(taddr, TMEM_COLS);
 }
 
@@ -334,7 +404,7 @@ static int run_tc(Context *c, double *vals)
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
   const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
-  auto kern = tc_tangent_kernel<LAWK>;
+  auto kern = tc_tangent_kernel<LAWK, false>;
   static bool attr = false;
   if (!attr) {
     IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -357,8 +427,8 @@ static int run_tc(Context *c, double *vals)
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
         const int grid = nel < nsm ? nel : nsm;
-        kern<<<grid, TC_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, c->d_Uhist, vals,
-                                                    c->d_err);
+        kern<<<grid, TC_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, BatchArgs{}, c->d_Uhist,
+                                                    vals, c->d_err);
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
@@ -371,6 +441,31 @@ static int run_tc(Context *c, double *vals)
     c->prof_ev[1].emplace_back(e0, e1);
   }
   return IGAPGPU_OK;
+}
+
+template <int LAWK>
+static int run_tc_batch(Context *c, const BatchArgs &a, int grid, const double *Uhist, double *vals)
+{
+  const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
+  auto kern = tc_tangent_kernel<LAWK, true>;
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  kern<<<grid, TC_THREADS, smem, c->stream>>>(DevMesh{}, DevLaw{}, 0, 0, 0, 0, 0, 0, a, Uhist, vals, a.err);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+int launch_tc_batch(Context *c, const BatchArgs &a, int law, int grid, const double *Uhist, double *vals)
+{
+  if (law == IGAPGPU_LAW_LINGRAD) return run_tc_batch<0>(c, a, grid, Uhist, vals);
+  if (law == IGAPGPU_LAW_GRADELAST) return run_tc_batch<1>(c, a, grid, Uhist, vals);
+  if (law == IGAPGPU_LAW_GRADELASTTIME) return run_tc_batch<2>(c, a, grid, Uhist, vals);
+  set_error("unknown law %d", law);
+  return IGAPGPU_ERR_LAW;
 }
 
 int launch_tc_tangent(Context *c, double *vals)

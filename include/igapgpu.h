@@ -216,6 +216,41 @@ int igapgpu_tc_selftest(int variant, float *out);
  * kernel; used as the denominator of FP64-bound roofline fractions. */
 int igapgpu_measure_fp64_peak(double *tflops);
 
+
+/* ---------------------------------------------------------------------
+ * Batched instances (no counterpart in the reference): many independent
+ * beams assembled by one persistent launch per kernel.  The returned context
+ * is the block-diagonal union of the instances -- DOFs and CSR rows of
+ * instance i follow those of instance i-1 -- and every igapgpu_* call above
+ * applies to it (residual, tangent, solve, matmult, graphs, pattern, history,
+ * Dirichlet).  All instances share one law; parameters, meshes and boundary
+ * conditions are per instance.  igapgpu_set_neumann sets the same traction
+ * table on every instance.  Elements of all instances form one colour-major
+ * work queue; an element waits (bounded) until its instance's elements of the
+ * earlier colours are finished, so CSR slots receive contributions in the
+ * same order as the single-instance colour launches (bit-identical results). */
+typedef struct {
+  int grab_fp64;        /* elements per queue fetch, FP64 element kernel (>= 1) */
+  int ctas_per_sm_fp64; /* resident CTAs per SM (capped by the kernel's occupancy) */
+  int grab_tc;          /* elements per queue fetch, tensor-core tangent kernel */
+  int order;            /* 0: instances in input order within a colour; 1: largest first */
+} igapgpu_batch_schedule;
+
+int igapgpu_batch_init(igapgpu_t *ctx, int ninst, const igapgpu_mesh_desc *meshes,
+                       const igapgpu_phys_desc *phys, const igapgpu_bc_desc *bcs, int nquad);
+/* dof_off / elem_off: [ninst+1] prefix offsets (may be NULL). */
+int igapgpu_batch_info(igapgpu_t ctx, int *ninst, int64_t *dof_off, int64_t *elem_off);
+/* FP64 2-norm of each instance's segment of x (host or device), norms[ninst] host. */
+int igapgpu_batch_norms(igapgpu_t ctx, const double *x, double *norms);
+int igapgpu_batch_set_schedule(igapgpu_t ctx, const igapgpu_batch_schedule *s);
+int igapgpu_batch_get_schedule(igapgpu_t ctx, igapgpu_batch_schedule *s);
+/* Times candidate schedules of both kernels on the current state (each
+ * candidate runs `reps` times on a prefix of `frac` of the work queue), keeps
+ * the fastest and returns it; ms_fp64 / ms_tc: best time of each kernel on the
+ * prefix (may be NULL).  Leaves the context's residual and matrix invalid. */
+int igapgpu_batch_autotune(igapgpu_t ctx, int reps, double frac, igapgpu_batch_schedule *best,
+                           double *ms_fp64, double *ms_tc);
+
 /* ---- learned Newton predictor (no counterpart in the reference) --------
  * 3-D convolutional network on the control-point lattice (nx, ny, nz):
  * channels 9 -> 32 -> 32 -> 32 -> 3, 3x3x3 kernels, zero padding, ReLU after
