@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--spmv", type=int, default=200, help="SpMV repetitions")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch", type=int, default=256,
+                    help="instances of the batched workload (0 skips it)")
+    ap.add_argument("--batch-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -184,6 +187,91 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def bench_batched(ig, torch, dev, n, steps, warmup, flush, peaks):
+    """Batched uneven instances: n seeded linear-law beams (nx in 8..64,
+    ny = nz in 2..16, lambda, mu in [0.5, 2], length scale in [0.02, 0.2]),
+    split-precision tangent + FP64 residual, one persistent launch per kernel
+    per assembly; schedule from the autotuner; one Newton step (assembly and
+    GMRES cycles) replayed from CUDA graphs."""
+    t0 = time.perf_counter()
+    insts = ig.batch_instances(n, seed=SEED)
+    B = ig.BatchAssembly(insts, law=ig.LAW_LINGRAD)
+    t_init = time.perf_counter() - t0
+    B.set_precision(ig.PREC_SPLIT)
+    stream = torch.cuda.Stream(device=dev)
+    B.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(SEED + 7)
+    U = torch.tensor(rng.uniform(-1e-2, 1e-2, B.ndof), device=dev)
+    RR = torch.zeros(B.ndof, dtype=torch.float64, device=dev)
+    B.set_history(0, U)
+    t0 = time.perf_counter()
+    sched, t64, ttc = B.autotune(reps=2, frac=0.1)
+    t_tune = time.perf_counter() - t0
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            B.assemble(U, RR, None)
+    torch.cuda.synchronize()
+    l0 = ig.launch_count()
+    B.profile(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            B.assemble(U, RR, None)
+            evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ig.launch_count() - l0
+    kinds = {kd: B.profile_read(kd) for kd in (0, 1)}
+    B.profile(False)
+    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms_step = sum(ms) / steps
+    tc_ms, tc_l, tc_e = kinds[1]
+    res_ms, res_l, res_e = kinds[0]
+    tc_ach = TAN_FLOP_PER_ELEM * tc_e / (tc_ms * 1e-3) / 1e12 if tc_ms > 0 else None
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    # one Newton step of the block-diagonal system from zero: assembly, then a
+    # fixed budget of GMRES(100) iterations (Jacobi), replayed from CUDA graphs
+    B.set_stream(None)
+    Z = torch.zeros(B.ndof, dtype=torch.float64, device=dev)
+    kits = 200
+    opts = dict(snes_abstol=1e-300, ksp_rtol=1e-14, ksp_restart=100, ksp_max_it=kits, snes_max_it=1,
+                use_graphs=1, pc=1, linesearch=0)
+    F0 = torch.zeros_like(Z)
+    B.residual(Z, F0)
+    n0 = B.norms(F0)
+    B.solve(Z.clone(), **opts)  # first call captures the graphs
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = B.solve(Z, **opts)
+    B.synchronize()
+    t_newton = time.perf_counter() - t0
+    B.residual(Z, F0)
+    n1 = B.norms(F0)
+    red = n1 / np.maximum(n0, 1e-300)
+    out = {"workload": f"{n} seeded uneven quadratic beams (nx 8..64, ny=nz 2..16), linear law with "
+                       "per-instance lambda, mu in [0.5,2], ell in [0.02,0.2]; clamped x=0, traction 1e-3",
+           "instances": n, "elements": B.nelem_total, "dof": B.ndof, "nnz": B.nnz,
+           "precision": "split tangent (tcgen05 TF32x3, f32 accumulate) + f64 residual",
+           "value": B.nelem_total / (ms_step * 1e-3), "unit": "elements/s", "ms_per_step": ms_step,
+           "step_ms": ms, "steps": steps, "gpu_launches_per_step": launches / steps,
+           "tc_kernel_ms_per_step": tc_ms / steps, "fp64_residual_kernel_ms_per_step": res_ms / steps,
+           "schedule": sched, "autotune_s": t_tune, "autotune_prefix_ms": {"fp64": t64, "tc": ttc},
+           "init_s": t_init,
+           "roofline": {"bound": "tensor", "kernel": "tc_tangent_kernel<batch>", "achieved": tc_ach,
+                        "peak": bf16_peak, "unit": "TFLOP/s",
+                        "frac": tc_ach / bf16_peak if tc_ach else None},
+           "newton_step": {"seconds": t_newton, "newton_its": st["newton_its"], "ksp_its": st["ksp_its_total"],
+                           "ms_per_ksp_it": None if not st["ksp_its_total"] else
+                           1e3 * t_newton / st["ksp_its_total"],
+                           "instance_residual_reduction": {"median": float(np.median(red)),
+                                                           "max": float(np.max(red))},
+                           "options": f"one Newton step from U=0: assembly then {kits} GMRES(100) MGS "
+                                      "iterations with Jacobi, replayed from CUDA graphs"}}
+    B.close()
+    return out
 
 
 def main():
@@ -333,6 +421,14 @@ def main():
     peaks = _peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = ig.measure_fp64_peak()
+    nelem_total, ndof_total, nnz_total = A.nelem_total, A.ndof, A.nnz
+    A.close()  # frees the beam's matrix and geometry cache before the batched workload
+    del x, y
+    batched = None
+    if a.batch > 0:
+        sampler.start()
+        batched = bench_batched(ig, torch, dev, a.batch, a.batch_steps, max(3, a.warmup), flush, peaks)
+        sampler.stop()
     elem_kernel_ms = elem_ms / max(elem_launches, 1)
     flop_per_launch = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) * elem_count / max(elem_launches, 1)
     achieved = flop_per_launch / (elem_kernel_ms * 1e-3) / 1e12
@@ -353,7 +449,7 @@ def main():
             "dtype": "f64" if a.prec != "split" else "tf32x3/f32-acc tangent, f64 residual",
             "data": "synthetic",
             "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} "
-                                   f"({A.nelem_total} elements, {A.ndof} DOF, nnz {A.nnz}) "
+                                   f"({nelem_total} elements, {ndof_total} DOF, nnz {nnz_total}) "
                                    "residual Vec + CSR tangent assembly",
                        "law": "linear isotropic strain gradient lambda=1 mu=1 ell=0.1",
                        "quadrature": "4x4x4 Gauss", "bc": "clamped x=0, traction 1e-3 in -z at x=4",
@@ -361,8 +457,8 @@ def main():
                        "precision": "fp64" if a.prec != "split" else "split",
                        "l2": "flushed (256 MiB write) before every timed step; the 1.25 GB CSR output also exceeds L2",
                        "parallelism": f"replicas x{world}"},
-            "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": A.ndof * 8,
-                    "d2h_bytes_per_step": A.ndof * 8,
+            "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": ndof_total * 8,
+                    "d2h_bytes_per_step": ndof_total * 8,
                     "note": "state H2D from pinned host memory, residual D2H; tangent kept in the device matrix"},
             "gpu_launches": launches,
             "roofline": roofline,
@@ -371,6 +467,7 @@ def main():
                      "repetitions": a.spmv},
             "cpu_baseline": cpu,
             "split": split,
+            "batched": batched,
             "clocks": sampler.summary(local),
             "step_ms": step_ms,
             "wall_s": t_wall,

@@ -205,10 +205,10 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
     const int64_t pos_cb = stencil_pos(sx, sy, sz, rx, ry, rz, nbv);
     for (int d = 0; d < 3; d++)
       for (int e = 0; e < 3; e++) {
-        double *p1 = vals + m.rowptr[3 * cpb + d] + 3 * pos_bc + e;
+        double *p1 = vals + __ldg(m.rowptr + 3 * cpb + d) + 3 * pos_bc + e;
         *p1 = (COH ? __ldcg(p1) : *p1) + acc[3 * d + e];
         if (pb != pc) {
-          double *p2 = vals + m.rowptr[3 * cpc + e] + 3 * pos_cb + d;
+          double *p2 = vals + __ldg(m.rowptr + 3 * cpc + e) + 3 * pos_cb + d;
           *p2 = (COH ? __ldcg(p2) : *p2) + acc[3 * d + e];
         }
       }
@@ -231,6 +231,13 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ------------------------------------------------- batched (persistent)
+// Publishes the CTA's finished element: the barrier before the call orders
+// every thread's stores before this thread's release at GPU scope.
+__device__ __forceinline__ void release_add(int *p, int v)
+{
+  asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Waits (bounded) until *p >= target; acquire at GPU scope.
 __device__ __forceinline__ bool wait_count_ge(const int *p, int target)
 {
@@ -244,7 +251,8 @@ __device__ __forceinline__ bool wait_count_ge(const int *p, int target)
 }
 
 // Persistent CTAs take elements of every instance from one colour-major
-// queue.  An element of colour k of instance i starts only after all its
+// queue (a CTA reserves its next fetch while it works on the current one;
+// items are reserved only by running CTAs, in queue order).  An element of colour k of instance i starts only after all its
 // instance's elements of colours < k are finished (a per-instance count
 // reaching the number of those elements); they sit earlier in the queue and
 // were taken by running CTAs, so every wait ends.  Each CSR slot and residual
@@ -258,28 +266,32 @@ __global__ void __launch_bounds__(THREADS, 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
   LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
-  __shared__ DevMesh sm;
-  __shared__ DevLaw sl;
   __shared__ int64_t s_base;
   __shared__ int s_abort;
   const int tid = threadIdx.x;
   int cur = -1;
-  if (tid == 0) s_abort = 0;
+  DevMesh m;  // current instance, in registers
+  DevLaw L;
+  // the queue position of the following fetch is taken one fetch ahead, so
+  // the atomic's round trip overlaps the current elements
+  int64_t next = 0;
+  if (tid == 0) {
+    s_abort = 0;
+    next = atomicAdd(a.head, a.grab);
+  }
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_base = atomicAdd(a.head, a.grab);
+    if (tid == 0) s_base = next;
     __syncthreads();
     const int64_t base = s_base;
     if (base >= a.nitems || s_abort) break;
+    if (tid == 0) next = atomicAdd(a.head, a.grab);
     const int64_t end = base + a.grab < a.nitems ? base + a.grab : a.nitems;
     for (int64_t it = base; it < end; it++) {
       const BatchItem w = a.items[it];
       if (w.inst != cur) {
-        __syncthreads();
-        if (tid == 0) {
-          sm = a.meshes[w.inst];
-          sl = a.laws[w.inst];
-        }
+        m = a.meshes[w.inst];
+        L = a.laws[w.inst];
         cur = w.inst;
       }
       if (tid == 0 && w.col > 0) {
@@ -290,10 +302,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       __syncthreads();
       if (s_abort) break;
-      element_body<LAWK, RES, TAN, true>(S, LS, sm, sl, w.ex, w.eyz >> 16, w.eyz & 0xffff, Uhist, RR, vals);
-      __threadfence();
+      element_body<LAWK, RES, TAN, true>(S, LS, m, L, w.ex, w.eyz >> 16, w.eyz & 0xffff, Uhist, RR, vals);
       __syncthreads();
-      if (tid == 0) atomicAdd(a.done + w.inst, 1);
+      if (tid == 0) release_add(a.done + w.inst, 1);
     }
   }
 }

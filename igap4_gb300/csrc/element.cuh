@@ -1,5 +1,9 @@
 // Per-element data and the per-quadrature-point set-up (phase A) shared by
 // the FP64 element kernel and the tensor-core split-precision kernel.
+// Mesh, tables, geometry cache, state and law constants are read-only during
+// an assembly and are loaded through the read-only path (__ldg), also in the
+// batched kernels whose queue atomics would otherwise hide that from the
+// compiler.
 #pragma once
 #include "common.cuh"
 #include "laws.cuh"
@@ -44,10 +48,11 @@ __device__ __forceinline__ void load_element(ElemData &E, const DevMesh &m, int 
   for (int t = tid; t < NB; t += nthreads) {
     const int i = t / 9, j = (t / 3) % 3, l = t % 3;
     const int64_t cp = ((int64_t)(ex + i) * nb1 + (ey + j)) * nb2 + (ez + l);
-    E.wV[t] = m.w[cp];
-    for (int d = 0; d < 3; d++) E.XV[3 * t + d] = m.X[3 * cp + d];
+    E.wV[t] = __ldg(m.w + cp);
+    for (int d = 0; d < 3; d++) E.XV[3 * t + d] = __ldg(m.X + 3 * cp + d);
     for (int h = 0; h < nh; h++)
-      for (int d = 0; d < 3; d++) E.U[h * NE + 3 * t + d] = Uhist[(int64_t)h * m.ndof + m.dof_off + 3 * cp + d];
+      for (int d = 0; d < 3; d++)
+        E.U[h * NE + 3 * t + d] = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
   }
 }
 
@@ -84,9 +89,9 @@ __device__ inline double point_geometry(const ElemData &E, PointScratch &P, cons
   // (a) tensor-product basis, src/meshcore_iga.c:311-326
   if (lane < NB) {
     const int i = lane / 9, j = (lane / 3) % 3, l = lane % 3;
-    const double nx = tx[i], dx = tx[P1 + i], ddx = tx[2 * P1 + i];
-    const double ny = ty[j], dy = ty[P1 + j], ddy = ty[2 * P1 + j];
-    const double nz = tz[l], dz = tz[P1 + l], ddz = tz[2 * P1 + l];
+    const double nx = __ldg(tx + i), dx = __ldg(tx + P1 + i), ddx = __ldg(tx + 2 * P1 + i);
+    const double ny = __ldg(ty + j), dy = __ldg(ty + P1 + j), ddy = __ldg(ty + 2 * P1 + j);
+    const double nz = __ldg(tz + l), dz = __ldg(tz + P1 + l), ddz = __ldg(tz + 2 * P1 + l);
     double *o = R + NDD * lane;
     o[0] = nx * ny * nz;
     o[1] = dx * ny * nz;
@@ -170,7 +175,8 @@ __device__ inline double point_geometry(const ElemData &E, PointScratch &P, cons
       }
   }
   __syncwarp();
-  return m.wq[qx] * m.wq[qy] * m.wq[qz] * tx[3 * P1 + 1] * ty[3 * P1 + 1] * tz[3 * P1 + 1] * detG;
+  return __ldg(m.wq + qx) * __ldg(m.wq + qy) * __ldg(m.wq + qz) * __ldg(tx + 3 * P1 + 1) * __ldg(ty + 3 * P1 + 1) *
+         __ldg(tz + 3 * P1 + 1) * detG;
 }
 
 // Outputs: R[27*10] physical basis, rr[30] weighted residual integrand,
@@ -193,8 +199,8 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
   if (m.geo) {
     const int64_t e = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
     const double *g = m.geo + (e * m.npts + q) * GEO_STRIDE;
-    for (int i = lane; i < NB * NDD; i += 32) R[i] = g[i];
-    wt = g[NB * NDD];
+    for (int i = lane; i < NB * NDD; i += 32) R[i] = __ldg(g + i);
+    wt = __ldg(g + NB * NDD);
     __syncwarp();
   } else {
     wt = point_geometry(E, P, m, ex, ey, ez, q, lane, R);
@@ -217,14 +223,15 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
     if (RES && lane < 30) {
       double s = 0.0;
       if (L.dptr) {  // sparse constant tangent
-        for (int j = L.dptr[lane]; j < L.dptr[lane + 1]; j++) s += L.dval[j] * u[L.dcol[j]];
+        const int j1 = __ldg(L.dptr + lane + 1);
+        for (int j = __ldg(L.dptr + lane); j < j1; j++) s += __ldg(L.dval + j) * u[__ldg(L.dcol + j)];
       } else {
-        for (int j = 0; j < 30; j++) s += Dconst[30 * lane + j] * u[j];
+        for (int j = 0; j < 30; j++) s += __ldg(Dconst + 30 * lane + j) * u[j];
       }
       rr[lane] = wt * s;
     }
     if (TAN)
-      for (int i = lane; i < 900; i += 32) D[i] = (DT)(wt * Dconst[i]);
+      for (int i = lane; i < 900; i += 32) D[i] = (DT)(wt * __ldg(Dconst + i));
     __syncwarp();
   } else if constexpr (LAWK == 1) {
     gradelast_warp<1, RES, TAN, DT>(P.u, L.par, false, wt, rr, D, LS.s[w], lane);

@@ -68,8 +68,6 @@ struct TcSmem {
   int64_t rowp[NE];          // CSR row offsets of the element's 81 rows (b,d)
   float wtf[PW];             // quadrature weights (constant-tangent path)
   float Dc[900];             // constant tangent (FP32) of the linear law
-  DevMesh m;                 // mesh and law of the current element
-  DevLaw L;
   int64_t base;              // batched launch: first queue item of this fetch
 };
 
@@ -121,19 +119,202 @@ __global__ void tc_selftest_kernel(int variant, float *out, int *err)
 }
 
 // ------------------------------------------------------ split tangent
-// BATCH: elements come from the colour-major queue of a batch (see
-// element_batch_kernel); otherwise the CTAs stride over one colour.
-template <int LAWK, bool BATCH>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_tangent_kernel(DevMesh m_arg, DevLaw L_arg, int cx, int cy, int cz, int ncx, int ncy, int ncz,
-                      BatchArgs ba, const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
+// One element on the tensor cores: phase A (FP32 basis and tangent
+// integrand), stage 1 and B operands in shared memory, tcgen05 MMAs into
+// TMEM, epilogue scatter into the CSR values.  `commits` counts the MMA
+// commits of the CTA (mbarrier phase).  Returns false when a bounded wait
+// expired (S.abort set).  COH: the CSR read-modify-write bypasses L1.
+template <int LAWK, bool COH>
+__device__ __forceinline__ bool tc_element(TcSmem &S, LawSmem<LAWK> &LS, const DevMesh &m, const DevLaw &L,
+                                           int ex, int ey, int ez, bool const_d,
+                                           const double *__restrict__ Uhist, double *__restrict__ vals,
+                                           uint32_t taddr, uint32_t idesc, uint32_t a_base, uint32_t b_base,
+                                           uint32_t &commits)
 {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
-  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(TcSmem));
-  const DevMesh &m = S.m;
-  const DevLaw &L = S.L;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nh = L.nhist;
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  const int nbv[3] = {m.nbasis[0], nb1, nb2};
+  const int nchunk = (m.npts + PW - 1) / PW;
+  load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, TC_THREADS);
+  if (tid < NE) {
+    const int b = tid / 3, dd = tid % 3;
+    const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    S.rowp[tid] = __ldg(m.rowptr + 3 * cpb + dd);
+  }
+  __syncthreads();
+  bool first = true;
+  for (int ch = 0; ch < nchunk; ch++) {
+    // phase A: 8 points, one warp each
+    if (const_d) {  // FP32 cached basis and weight; the tangent is constant
+      const int q = ch * PW + warp;
+      if (q < m.npts) {
+        const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+        const float *g = m.geof + (eg * m.npts + q) * GEO_STRIDE;
+        for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = __ldg(g + i);
+        if (lane == 0) S.wtf[warp] = __ldg(g + NB * NDD);
+      } else {
+        for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = 0.f;
+        if (lane == 0) S.wtf[warp] = 0.f;
+      }
+    } else {  // FP64 geometry, FP32 tangent integrand
+      point_setup<LAWK, false, true, float>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp,
+                                            ch * PW + warp, lane, S.R[warp], nullptr, S.Dwf[warp]);
+      for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = (float)S.R[warp][i];
+    }
+    __syncthreads();
+    for (int kg = 0; kg < 2; kg++) {
+      // the previous chunk's MMAs must be done before A/B are overwritten
+      if (commits > 0) {
+        if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
+      }
+      __syncthreads();
+      if (S.abort) return false;
+      // stage 1 (rows (d,c,e)) and B (rows b); columns kk = kq*8 + pt.
+      // Loop order: 4 points at a time (R rows in registers), then the 5
+      // derivative slots of this group; float4 stores of 4 points.
+      if (tid < 243 && const_d) {
+        // A = w_q * sum_l D[(d,k),(e,l)] R_q[c,l] with the constant D row
+        // loaded once for the 4 points of a half
+        const int d = tid / 81, c = (tid % 81) / 3, e = tid % 3;
+        const int r = tid, mt = r >> 7;
+        for (int half = 0; half < 2; half++) {
+          float rc[4][NDD], wq[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            wq[j] = S.wtf[half * 4 + j];
+#pragma unroll
+            for (int l = 0; l < NDD; l++) rc[j][l] = S.Rf[half * 4 + j][NDD * c + l];
+          }
+          for (int kq = 0; kq < 5; kq++) {
+            const int k = kg * 5 + kq;
+            float dr[NDD];
+#pragma unroll
+            for (int l = 0; l < NDD; l++) dr[l] = S.Dc[30 * (10 * d + k) + 10 * e + l];
+            float4 hi, lo;
+            float *ph = &hi.x, *pl = &lo.x;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              float sacc = 0.f;
+#pragma unroll
+              for (int l = 0; l < NDD; l++) sacc = fmaf(dr[l], rc[j][l], sacc);
+              sacc *= wq[j];
+              const float h = tc::to_tf32(sacc);
+              ph[j] = h;
+              pl[j] = tc::to_tf32(sacc - h);
+            }
+            const uint32_t off = (uint32_t)((kq * 2 + mt) * A_TILE) + kmajor_off(r & 127, half * 4);
+            *reinterpret_cast<float4 *>(S.A + off) = hi;
+            *reinterpret_cast<float4 *>(S.A + A_PIECE + off) = lo;
+          }
+        }
+      } else if (tid < 243) {
+        const int d = tid / 81, c = (tid % 81) / 3, e = tid % 3;
+        const int r = tid, mt = r >> 7;
+        for (int half = 0; half < 2; half++) {
+          float rc[4][NDD];
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int l = 0; l < NDD; l++) rc[j][l] = S.Rf[half * 4 + j][NDD * c + l];
+          for (int kq = 0; kq < 5; kq++) {
+            const int k = kg * 5 + kq;
+            float4 hi, lo;
+            float *ph = &hi.x, *pl = &lo.x;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const float *drow = S.Dwf[half * 4 + j] + 30 * (10 * d + k) + 10 * e;
+              float sacc = 0.f;
+#pragma unroll
+              for (int l = 0; l < NDD; l++) sacc = fmaf(drow[l], rc[j][l], sacc);
+              const float h = tc::to_tf32(sacc);
+              ph[j] = h;
+              pl[j] = tc::to_tf32(sacc - h);
+            }
+            const uint32_t off = (uint32_t)((kq * 2 + mt) * A_TILE) + kmajor_off(r & 127, half * 4);
+            *reinterpret_cast<float4 *>(S.A + off) = hi;
+            *reinterpret_cast<float4 *>(S.A + A_PIECE + off) = lo;
+          }
+        }
+      }
+      if (tid < NB) {
+        const int b = tid;
+        for (int kq = 0; kq < 5; kq++) {
+          const int k = kg * 5 + kq;
+          for (int half = 0; half < 2; half++) {
+            float4 hi, lo;
+            float *ph = &hi.x, *pl = &lo.x;
+            for (int j = 0; j < 4; j++) {
+              const float s = S.Rf[half * 4 + j][NDD * b + k];
+              const float h = tc::to_tf32(s);
+              ph[j] = h;
+              pl[j] = tc::to_tf32(s - h);
+            }
+            const uint32_t off = (uint32_t)(kq * B_TILE) + kmajor_off(b, half * 4);
+            *reinterpret_cast<float4 *>(S.B + off) = hi;
+            *reinterpret_cast<float4 *>(S.B + B_PIECE + off) = lo;
+          }
+        }
+      }
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        for (int kt = 0; kt < NKT; kt++)
+          for (int mt = 0; mt < 2; mt++)
+            for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
+              const int pa = (pp == 2) ? 1 : 0, pb = (pp == 1) ? 1 : 0;
+              const uint64_t ad = tc::smem_desc(a_base + pa * A_PIECE + (kt * 2 + mt) * A_TILE, 128, 256);
+              const uint64_t bd = tc::smem_desc(b_base + pb * B_PIECE + kt * B_TILE, 128, 256);
+              const uint32_t acc = (first && kt == 0 && pp == 0) ? 0u : 1u;
+              tc::mma_tf32(taddr + (uint32_t)(mt * 32), ad, bd, idesc, acc);
+            }
+        tc::mma_commit(&S.mbar);
+      }
+      commits++;
+      first = false;
+    }
+    __syncthreads();  // Rf / Dwf of this chunk are no longer read after the next wait
+  }
+  // epilogue: wait for the element's last MMAs, read TMEM, scatter
+  if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
+  tc::fence_after_sync();
+  __syncthreads();
+  if (S.abort) return false;
+  {
+    // warp w reads tile (w / 4), TMEM lane quarter (w % 4)
+    const int mt = warp >> 2, quarter = warp & 3;
+    uint32_t v[32];
+    tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * 32), v);
+    const int r = mt * 128 + quarter * 32 + lane;
+    if (r < 243) {
+      const int d = r / 81, c = (r % 81) / 3, e = r % 3;
+      const int sx = ex + c / 9, sy = ey + (c / 3) % 3, sz = ez + c % 3;
+      for (int bi = 0; bi < 3; bi++) {  // 9 rows b at a time: loads first, then stores
+        int64_t slot[9];
+        double old[9];
+#pragma unroll
+        for (int t = 0; t < 9; t++) {
+          const int b = 9 * bi + t;
+          const int rx = ex + bi, ry = ey + t / 3, rz = ez + t % 3;
+          slot[t] = S.rowp[3 * b + d] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
+        }
+#pragma unroll
+        for (int t = 0; t < 9; t++) old[t] = COH ? __ldcg(vals + slot[t]) : vals[slot[t]];
+#pragma unroll
+        for (int t = 0; t < 9; t++) vals[slot[t]] = old[t] + (double)__uint_as_float(v[9 * bi + t]);
+      }
+    }
+  }
+  return true;
+}
+
+// TMEM allocation, mbarrier, zero padding rows (243..255 of A, 27..31 of B
+// stay zero for the whole kernel).
+__device__ __forceinline__ void tc_setup(TcSmem &S)
+{
+  const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) {
     tc::tmem_alloc(&S.taddr, TMEM_COLS);
     tc::tmem_relinquish();
@@ -141,59 +322,91 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (tid == 0) {
     tc::mbar_init(&S.mbar, 1);
     S.abort = 0;
-    if (!BATCH) {
-      S.m = m_arg;
-      S.L = L_arg;
-    }
   }
-  // padding rows (243..255 of A, 27..31 of B) stay zero for the whole kernel
   for (int i = tid; i < (int)(sizeof(S.A) / 4); i += TC_THREADS) reinterpret_cast<float *>(S.A)[i] = 0.f;
   for (int i = tid; i < (int)(sizeof(S.B) / 4); i += TC_THREADS) reinterpret_cast<float *>(S.B)[i] = 0.f;
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+}
+
+__device__ __forceinline__ void tc_teardown(TcSmem &S, uint32_t taddr, int *err)
+{
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort && threadIdx.x == 0) atomicCAS(err, 0, 2);
+  if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(taddr, TMEM_COLS);
+}
+
+// One persistent CTA per SM walks the elements of one colour.
+template <int LAWK>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_tangent_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz,
+                      const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(TcSmem));
+  const int tid = threadIdx.x;
+  tc_setup(S);
   const uint32_t taddr = S.taddr;
   const uint32_t idesc = tc::instr_desc(2, 128, 32);
   const uint32_t a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
   uint32_t commits = 0;  // commits issued so far (uniform across the CTA)
   const int nelem_c = ncx * ncy * ncz;
-  bool const_d = false;
-  int cur = -1;             // batch instance whose mesh and law are loaded
-  int64_t it = 0, it_end = 0;
-  BatchItem w{};
-  if (!BATCH) {
-    __syncthreads();
-    // constant sparse tangent (linear law) with the FP32 geometry cache
-    const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
-    if (const_d)
-      for (int i = tid; i < 900; i += TC_THREADS) S.Dc[i] = (float)L.Dconst[i];
-  }
+  // constant sparse tangent (linear law) with the FP32 geometry cache
+  const bool const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
+  if (const_d)
+    for (int i = tid; i < 900; i += TC_THREADS) S.Dc[i] = (float)L.Dconst[i];
   __syncthreads();
+  for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    if (!tc_element<LAWK, false>(S, LS, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, const_d, Uhist, vals, taddr,
+                                 idesc, a_base, b_base, commits))
+      break;
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  tc_teardown(S, taddr, err);
+}
 
-  for (int ei = blockIdx.x;; ei += gridDim.x) {
-    int ex, ey, ez;
-    if (!BATCH) {
-      if (ei >= nelem_c) break;
-      const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
-      ex = cx + 3 * ix;
-      ey = cy + 3 * iy;
-      ez = cz + 3 * iz;
-    } else {
-      if (it >= it_end) {  // next fetch from the queue
-        if (tid == 0) S.base = atomicAdd(ba.head, ba.grab);
-        __syncthreads();
-        it = S.base;
-        __syncthreads();
-        if (it >= ba.nitems) break;
-        it_end = it + ba.grab < ba.nitems ? it + ba.grab : ba.nitems;
-      }
-      w = ba.items[it++];
+// Batched launch: elements come from the colour-major queue of a batch (see
+// element_batch_kernel); mesh and law of the current instance live in shared
+// memory.
+template <int LAWK>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_batch_kernel(BatchArgs ba, const double *__restrict__ Uhist, double *__restrict__ vals)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(TcSmem));
+  const int tid = threadIdx.x;
+  tc_setup(S);
+  const uint32_t taddr = S.taddr;
+  const uint32_t idesc = tc::instr_desc(2, 128, 32);
+  const uint32_t a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
+  uint32_t commits = 0;
+  bool const_d = false;
+  int cur = -1;
+  DevMesh m;  // current instance, in registers
+  DevLaw L;
+  int64_t next = 0;  // queue position of the following fetch, reserved one fetch ahead
+  if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+  for (;;) {
+    if (tid == 0) S.base = next;
+    __syncthreads();
+    const int64_t base = S.base;
+    __syncthreads();
+    if (base >= ba.nitems || S.abort) break;
+    if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+    const int64_t end = base + ba.grab < ba.nitems ? base + ba.grab : ba.nitems;
+    bool ok = true;
+    for (int64_t it = base; it < end && ok; it++) {
+      const BatchItem w = ba.items[it];
       if (w.inst != cur) {
-        if (tid == 0) {
-          S.m = ba.meshes[w.inst];
-          S.L = ba.laws[w.inst];
-        }
-        __syncthreads();
+        __syncthreads();  // the previous instance's constant tangent is no longer read
+        m = ba.meshes[w.inst];
+        L = ba.laws[w.inst];
         cur = w.inst;
         const_d = (LAWK == 0) && m.geof != nullptr && L.Dconst != nullptr;
         if (const_d)
@@ -202,200 +415,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (tid == 0 && w.col > 0) {
         if (!tc_wait_count_ge(ba.done + w.inst, ba.need[27 * w.inst + w.col])) {
           S.abort = 1;
-          atomicExch(err, 3);
+          atomicExch(ba.err, 3);
         }
       }
       __syncthreads();
-      if (S.abort) goto done;
-      ex = w.ex;
-      ey = w.eyz >> 16;
-      ez = w.eyz & 0xffff;
-    }
-    const int nh = L.nhist;
-    const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
-    const int nbv[3] = {m.nbasis[0], nb1, nb2};
-    const int nchunk = (m.npts + PW - 1) / PW;
-    load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, TC_THREADS);
-    if (tid < NE) {
-      const int b = tid / 3, dd = tid % 3;
-      const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
-      S.rowp[tid] = m.rowptr[3 * cpb + dd];
-    }
-    __syncthreads();
-    bool first = true;
-    for (int ch = 0; ch < nchunk; ch++) {
-      // phase A: 8 points, one warp each
-      if (const_d) {  // FP32 cached basis and weight; the tangent is constant
-        const int q = ch * PW + warp;
-        if (q < m.npts) {
-          const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
-          const float *g = m.geof + (eg * m.npts + q) * GEO_STRIDE;
-          for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = g[i];
-          if (lane == 0) S.wtf[warp] = g[NB * NDD];
-        } else {
-          for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = 0.f;
-          if (lane == 0) S.wtf[warp] = 0.f;
-        }
-      } else {  // FP64 geometry, FP32 tangent integrand
-        point_setup<LAWK, false, true, float>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp,
-                                              ch * PW + warp, lane, S.R[warp], nullptr, S.Dwf[warp]);
-        for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = (float)S.R[warp][i];
+      if (S.abort) {
+        ok = false;
+        break;
       }
+      ok = tc_element<LAWK, true>(S, LS, m, L, w.ex, w.eyz >> 16, w.eyz & 0xffff, const_d, Uhist, vals,
+                                  taddr, idesc, a_base, b_base, commits);
+      if (!ok) break;
+      tc::fence_before_sync();
       __syncthreads();
-      for (int kg = 0; kg < 2; kg++) {
-        // the previous chunk's MMAs must be done before A/B are overwritten
-        if (commits > 0) {
-          if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
-        }
-        __syncthreads();
-        if (S.abort) goto done;
-        // stage 1 (rows (d,c,e)) and B (rows b); columns kk = kq*8 + pt.
-        // Loop order: 4 points at a time (R rows in registers), then the 5
-        // derivative slots of this group; float4 stores of 4 points.
-        if (tid < 243 && const_d) {
-          // A = w_q * sum_l D[(d,k),(e,l)] R_q[c,l] with the constant D row
-          // loaded once for the 4 points of a half
-          const int d = tid / 81, c = (tid % 81) / 3, e = tid % 3;
-          const int r = tid, mt = r >> 7;
-          for (int half = 0; half < 2; half++) {
-            float rc[4][NDD], wq[4];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              wq[j] = S.wtf[half * 4 + j];
-#pragma unroll
-              for (int l = 0; l < NDD; l++) rc[j][l] = S.Rf[half * 4 + j][NDD * c + l];
-            }
-            for (int kq = 0; kq < 5; kq++) {
-              const int k = kg * 5 + kq;
-              float dr[NDD];
-#pragma unroll
-              for (int l = 0; l < NDD; l++) dr[l] = S.Dc[30 * (10 * d + k) + 10 * e + l];
-              float4 hi, lo;
-              float *ph = &hi.x, *pl = &lo.x;
-#pragma unroll
-              for (int j = 0; j < 4; j++) {
-                float sacc = 0.f;
-#pragma unroll
-                for (int l = 0; l < NDD; l++) sacc = fmaf(dr[l], rc[j][l], sacc);
-                sacc *= wq[j];
-                const float h = tc::to_tf32(sacc);
-                ph[j] = h;
-                pl[j] = tc::to_tf32(sacc - h);
-              }
-              const uint32_t off = (uint32_t)((kq * 2 + mt) * A_TILE) + kmajor_off(r & 127, half * 4);
-              *reinterpret_cast<float4 *>(S.A + off) = hi;
-              *reinterpret_cast<float4 *>(S.A + A_PIECE + off) = lo;
-            }
-          }
-        } else if (tid < 243) {
-          const int d = tid / 81, c = (tid % 81) / 3, e = tid % 3;
-          const int r = tid, mt = r >> 7;
-          for (int half = 0; half < 2; half++) {
-            float rc[4][NDD];
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-#pragma unroll
-              for (int l = 0; l < NDD; l++) rc[j][l] = S.Rf[half * 4 + j][NDD * c + l];
-            for (int kq = 0; kq < 5; kq++) {
-              const int k = kg * 5 + kq;
-              float4 hi, lo;
-              float *ph = &hi.x, *pl = &lo.x;
-#pragma unroll
-              for (int j = 0; j < 4; j++) {
-                const float *drow = S.Dwf[half * 4 + j] + 30 * (10 * d + k) + 10 * e;
-                float sacc = 0.f;
-#pragma unroll
-                for (int l = 0; l < NDD; l++) sacc = fmaf(drow[l], rc[j][l], sacc);
-                const float h = tc::to_tf32(sacc);
-                ph[j] = h;
-                pl[j] = tc::to_tf32(sacc - h);
-              }
-              const uint32_t off = (uint32_t)((kq * 2 + mt) * A_TILE) + kmajor_off(r & 127, half * 4);
-              *reinterpret_cast<float4 *>(S.A + off) = hi;
-              *reinterpret_cast<float4 *>(S.A + A_PIECE + off) = lo;
-            }
-          }
-        }
-        if (tid < NB) {
-          const int b = tid;
-          for (int kq = 0; kq < 5; kq++) {
-            const int k = kg * 5 + kq;
-            for (int half = 0; half < 2; half++) {
-              float4 hi, lo;
-              float *ph = &hi.x, *pl = &lo.x;
-              for (int j = 0; j < 4; j++) {
-                const float s = S.Rf[half * 4 + j][NDD * b + k];
-                const float h = tc::to_tf32(s);
-                ph[j] = h;
-                pl[j] = tc::to_tf32(s - h);
-              }
-              const uint32_t off = (uint32_t)(kq * B_TILE) + kmajor_off(b, half * 4);
-              *reinterpret_cast<float4 *>(S.B + off) = hi;
-              *reinterpret_cast<float4 *>(S.B + B_PIECE + off) = lo;
-            }
-          }
-        }
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {
-          tc::fence_after_sync();
-          for (int kt = 0; kt < NKT; kt++)
-            for (int mt = 0; mt < 2; mt++)
-              for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
-                const int pa = (pp == 2) ? 1 : 0, pb = (pp == 1) ? 1 : 0;
-                const uint64_t ad = tc::smem_desc(a_base + pa * A_PIECE + (kt * 2 + mt) * A_TILE, 128, 256);
-                const uint64_t bd = tc::smem_desc(b_base + pb * B_PIECE + kt * B_TILE, 128, 256);
-                const uint32_t acc = (first && kt == 0 && pp == 0) ? 0u : 1u;
-                tc::mma_tf32(taddr + (uint32_t)(mt * 32), ad, bd, idesc, acc);
-              }
-          tc::mma_commit(&S.mbar);
-        }
-        commits++;
-        first = false;
-      }
-      __syncthreads();  // Rf / Dwf of this chunk are no longer read after the next wait
+      if (tid == 0)  // release at GPU scope after the barrier (see release_add)
+        asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.s32 [%0], 1;" ::"l"(ba.done + w.inst) : "memory");
     }
-    // epilogue: wait for the element's last MMAs, read TMEM, scatter
-    if (!tc::mbar_wait(&S.mbar, (commits - 1) & 1, WAIT_LIMIT)) S.abort = 1;
-    tc::fence_after_sync();
-    __syncthreads();
-    if (S.abort) goto done;
-    {
-      // warp w reads tile (w / 4), TMEM lane quarter (w % 4)
-      const int mt = warp >> 2, quarter = warp & 3;
-      uint32_t v[32];
-      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mt * 32), v);
-      const int r = mt * 128 + quarter * 32 + lane;
-      if (r < 243) {
-        const int d = r / 81, c = (r % 81) / 3, e = r % 3;
-        const int sx = ex + c / 9, sy = ey + (c / 3) % 3, sz = ez + c % 3;
-        for (int bi = 0; bi < 3; bi++) {  // 9 rows b at a time: loads first, then stores
-          int64_t slot[9];
-          double old[9];
-#pragma unroll
-          for (int t = 0; t < 9; t++) {
-            const int b = 9 * bi + t;
-            const int rx = ex + bi, ry = ey + t / 3, rz = ez + t % 3;
-            slot[t] = S.rowp[3 * b + d] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
-          }
-#pragma unroll
-          for (int t = 0; t < 9; t++) old[t] = BATCH ? __ldcg(vals + slot[t]) : vals[slot[t]];
-#pragma unroll
-          for (int t = 0; t < 9; t++) vals[slot[t]] = old[t] + (double)__uint_as_float(v[9 * bi + t]);
-        }
-      }
-    }
-    if (BATCH) __threadfence();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (BATCH && tid == 0) atomicAdd(ba.done + w.inst, 1);
+    if (!ok) break;
   }
-done:
-  tc::fence_before_sync();
-  __syncthreads();
-  if (S.abort && tid == 0) atomicCAS(err, 0, 2);
-  if (warp == 0) tc::tmem_dealloc(taddr, TMEM_COLS);
+  tc_teardown(S, taddr, ba.err);
 }
 
 template <int LAWK>
@@ -404,7 +442,7 @@ static int run_tc(Context *c, double *vals)
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
   const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
-  auto kern = tc_tangent_kernel<LAWK, false>;
+  auto kern = tc_tangent_kernel<LAWK>;
   static bool attr = false;
   if (!attr) {
     IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -427,8 +465,8 @@ static int run_tc(Context *c, double *vals)
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
         const int grid = nel < nsm ? nel : nsm;
-        kern<<<grid, TC_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, BatchArgs{}, c->d_Uhist,
-                                                    vals, c->d_err);
+        kern<<<grid, TC_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, c->d_Uhist, vals,
+                                                    c->d_err);
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
@@ -447,13 +485,13 @@ template <int LAWK>
 static int run_tc_batch(Context *c, const BatchArgs &a, int grid, const double *Uhist, double *vals)
 {
   const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
-  auto kern = tc_tangent_kernel<LAWK, true>;
+  auto kern = tc_batch_kernel<LAWK>;
   static bool attr = false;
   if (!attr) {
     IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  kern<<<grid, TC_THREADS, smem, c->stream>>>(DevMesh{}, DevLaw{}, 0, 0, 0, 0, 0, 0, a, Uhist, vals, a.err);
+  kern<<<grid, TC_THREADS, smem, c->stream>>>(a, Uhist, vals);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;
