@@ -131,10 +131,21 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
   const int pc = tid < NPAIR ? c_pair_c[tid] : 0;
 
   const int nchunk = (m.npts + PW - 1) / PW;
+  // Linear isotropic strain-gradient law: its tangent block of a basis pair
+  // (b,c) is, with per-point Gram sums G1[i][j] = sum_q w dN_b/dx_i dN_c/dx_j
+  // and G2[d][e] = sum_q w sum_m d2N_b/dx_d dx_m d2N_c/dx_e dx_m,
+  //   K[(b,d),(c,e)] = lam G1[d][e] + mu (delta_de tr G1 + G1[e][d])
+  //                  + ell^2 (lam G2[d][e] + mu (delta_de tr G2 + G2[e][d])),
+  // the same sum as R^T D R of the assembly loop with this law's constant D
+  // (36 instead of 81 + 27 x 81 x 9 / 378 FMAs per pair and point).
+  constexpr bool ISO = (LAWK == 0) && TAN;
+  double g1[9], g2[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) g1[i] = g2[i] = 0.0;
   for (int ch = 0; ch < nchunk; ch++) {
     if (warp < PW)
       point_setup<LAWK, RES, TAN, double>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp, ch * PW + warp,
-                                          lane, S.R[warp], S.rr[warp], S.Dw[warp]);
+                                          lane, S.R[warp], S.rr[warp], S.Dw[warp], !ISO);
     __syncthreads();
     if (RES && tid < NE) {
       const int bb = tid / 3, d = tid % 3;
@@ -144,20 +155,51 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
         racc += s;
       }
     }
-    if (TAN) {
+    if (ISO) {
+      if (tid < NPAIR) {
+        for (int w = 0; w < PW; w++) {
+          const double *rb = S.R[w] + NDD * pb, *rc = S.R[w] + NDD * pc;
+          const double wt = S.Pt[w].wt;
+          double gb[3], gc[3], hb[3][3], hc[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            gb[i] = wt * rb[1 + i];
+            gc[i] = rc[1 + i];
+          }
+          // Hessian components (xx, xy, xz, yy, yz, zz) -> symmetric 3 x 3
+          hb[0][0] = wt * rb[4]; hb[0][1] = hb[1][0] = wt * rb[5]; hb[0][2] = hb[2][0] = wt * rb[6];
+          hb[1][1] = wt * rb[7]; hb[1][2] = hb[2][1] = wt * rb[8]; hb[2][2] = wt * rb[9];
+          hc[0][0] = rc[4]; hc[0][1] = hc[1][0] = rc[5]; hc[0][2] = hc[2][0] = rc[6];
+          hc[1][1] = rc[7]; hc[1][2] = hc[2][1] = rc[8]; hc[2][2] = rc[9];
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+              g1[3 * i + j] = fma(gb[i], gc[j], g1[3 * i + j]);
+              double t = g2[3 * i + j];
+#pragma unroll
+              for (int mm = 0; mm < 3; mm++) t = fma(hb[i][mm], hc[j][mm], t);
+              g2[3 * i + j] = t;
+            }
+        }
+      }
+      __syncthreads();
+    } else if (TAN) {
       for (int w = 0; w < PW; w++) {
         const double *R = S.R[w];
         const double *Dw = S.Dw[w];
-        // B1: M[(d,k-1),(c,e)] = sum_{l=1..9} Dw[(d,k),(e,l)] R[c,l]
-        for (int t = tid; t < 27 * 81; t += THREADS) {
-          const int row = t / 81, col = t % 81;
-          const int d = row / 9, k = row % 9 + 1, c = col / 3, e = col % 3;
-          const double *drow = Dw + 30 * (10 * d + k) + 10 * e;
-          const double *rc = R + NDD * c;
-          double s = 0.0;
+        {
+          // B1: M[(d,k-1),(c,e)] = sum_{l=1..9} Dw[(d,k),(e,l)] R[c,l]
+          for (int t = tid; t < 27 * 81; t += THREADS) {
+            const int row = t / 81, col = t % 81;
+            const int d = row / 9, k = row % 9 + 1, c = col / 3, e = col % 3;
+            const double *drow = Dw + 30 * (10 * d + k) + 10 * e;
+            const double *rc = R + NDD * c;
+            double s = 0.0;
 #pragma unroll
-          for (int l = 1; l < NDD; l++) s = fma(drow[l], rc[l], s);
-          S.M[t] = s;
+            for (int l = 1; l < NDD; l++) s = fma(drow[l], rc[l], s);
+            S.M[t] = s;
+          }
         }
         __syncthreads();
         // B2: K[(b,d),(c,e)] += sum_k R[b,k] M[(d,k),(c,e)] + value (mass) term
@@ -184,6 +226,22 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
     } else {
       __syncthreads();
     }
+  }
+  if (ISO && tid < NPAIR) {
+    const double lam = L.par[0], mu = L.par[1], l2 = L.par[2] * L.par[2];
+    const double t1 = g1[0] + g1[4] + g1[8], t2 = g2[0] + g2[4] + g2[8];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int e = 0; e < 3; e++) {
+        double k1 = lam * g1[3 * d + e] + mu * g1[3 * e + d];
+        double k2 = lam * g2[3 * d + e] + mu * g2[3 * e + d];
+        if (d == e) {
+          k1 += mu * t1;
+          k2 += mu * t2;
+        }
+        acc[3 * d + e] = k1 + l2 * k2;
+      }
   }
   // scatter (conflict-free within a colour)
   const int nbv[3] = {m.nbasis[0], nb1, nb2};

@@ -25,6 +25,7 @@ struct PointScratch {
   double W[NDD];
   double Xg[3 * NDD];
   double u[90];
+  double wt;  // quadrature weight x |span| x detG of the point
 };
 
 template <int LAWK>
@@ -182,16 +183,19 @@ __device__ inline double point_geometry(const ElemData &E, PointScratch &P, cons
 // Outputs: R[27*10] physical basis, rr[30] weighted residual integrand,
 // D[900] weighted tangent integrand (DT = double, or float for the split mode).
 // With a geometry cache (m.geo) R and the weight are read, not recomputed.
+// fill_D = false (constant-tangent law only): D is not written; the caller
+// contracts with the sparse constant tangent and the weight P.wt.
 template <int LAWK, bool RES, bool TAN, typename DT>
 __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &LS, const DevMesh &m,
                             const DevLaw &L, int ex, int ey, int ez, int w, int q, int lane,
-                            double *R, double *rr, DT *D)
+                            double *R, double *rr, DT *D, bool fill_D = true)
 {
   const double *__restrict__ Dconst = L.Dconst;
   if (q >= m.npts) {  // padding point of an incomplete chunk: no contribution
     for (int i = lane; i < NB * NDD; i += 32) R[i] = 0.0;
     if (RES) for (int i = lane; i < 30; i += 32) rr[i] = 0.0;
-    if (TAN) for (int i = lane; i < 900; i += 32) D[i] = (DT)0;
+    if (TAN && fill_D) for (int i = lane; i < 900; i += 32) D[i] = (DT)0;
+    if (lane == 0) P.wt = 0.0;
     __syncwarp();
     return;
   }
@@ -205,6 +209,7 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
   } else {
     wt = point_geometry(E, P, m, ex, ey, ez, q, lane, R);
   }
+  if (lane == 0) P.wt = wt;
   // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
   const int nh = L.nhist;
   constexpr bool NEED_U = RES || LAWK != 0;
@@ -230,7 +235,7 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
       }
       rr[lane] = wt * s;
     }
-    if (TAN)
+    if (TAN && fill_D)
       for (int i = lane; i < 900; i += 32) D[i] = (DT)(wt * __ldg(Dconst + i));
     __syncwarp();
   } else if constexpr (LAWK == 1) {
