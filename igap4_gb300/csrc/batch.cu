@@ -48,6 +48,7 @@ struct Batch {
   double *d_norms = nullptr;   // [n]
   igapgpu_batch_schedule sched{1, 1, 1, 0};
   int nsm = 0;
+  bool all_geof = false;  // every instance has the FP32 geometry cache
   size_t ctrl_bytes() const { return sizeof(int) * (64 + 2 * (size_t)ninst); }
 };
 
@@ -196,7 +197,9 @@ static int batch_kernels(Context *c, bool do_res, bool do_tan, double *RR, doubl
       IGAP_CUDA(cudaEventCreate(&e1));
       IGAP_CUDA(cudaEventRecord(e0, c->stream));
     }
-    int r = launch_tc_batch(c, batch_args(c, 1, nitems), c->law, b->nsm, c->d_Uhist, vals);
+    int r = (c->law == IGAPGPU_LAW_LINGRAD && b->all_geof && !getenv("IGAPGPU_TC_DENSE"))
+                ? launch_tc_gram_batch(c, batch_args(c, 1, nitems), b->nsm, vals)
+                : launch_tc_batch(c, batch_args(c, 1, nitems), c->law, b->nsm, c->d_Uhist, vals);
     if (r) return r;
     if (c->prof) {
       IGAP_CUDA(cudaEventRecord(e1, c->stream));
@@ -476,6 +479,8 @@ int igapgpu_batch_init(igapgpu_t *out, int ninst, const igapgpu_mesh_desc *meshe
     BCUDA(cudaMemcpy(b->d_nbs, nbs.data(), sizeof(int) * 3 * ninst, cudaMemcpyHostToDevice));
     BCUDA(cudaMemcpy(b->d_off, b->dof_off.data(), sizeof(int64_t) * (ninst + 1), cudaMemcpyHostToDevice));
   }
+  b->all_geof = true;
+  for (Context *s : b->subs) b->all_geof = b->all_geof && s->d_geof != nullptr;
   BTRY(balloc(&b->d_ctrl, b->ctrl_bytes() / sizeof(int)));
   BTRY(build_items(c, b->sched.order));
   BCUDA(cudaStreamSynchronize(c->stream));

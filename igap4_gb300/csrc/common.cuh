@@ -226,6 +226,9 @@ int launch_geometry_cache(Context *c);
 int launch_geometry_cache_f32(Context *c);
 // tc_tangent.cu
 int launch_tc_tangent(Context *c, double *vals);
+// tc_gram.cu (linear isotropic law with the FP32 geometry cache)
+int launch_tc_gram(Context *c, double *vals);
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals);
 // krylov.cu
 int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,

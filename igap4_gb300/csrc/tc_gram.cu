@@ -1,0 +1,410 @@
+// Split-precision tangent of the linear isotropic strain-gradient law on the
+// tensor cores, in Gram form.
+//
+// For this law the tangent block of basis functions b, c is
+//   K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu sum_i G[(b,i),(c,i)]
+// with the Gram matrix (rows (b,i), columns (c,j), i,j = 0..2)
+//   G[(b,i),(c,j)] = sum_q w_q ( dN_b/dx_i dN_c/dx_j + ell^2 sum_m d2N_b/dx_i dx_m d2N_c/dx_j dx_m ),
+// the same sum as the assembly loop's R^T D R (src/assmcore_iga.c:722-750)
+// with this law's constant D.  Per element that is one GEMM
+//   G = A . B^T,  A[(b,i), k] = w_q [dN_b/dx_i | ell^2 d2N_b/dx_i dx_m],
+//                 B[(c,j), k] = [dN_c/dx_j | d2N_c/dx_j dx_m],
+// M = 81 rows (one 128-row tile), N = 81 columns (96), K = 64 points x (1 + 3)
+// = 256, processed in chunks of 8 points (K = 32 = 4 tf32 K-steps).  A and B
+// come straight from the FP32 geometry cache: each chunk's 8 point rows
+// (8 x 1088 contiguous bytes) are fetched by a bulk asynchronous copy one
+// chunk ahead, the operands are split into TF32 hi + lo, and hi.hi + hi.lo +
+// lo.hi accumulate in FP32 in tensor memory (tcgen05.mma kind::tf32).  The
+// operand buffers are double buffered: chunk n+1 is built while the MMAs of
+// chunk n run.  The epilogue stages G in shared memory, forms K and adds it
+// into the FP64 CSR values.  Every mbarrier wait is bounded.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "element.cuh"
+#include "tcgen05.cuh"
+
+namespace igap {
+
+namespace {
+constexpr int G_THREADS = 256;
+constexpr int GROWS = 81;                    // (b,i) rows / (c,j) columns
+constexpr int GN = 96;                       // MMA N (>= 81, multiple of 16)
+constexpr int GKS = 4;                       // K-steps per chunk (K = 32)
+constexpr int GA_TILE = 128 * 8 * 4;         // one K-step of A: 4096 B
+constexpr int GB_TILE = GN * 8 * 4;          // one K-step of B: 3072 B
+constexpr int GA_PIECE = GKS * GA_TILE;      // 16384 B (hi or lo)
+constexpr int GB_PIECE = GKS * GB_TILE;      // 12288 B
+constexpr int PT_FLOATS = GEO_STRIDE;        // 272 floats per cached point
+constexpr uint32_t G_WAIT_LIMIT = 1u << 26;
+constexpr uint32_t G_TMEM_COLS = 128;
+constexpr int GPAD = 84;                     // row stride of the staged Gram matrix
+
+__device__ __forceinline__ int hess_slot(int i, int m)
+{
+  const int a = i < m ? i : m, b = i < m ? m : i;
+  return a == 0 ? b : (a == 1 ? 2 + b : 5);  // (0,0)0 (0,1)1 (0,2)2 (1,1)3 (1,2)4 (2,2)5
+}
+
+__device__ __forceinline__ bool tc_wait_ge(const int *p, int target)
+{
+  for (uint32_t i = 0; i < (1u << 24); i++) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v >= target) return true;
+    __nanosleep(128);
+  }
+  return false;
+}
+}  // namespace
+
+struct TcgSmem {
+  unsigned char A[2][2 * GA_PIECE];  // [buffer][hi, lo][K-step][4096 B]
+  unsigned char B[2][2 * GB_PIECE];  // [buffer][hi, lo][K-step][3072 B]
+  float Rf[2][PW * PT_FLOATS];       // [buffer] 8 cached point rows
+  float G[GROWS * GPAD];             // staged Gram matrix
+  int64_t rowp[NE];
+  uint64_t mbar_mma[2];
+  uint64_t mbar_cp[2];
+  uint32_t taddr;
+  int abort;
+  int64_t base;
+};
+
+// Barrier phase bookkeeping of one CTA (uniform across its threads).
+struct TcgState {
+  uint32_t mma_n[2];  // commits issued to mbar_mma[b]
+  uint32_t cp_n[2];   // copies issued to mbar_cp[b]
+};
+
+__device__ __forceinline__ void tcg_issue_copy(TcgSmem &S, TcgState &st, const float *gsrc, int npts, int ch)
+{
+  const int rb = ch & 1;
+  const int q0 = ch * PW;
+  const int nv = npts - q0 < PW ? npts - q0 : PW;
+  if (threadIdx.x == 0) {
+    tc::fence_proxy_async();
+    tc::mbar_arrive_expect_tx(&S.mbar_cp[rb], (uint32_t)(nv * PT_FLOATS * 4));
+    tc::bulk_g2s(S.Rf[rb], gsrc + (size_t)q0 * PT_FLOATS, (uint32_t)(nv * PT_FLOATS * 4), &S.mbar_cp[rb]);
+  }
+  st.cp_n[rb]++;
+}
+
+// One element.  Returns false when a bounded wait expired (S.abort set).
+template <bool COH>
+__device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevMesh &m, const DevLaw &L, int ex,
+                                            int ey, int ez, double *__restrict__ vals, uint32_t taddr,
+                                            uint32_t a_base, uint32_t b_base)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  const int nbv[3] = {m.nbasis[0], nb1, nb2};
+  const int npts = m.npts;
+  const int nchunk = (npts + PW - 1) / PW;
+  const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+  const float *gsrc = m.geof + eg * npts * PT_FLOATS;
+  const float l2 = (float)(L.par[2] * L.par[2]);
+  const uint32_t idesc = tc::instr_desc(2, 128, GN);
+  tcg_issue_copy(S, st, gsrc, npts, 0);
+  if (tid < NE) {
+    const int b = tid / 3, dd = tid % 3;
+    const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    S.rowp[tid] = __ldg(m.rowptr + 3 * cpb + dd);
+  }
+  for (int ch = 0; ch < nchunk; ch++) {
+    const int rb = ch & 1, ob = ch & 1;
+    if (ch + 1 < nchunk) tcg_issue_copy(S, st, gsrc, npts, ch + 1);  // its buffer was last read by chunk ch-1
+    bool ok = tc::mbar_wait(&S.mbar_cp[rb], (st.cp_n[rb] - 1) & 1, G_WAIT_LIMIT);
+    if (ok && st.mma_n[ob] > 0) ok = tc::mbar_wait(&S.mbar_mma[ob], (st.mma_n[ob] - 1) & 1, G_WAIT_LIMIT);
+    if (!ok) S.abort = 1;
+    __syncthreads();
+    if (S.abort) return false;
+    // operands of this chunk: task = (matrix, row, K-step, half) -> 4 consecutive k
+    const float *R = S.Rf[rb];
+    const int q0 = ch * PW;
+    for (int t = tid; t < 2 * GROWS * GKS * 2; t += G_THREADS) {
+      const int mat = t / (GROWS * GKS * 2);  // 0: A, 1: B
+      const int u = t % (GROWS * GKS * 2);
+      const int r = u % GROWS, ks = (u / GROWS) % GKS, half = u / (GROWS * GKS);
+      const int bsf = r / 3, i = r % 3;
+      float4 hi, lo;
+      float *ph = &hi.x, *pl = &lo.x;
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) {
+        const int k = ks * 8 + half * 4 + jj;
+        int p, idx;
+        float scale;
+        if (k < PW) {  // gradient part: one slot per point
+          p = k;
+          idx = 1 + i;
+          scale = 1.f;
+        } else {       // Hessian part: three slots per point
+          p = (k - PW) / 3;
+          idx = 4 + hess_slot(i, (k - PW) % 3);
+          scale = l2;
+        }
+        const float *row = R + p * PT_FLOATS;
+        float v = 0.f;
+        if (q0 + p < npts) {
+          v = row[NDD * bsf + idx];
+          if (mat == 0) v *= scale * row[NB * NDD];  // A carries w_q (and ell^2)
+        }
+        const float h = tc::to_tf32(v);
+        ph[jj] = h;
+        pl[jj] = tc::to_tf32(v - h);
+      }
+      unsigned char *base = mat == 0 ? S.A[ob] : S.B[ob];
+      const int piece = mat == 0 ? GA_PIECE : GB_PIECE;
+      const uint32_t off = (uint32_t)(ks * (mat == 0 ? GA_TILE : GB_TILE)) + tc::kmajor_off(r, half * 4);
+      *reinterpret_cast<float4 *>(base + off) = hi;
+      *reinterpret_cast<float4 *>(base + piece + off) = lo;
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t ab = a_base + (uint32_t)(ob * 2 * GA_PIECE), bb = b_base + (uint32_t)(ob * 2 * GB_PIECE);
+      for (int ks = 0; ks < GKS; ks++)
+        for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
+          const int pa = (pp == 2) ? 1 : 0, pb = (pp == 1) ? 1 : 0;
+          const uint64_t ad = tc::smem_desc(ab + (uint32_t)(pa * GA_PIECE + ks * GA_TILE), 128, 256);
+          const uint64_t bd = tc::smem_desc(bb + (uint32_t)(pb * GB_PIECE + ks * GB_TILE), 128, 256);
+          tc::mma_tf32(taddr, ad, bd, idesc, (ch == 0 && ks == 0 && pp == 0) ? 0u : 1u);
+        }
+      tc::mma_commit(&S.mbar_mma[ob]);
+    }
+    st.mma_n[ob]++;
+  }
+  // epilogue: the last commit covers every MMA of the element
+  {
+    const int lb = (nchunk - 1) & 1;
+    if (!tc::mbar_wait(&S.mbar_mma[lb], (st.mma_n[lb] - 1) & 1, G_WAIT_LIMIT)) S.abort = 1;
+  }
+  tc::fence_after_sync();
+  __syncthreads();
+  if (S.abort) return false;
+  {
+    // warp w reads TMEM lane quarter (w % 4), columns [32 (w / 4), +32) and, for
+    // w < 4, also [64, 96)
+    const int quarter = warp & 3;
+    const int r = quarter * 32 + lane;
+    for (int cb = warp >> 2; cb < 3; cb += 2) {
+      uint32_t v[32];
+      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cb * 32), v);
+      if (r < GROWS)
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (cb * 32 + j < GROWS) S.G[r * GPAD + cb * 32 + j] = __uint_as_float(v[j]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  // K[(b,d),(c,e)] for every (b,d), (c,e): 6561 slots, each written once
+  {
+    const float lam = (float)L.par[0], mu = (float)L.par[1];
+    for (int t0 = tid; t0 < NE * NE; t0 += 9 * G_THREADS) {
+      int64_t slot[9];
+      float kv[9];
+      int cnt = 0;
+#pragma unroll
+      for (int s = 0; s < 9; s++) {
+        const int t = t0 + s * G_THREADS;
+        slot[s] = -1;
+        kv[s] = 0.f;
+        if (t < NE * NE) {
+          const int rr = t / NE, cc = t % NE;
+          const int b = rr / 3, d = rr % 3, c = cc / 3, e = cc % 3;
+          float kk = lam * S.G[(3 * b + d) * GPAD + 3 * c + e] + mu * S.G[(3 * b + e) * GPAD + 3 * c + d];
+          if (d == e)
+            kk += mu * (S.G[(3 * b) * GPAD + 3 * c] + S.G[(3 * b + 1) * GPAD + 3 * c + 1] +
+                        S.G[(3 * b + 2) * GPAD + 3 * c + 2]);
+          const int rx = ex + b / 9, ry = ey + (b / 3) % 3, rz = ez + b % 3;
+          const int sx = ex + c / 9, sy = ey + (c / 3) % 3, sz = ez + c % 3;
+          slot[s] = S.rowp[rr] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
+          kv[s] = kk;
+          cnt = s + 1;
+        }
+      }
+      double old[9];
+#pragma unroll
+      for (int s = 0; s < 9; s++)
+        if (s < cnt) old[s] = COH ? __ldcg(vals + slot[s]) : vals[slot[s]];
+#pragma unroll
+      for (int s = 0; s < 9; s++)
+        if (s < cnt) vals[slot[s]] = old[s] + (double)kv[s];
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tcg_setup(TcgSmem &S)
+{
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, G_TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; b++) {
+      tc::mbar_init(&S.mbar_mma[b], 1);
+      tc::mbar_init(&S.mbar_cp[b], 1);
+    }
+    S.abort = 0;
+  }
+  // padding rows 81..127 of A and 81..95 of B stay zero for the whole kernel
+  for (int i = tid; i < (int)(sizeof(S.A) / 4); i += G_THREADS) reinterpret_cast<float *>(S.A)[i] = 0.f;
+  for (int i = tid; i < (int)(sizeof(S.B) / 4); i += G_THREADS) reinterpret_cast<float *>(S.B)[i] = 0.f;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+}
+
+// Teardown: on an abort, wait (bounded) for copies still in flight before the
+// CTA's shared memory is released; then free TMEM.
+__device__ __forceinline__ void tcg_teardown(TcgSmem &S, const TcgState &st, int *err)
+{
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort) {
+    for (int b = 0; b < 2; b++)
+      if (st.cp_n[b] > 0) tc::mbar_wait(&S.mbar_cp[b], (st.cp_n[b] - 1) & 1, G_WAIT_LIMIT);
+    if (threadIdx.x == 0) atomicCAS(err, 0, 2);
+  }
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(S.taddr, G_TMEM_COLS);
+}
+
+__global__ void __launch_bounds__(G_THREADS, 1)
+    tcg_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
+               int *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcgSmem &S = *reinterpret_cast<TcgSmem *>(smem_raw);
+  tcg_setup(S);
+  const uint32_t taddr = S.taddr, a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
+  TcgState st = {{0, 0}, {0, 0}};
+  const int nelem_c = ncx * ncy * ncz;
+  for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    if (!tcg_element<false>(S, st, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, vals, taddr, a_base, b_base))
+      break;
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  tcg_teardown(S, st, err);
+}
+
+// Batched: elements from the colour-major queue (see element_batch_kernel).
+__global__ void __launch_bounds__(G_THREADS, 1) tcg_batch_kernel(BatchArgs ba, double *__restrict__ vals)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcgSmem &S = *reinterpret_cast<TcgSmem *>(smem_raw);
+  const int tid = threadIdx.x;
+  tcg_setup(S);
+  const uint32_t taddr = S.taddr, a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
+  TcgState st = {{0, 0}, {0, 0}};
+  int cur = -1;
+  DevMesh m;
+  DevLaw L;
+  int64_t next = 0;
+  if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+  for (;;) {
+    if (tid == 0) S.base = next;
+    __syncthreads();
+    const int64_t base = S.base;
+    __syncthreads();
+    if (base >= ba.nitems || S.abort) break;
+    if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+    const int64_t end = base + ba.grab < ba.nitems ? base + ba.grab : ba.nitems;
+    bool ok = true;
+    for (int64_t it = base; it < end; it++) {
+      const BatchItem w = ba.items[it];
+      if (w.inst != cur) {
+        m = ba.meshes[w.inst];
+        L = ba.laws[w.inst];
+        cur = w.inst;
+      }
+      if (tid == 0 && w.col > 0) {
+        if (!tc_wait_ge(ba.done + w.inst, ba.need[27 * w.inst + w.col])) {
+          S.abort = 1;
+          atomicExch(ba.err, 3);
+        }
+      }
+      __syncthreads();
+      if (S.abort) {
+        ok = false;
+        break;
+      }
+      ok = tcg_element<true>(S, st, m, L, w.ex, w.eyz >> 16, w.eyz & 0xffff, vals, taddr, a_base, b_base);
+      if (!ok) break;
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0)  // release at GPU scope after the barrier
+        asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.s32 [%0], 1;" ::"l"(ba.done + w.inst)
+                     : "memory");
+    }
+    if (!ok) break;
+  }
+  tcg_teardown(S, st, ba.err);
+}
+
+// ------------------------------------------------------------- launches
+static size_t tcg_smem() { return sizeof(TcgSmem) + 1024; }
+
+int launch_tc_gram(Context *c, double *vals)
+{
+  const DevMesh m = c->devmesh();
+  const DevLaw L = c->devlaw();
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg_smem()));
+    attr = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  for (int cx = 0; cx < 3; cx++)
+    for (int cy = 0; cy < 3; cy++)
+      for (int cz = 0; cz < 3; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        const int nel = ncx * ncy * ncz;
+        if (nel <= 0) continue;
+        const int grid = nel < nsm ? nel : nsm;
+        tcg_kernel<<<grid, G_THREADS, tcg_smem(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
+        count_launch();
+        IGAP_CHECK_LAUNCH();
+        if (c->prof) {
+          c->prof_launches[1]++;
+          c->prof_elements[1] += nel;
+        }
+      }
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[1].emplace_back(e0, e1);
+  }
+  return IGAPGPU_OK;
+}
+
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals)
+{
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(tcg_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tcg_smem()));
+    attr = true;
+  }
+  tcg_batch_kernel<<<grid, G_THREADS, tcg_smem(), c->stream>>>(a, vals);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+}  // namespace igap

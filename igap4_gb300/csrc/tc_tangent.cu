@@ -16,6 +16,7 @@
 // One persistent CTA per SM walks the elements of one colour, so the CSR
 // scatter is conflict-free as in the FP64 kernel.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 #include "element.cuh"
@@ -46,12 +47,7 @@ __device__ __forceinline__ bool tc_wait_count_ge(const int *p, int target)
   return false;
 }
 
-// byte offset of (row r, k index kk8 in [0,8)) inside one 128-row (or 32-row)
-// block of a K-step: K-major, no swizzle, LBO = 128 B, SBO = 256 B
-__device__ __forceinline__ uint32_t kmajor_off(int r, int kk8)
-{
-  return (uint32_t)((r >> 3) * 256 + (kk8 >> 2) * 128 + (r & 7) * 16 + (kk8 & 3) * 4);
-}
+using tc::kmajor_off;
 }  // namespace
 
 struct TcSmem {
@@ -508,6 +504,7 @@ int launch_tc_batch(Context *c, const BatchArgs &a, int law, int grid, const dou
 
 int launch_tc_tangent(Context *c, double *vals)
 {
+  if (c->law == IGAPGPU_LAW_LINGRAD && c->d_geof && !getenv("IGAPGPU_TC_DENSE")) return launch_tc_gram(c, vals);
   if (c->law == IGAPGPU_LAW_LINGRAD) return run_tc<0>(c, vals);
   if (c->law == IGAPGPU_LAW_GRADELAST) return run_tc<1>(c, vals);
   if (c->law == IGAPGPU_LAW_GRADELASTTIME) return run_tc<2>(c, vals);

@@ -131,6 +131,33 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
   return false;
 }
 
+// Arrive once on the mbarrier and add `bytes` to the transaction count its
+// current phase waits for (the bulk copies below complete that count).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// Bulk asynchronous copy global -> shared memory of this CTA, completing
+// `bytes` transactions on the mbarrier.  dst and src 16-byte aligned, bytes a
+// multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+               : "memory");
+}
+
+// Byte offset of (row r, k index kk8 in [0,8)) inside one K-step block of a
+// K-major, no-swizzle operand: core matrices of 8 rows x 16 B, LBO = 128 B
+// (next 4 K values), SBO = 256 B (next 8 rows).
+__device__ __forceinline__ uint32_t kmajor_off(int r, int kk8)
+{
+  return (uint32_t)((r >> 3) * 256 + (kk8 >> 2) * 128 + (r & 7) * 16 + (kk8 & 3) * 4);
+}
+
 // Round an FP32 value to TF32 (round to nearest, ties away), as an FP32.
 __device__ __forceinline__ float to_tf32(float x)
 {

@@ -3,7 +3,8 @@
 * the tcgen05 self-test GEMM reproduces an exact integer product;
 * the split tangent agrees with the FP64 tangent within the stated bound
   (relative 2-norm error <= 1e-5, measured ~4e-6; TF32 hi+lo operands keep ~21 bits, the
-  FP32 tensor-memory accumulation over 640 terms dominates), for all three laws;
+  FP32 tensor-memory accumulation dominates), for all three laws and both GEMM forms
+  of the linear law (Gram form, and the two-stage form used by the other laws);
 * the residual of the split mode is the FP64 residual, unchanged.
 """
 import numpy as np
@@ -26,12 +27,16 @@ def test_tcgen05_selftest_exact():
     assert np.array_equal(D, E), f"max |D-E| = {np.abs(D - E).max()}"
 
 
-@pytest.mark.parametrize("law,nelem,perturb", [
-    (po.LAW_LINGRAD, (8, 4, 3), False),
-    (po.LAW_GRADELAST, (4, 4, 4), True),
-    (po.LAW_GRADELASTTIME, (3, 3, 4), False),
+@pytest.mark.parametrize("law,nelem,perturb,dense", [
+    (po.LAW_LINGRAD, (8, 4, 3), False, False),   # Gram-form GEMM (tc_gram.cu)
+    (po.LAW_LINGRAD, (5, 3, 4), True, False),
+    (po.LAW_LINGRAD, (8, 4, 3), False, True),    # two-stage GEMM (tc_tangent.cu)
+    (po.LAW_GRADELAST, (4, 4, 4), True, False),
+    (po.LAW_GRADELASTTIME, (3, 3, 4), False, False),
 ])
-def test_split_tangent_vs_fp64(law, nelem, perturb):
+def test_split_tangent_vs_fp64(law, nelem, perturb, dense, monkeypatch):
+    if dense:
+        monkeypatch.setenv("IGAPGPU_TC_DENSE", "1")
     bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     prob = po.Problem(nelem=nelem, law=law, perturb=perturb, bc_type=bct, neumann=neu)
     U = po.random_state(prob, 77)
@@ -53,6 +58,21 @@ def test_split_tangent_vs_fp64(law, nelem, perturb):
     A.assemble(None, RR, V)
     np.testing.assert_array_equal(RR, R64)
     assert rel(V, K64) <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("nquad", [3, 4])
+def test_split_gram_partial_chunks(nquad):
+    """Gram-form split tangent with 27 points per element (chunks of 8, 8, 8, 3)
+    and with 64, against the FP64 tangent of the same quadrature."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    knots, w, X = ig.beam_mesh((6, 3, 2), (4.0, 1.0, 1.0), 2, True)
+    A = ig.Assembly((6, 3, 2), knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct,
+                    neumann=neu, nquad=nquad)
+    U = np.random.default_rng(5).uniform(-1e-2, 1e-2, A.ndof)
+    K64 = A.tangent(U.copy())
+    A.set_precision(ig.PREC_SPLIT)
+    Ks = A.tangent(U.copy())
+    assert rel(Ks, K64) <= SPLIT_TOL
 
 
 def test_split_newton_converges_to_fp64_tolerance():
