@@ -107,11 +107,40 @@ struct ElemSmem {
   double M[27 * 81];
 };
 
+// Residual-only elements: no tangent integrand or stage buffers, 256 threads,
+// so that two CTAs share an SM.
+struct ResSmem {
+  ElemData E;
+  PointScratch Pt[PW];
+  double R[PW][NB * NDD];
+  double rr[PW][30];
+};
+
+template <bool TAN>
+struct ElemCfg {  // tangent (and residual): 384 threads, one CTA per SM
+  static constexpr int NT = THREADS;
+  static constexpr int MINB = 1;
+  using Smem = ElemSmem;
+};
+template <>
+struct ElemCfg<false> {
+  static constexpr int NT = 256;
+  static constexpr int MINB = 2;
+  using Smem = ResSmem;
+};
+
+template <bool TAN>
+__device__ __forceinline__ double *dw_ptr(typename ElemCfg<TAN>::Smem &S, int w)
+{
+  if constexpr (TAN) return S.Dw[w];
+  else return nullptr;
+}
+
 // One element: load, quadrature (phase A, B1, B2) and the scatter into RR /
 // vals.  COH: the read-modify-write of RR / vals bypasses L1 (a batched
 // launch orders colours inside one kernel, through L2).
 template <int LAWK, bool RES, bool TAN, bool COH>
-__device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, const DevMesh &m,
+__device__ __forceinline__ void element_body(typename ElemCfg<TAN>::Smem &S, LawSmem<LAWK> &LS, const DevMesh &m,
                                              const DevLaw &L, int ex, int ey, int ez,
                                              const double *__restrict__ Uhist, double *__restrict__ RR,
                                              double *__restrict__ vals)
@@ -120,7 +149,8 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
   const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
   const int nh = L.nhist;
   // element data: weights, control points, state of every history level
-  load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, THREADS);
+  constexpr int NT = ElemCfg<TAN>::NT;
+  load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, NT);
   __syncthreads();
 
   double acc[9];
@@ -145,7 +175,7 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
   for (int ch = 0; ch < nchunk; ch++) {
     if (warp < PW)
       point_setup<LAWK, RES, TAN, double>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp, ch * PW + warp,
-                                          lane, S.R[warp], S.rr[warp], S.Dw[warp], !ISO);
+                                          lane, S.R[warp], S.rr[warp], dw_ptr<TAN>(S, warp), !ISO);
     __syncthreads();
     if (RES && tid < NE) {
       const int bb = tid / 3, d = tid % 3;
@@ -155,7 +185,7 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
         racc += s;
       }
     }
-    if (ISO) {
+    if constexpr (ISO) {
       if (tid < NPAIR) {
         for (int w = 0; w < PW; w++) {
           const double *rb = S.R[w] + NDD * pb, *rc = S.R[w] + NDD * pc;
@@ -184,13 +214,13 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
         }
       }
       __syncthreads();
-    } else if (TAN) {
+    } else if constexpr (TAN) {
       for (int w = 0; w < PW; w++) {
         const double *R = S.R[w];
         const double *Dw = S.Dw[w];
         {
           // B1: M[(d,k-1),(c,e)] = sum_{l=1..9} Dw[(d,k),(e,l)] R[c,l]
-          for (int t = tid; t < 27 * 81; t += THREADS) {
+          for (int t = tid; t < 27 * 81; t += NT) {
             const int row = t / 81, col = t % 81;
             const int d = row / 9, k = row % 9 + 1, c = col / 3, e = col % 3;
             const double *drow = Dw + 30 * (10 * d + k) + 10 * e;
@@ -274,14 +304,15 @@ __device__ __forceinline__ void element_body(ElemSmem &S, LawSmem<LAWK> &LS, con
 }
 
 template <int LAWK, bool RES, bool TAN>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(ElemCfg<TAN>::NT, ElemCfg<TAN>::MINB)
     element_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncy, int ncz,
                    const double *__restrict__ Uhist, double *__restrict__ RR,
                    double *__restrict__ vals)
 {
+  using Smem = typename ElemCfg<TAN>::Smem;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
-  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
+  Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(Smem));
   // element of this colour
   const int b = blockIdx.x;
   const int iz = b % ncz, iy = (b / ncz) % ncy, ix = b / (ncz * ncy);
@@ -317,13 +348,14 @@ __device__ __forceinline__ bool wait_count_ge(const int *p, int target)
 // row therefore receives its element contributions in colour order, exactly
 // as with one launch per colour.
 template <int LAWK, bool RES, bool TAN>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(ElemCfg<TAN>::NT, ElemCfg<TAN>::MINB)
     element_batch_kernel(BatchArgs a, const double *__restrict__ Uhist, double *__restrict__ RR,
                          double *__restrict__ vals)
 {
+  using Smem = typename ElemCfg<TAN>::Smem;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ElemSmem &S = *reinterpret_cast<ElemSmem *>(smem_raw);
-  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(ElemSmem));
+  Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(Smem));
   __shared__ int64_t s_base;
   __shared__ int s_abort;
   const int tid = threadIdx.x;
@@ -546,7 +578,7 @@ static int run_colours(Context *c, double *RR, double *vals)
 {
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
-  const size_t smem = sizeof(ElemSmem) + sizeof(LawSmem<LAWK>);
+  const size_t smem = sizeof(typename ElemCfg<TAN>::Smem) + sizeof(LawSmem<LAWK>);
   auto kern = element_kernel<LAWK, RES, TAN>;
   static bool attr_set = false;
   if (!attr_set) {
@@ -566,7 +598,7 @@ static int run_colours(Context *c, double *RR, double *vals)
                   ncz = (c->nelem[2] - cz + 2) / 3;
         const int nblk = ncx * ncy * ncz;
         if (nblk <= 0) continue;
-        kern<<<nblk, THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncy, ncz, c->d_Uhist, RR, vals);
+        kern<<<nblk, ElemCfg<TAN>::NT, smem, c->stream>>>(m, L, cx, cy, cz, ncy, ncz, c->d_Uhist, RR, vals);
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
@@ -598,14 +630,14 @@ static int init_pairs()
 template <int LAWK, bool RES, bool TAN>
 static int run_batch(Context *c, const BatchArgs &a, int grid, const double *Uhist, double *RR, double *vals)
 {
-  const size_t smem = sizeof(ElemSmem) + sizeof(LawSmem<LAWK>);
+  const size_t smem = sizeof(typename ElemCfg<TAN>::Smem) + sizeof(LawSmem<LAWK>);
   auto kern = element_batch_kernel<LAWK, RES, TAN>;
   static bool attr_set = false;
   if (!attr_set) {
     IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  kern<<<grid, THREADS, smem, c->stream>>>(a, Uhist, RR, vals);
+  kern<<<grid, ElemCfg<TAN>::NT, smem, c->stream>>>(a, Uhist, RR, vals);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;
@@ -614,10 +646,10 @@ static int run_batch(Context *c, const BatchArgs &a, int grid, const double *Uhi
 template <int LAWK, bool RES, bool TAN>
 static int batch_occ(int *nb)
 {
-  const size_t smem = sizeof(ElemSmem) + sizeof(LawSmem<LAWK>);
+  const size_t smem = sizeof(typename ElemCfg<TAN>::Smem) + sizeof(LawSmem<LAWK>);
   auto kern = element_batch_kernel<LAWK, RES, TAN>;
   IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  IGAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, kern, THREADS, smem));
+  IGAP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, kern, ElemCfg<TAN>::NT, smem));
   return IGAPGPU_OK;
 }
 
