@@ -1,0 +1,67 @@
+"""Run one assembly configuration on the GPU a fixed number of times (for
+profilers and quick timings).
+
+    python -m igap4_gb300.run_case --nelem 64,16,16 --prec fp64 --what assemble --reps 2
+
+--what: assemble (residual + tangent), residual, tangent, spmv (after one
+assembly), batch (seeded uneven instances, --ninst of them).  Prints the
+wall time of each repetition after the first.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nelem", default="64,16,16")
+    ap.add_argument("--prec", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--what", default="assemble", choices=["assemble", "residual", "tangent", "spmv", "batch"])
+    ap.add_argument("--law", default="lingrad", choices=["lingrad", "gradelast", "gradelasttime"])
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--ninst", type=int, default=32)
+    a = ap.parse_args()
+    import torch
+
+    import igap4_gb300 as ig
+
+    law = {"lingrad": ig.LAW_LINGRAD, "gradelast": ig.LAW_GRADELAST, "gradelasttime": ig.LAW_GRADELASTTIME}[a.law]
+    if a.what == "batch":
+        insts = ig.batch_instances(a.ninst, seed=1, nx=(8, 32), nyz=(2, 8))
+        A = ig.BatchAssembly(insts, law=ig.LAW_LINGRAD)
+    else:
+        nelem = tuple(int(v) for v in a.nelem.split(","))
+        bct, neu = ig.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+        knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0))
+        par = (1.0, 1.0, 0.1) if law == ig.LAW_LINGRAD else None
+        A = ig.Assembly(nelem, knots, w, X, law=law, par=par, bc_type=bct, neumann=neu)
+    A.set_precision(ig.PREC_SPLIT if a.prec == "split" else ig.PREC_FP64)
+    dev = torch.device("cuda")
+    U = torch.tensor(np.random.default_rng(1).uniform(-1e-2, 1e-2, A.ndof), device=dev)
+    RR = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+    x = torch.tensor(np.random.default_rng(2).standard_normal(A.ndof), device=dev)
+    y = torch.zeros_like(x)
+    if a.what == "spmv":
+        A.assemble(U, RR, None)
+    for k in range(a.reps):
+        A.synchronize()
+        t0 = time.perf_counter()
+        if a.what in ("assemble", "batch"):
+            A.assemble(U, RR, None)
+        elif a.what == "residual":
+            A.residual(U, RR)
+        elif a.what == "tangent":
+            A.tangent(U, None)
+        else:
+            A.matmult(x, y)
+        A.synchronize()
+        if k:
+            print(f"rep {k}: {1e3 * (time.perf_counter() - t0):.3f} ms")
+    print(f"elements {A.nelem_total} ndof {A.ndof} nnz {A.nnz}")
+
+
+if __name__ == "__main__":
+    main()
