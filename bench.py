@@ -42,6 +42,15 @@ SEED = 20261203
 # algorithmic cost per element (p = 2, 64 points, 81 DOFs)
 TAN_FLOP_PER_ELEM = 2 * 64 * (30 * 27 * 3 * 10 + 81 * 81 * 10)  # 11,508,480
 RES_FLOP_PER_ELEM = 2 * 64 * (27 * 30 + 27 * 30)                 # 207,360
+# FLOPs the kernels execute for the linear law (Gram form of the tangent):
+# FP64 kernel: 378 basis pairs x 64 points x 81 (Gram sums) + 64 x 3,420
+# (state interpolation, law, projection) + block formation and scatter
+EXEC_FLOP_FP64_ELEM = 378 * 64 * 81 + 64 * 3420 + 30_000         # ~2.21 M
+# tensor-core kernel: 3 TF32 products of M128 x N96 x K256 per element
+EXEC_FLOP_TC_ELEM = 3 * 2 * 128 * 96 * 256                         # 18.9 M
+# DRAM traffic per launch of the FP64 element kernel at 128x32x32, from the
+# one-pass ncu launch list (profiles/assembly_launch_list_beam128x32x32.md)
+TRAFFIC_FP64_LAUNCH = 1.5063e9
 
 
 def parse():
@@ -377,14 +386,19 @@ def main():
         res_ms, res_l, res_e = skinds[0]
         tc_flop = TAN_FLOP_PER_ELEM * tc_e / max(tc_l, 1)
         tc_ach = tc_flop / (tc_ms / max(tc_l, 1) * 1e-3) / 1e12
+        tc_exec = tc_ach * EXEC_FLOP_TC_ELEM / TAN_FLOP_PER_ELEM
         bf16_peak = peaks.get("bf16_tflops", 1900.0) if (peaks := _peaks()) else 1900.0
         split = {"value": world * A.nelem_total / (sms * 1e-3), "unit": "elements/s",
                  "ms_per_step": sms, "step_ms": sstep, "gpu_launches": slaunch,
                  "tangent_rel_err_vs_fp64": err, "dtype": "tf32x3/f32-acc tangent, f64 residual",
                  "tc_kernel_ms_per_step": tc_ms / a.steps, "fp64_residual_kernel_ms_per_step": res_ms / a.steps,
-                 "roofline": {"bound": "tensor", "kernel": "tc_tangent_kernel (tcgen05.mma kind::tf32, TF32x3)",
+                 "roofline": {"bound": "tensor", "kernel": "tcg_kernel (tcgen05.mma kind::tf32, TF32x3, Gram form)",
                               "achieved": tc_ach, "peak": bf16_peak, "unit": "TFLOP/s",
                               "frac": tc_ach / bf16_peak,
+                              "executed_flop_per_element": EXEC_FLOP_TC_ELEM,
+                              "executed_achieved": tc_exec, "executed_frac": tc_exec / bf16_peak,
+                              "traffic": 1.1448e9 if nelem == NELEM else None,
+                              "traffic_source": "ncu launch list (tcg_kernel, per colour launch)",
                               "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense TF32 is half of it)",
                               "algorithmic_flop_per_element": TAN_FLOP_PER_ELEM}}
         A.set_precision(headline_prec)
@@ -432,9 +446,18 @@ def main():
     elem_kernel_ms = elem_ms / max(elem_launches, 1)
     flop_per_launch = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) * elem_count / max(elem_launches, 1)
     achieved = flop_per_launch / (elem_kernel_ms * 1e-3) / 1e12
+    exec_ach = EXEC_FLOP_FP64_ELEM * elem_count / max(elem_launches, 1) / (elem_kernel_ms * 1e-3) / 1e12
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "traffic_note": "FP64-bound: DRAM traffic is negligible (see profiles/)",
-                "frac": achieved / fp64_peak, "traffic": None,
+                "frac": achieved / fp64_peak,
+                "frac_note": "achieved counts the dense R^T D R FLOPs per element; the kernel evaluates the "
+                             "same sum through Gram sums with 5.3x fewer FLOPs, so frac exceeds 1; "
+                             "executed_frac is the FP64 pipe fraction",
+                "executed_flop_per_element": EXEC_FLOP_FP64_ELEM, "executed_achieved": exec_ach,
+                "executed_frac": exec_ach / fp64_peak,
+                "traffic": TRAFFIC_FP64_LAUNCH if nelem == NELEM else None,
+                "traffic_source": "ncu launch list, dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                  "(profiles/assembly_launch_list_beam128x32x32.md); the geometry cache "
+                                  "re-read replaces FP64 recomputation",
                 "kernel": "element_kernel (fused residual+tangent, FP64)",
                 "peak_source": "measured in-run FP64 FMA throughput (MEASURED_PEAKS.json has no FP64 figure)",
                 "algorithmic_flop_per_element": TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM,
