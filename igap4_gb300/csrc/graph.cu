@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "spmv.cuh"
 
 namespace igap {
 
@@ -35,15 +36,14 @@ __global__ void gm_reset(GmState *st) { st->done = 0; st->its = 0; }
 
 __global__ void __launch_bounds__(256) gm_spmv(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
                                                const double *__restrict__ vals, const double *__restrict__ x,
-                                               double *__restrict__ y, int64_t n, const GmState *st)
+                                               double *__restrict__ y, int64_t n, const GmState *st, int nb0,
+                                               int nb1, int nb2)
 {
   if (st && st->done) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  double s = 0.0;
-  for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) s = fma(vals[k], x[cols[k]], s);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const double s = spmv_row(rowptr, cols, vals, x, row, lane, nb0, nb1, nb2);
   if (lane == 0) y[row] = s;
 }
 
@@ -249,7 +249,9 @@ static int build_gmres_graph(Context *c, int m, int pc)
   int64_t nodes = 0;
   IGAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   gm_reset<<<1, 1, 0, s>>>(gw->st);
-  gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->x, gw->r, n, nullptr);
+  const int nb0 = c->batch ? 0 : c->nbasis[0];
+  gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->x, gw->r, n, nullptr, nb0, c->nbasis[1],
+                             c->nbasis[2]);
   gm_sub_from<<<vb, 256, 0, s>>>(gw->r, gw->b, n);
   gm_dot_partial<<<RB, RT, 0, s>>>(gw->r, gw->r, n, gw->partial, nullptr);
   gm_dot_final<<<1, 1024, 0, s>>>(gw->partial, RB, gw->scal, 1, nullptr);
@@ -260,7 +262,8 @@ static int build_gmres_graph(Context *c, int m, int pc)
     double *vj = gw->V + (size_t)j * n, *zj = gw->Z + (size_t)j * n, *vn = gw->V + (size_t)(j + 1) * n;
     double *hcol = gw->H + (size_t)j * (m + 1);
     gm_precond<<<vb, 256, 0, s>>>(zj, vj, gw->diag, pc, n, gw->st);
-    gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st);
+    gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st, nb0, c->nbasis[1],
+                               c->nbasis[2]);
     nodes += 2;
     for (int i = 0; i <= j; i++) {
       gm_dot_partial<<<RB, RT, 0, s>>>(gw->w, gw->V + (size_t)i * n, n, gw->partial, gw->st);

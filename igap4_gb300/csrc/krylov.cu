@@ -11,27 +11,25 @@
 #include <vector>
 
 #include "common.cuh"
+#include "spmv.cuh"
 
 namespace igap {
 
 constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
 constexpr int RED_THREADS = 512;
 
-// y = A x, one warp per row (rows hold ~100-375 entries, contiguous).
+// y = A x, one warp per row (spmv_row; structured columns when nb0 > 0).
 __global__ void __launch_bounds__(256) spmv_csr_kernel(const int64_t *__restrict__ rowptr,
                                                        const int32_t *__restrict__ cols,
                                                        const double *__restrict__ vals,
                                                        const double *__restrict__ x,
-                                                       double *__restrict__ y, int64_t n)
+                                                       double *__restrict__ y, int64_t n, int nb0, int nb1,
+                                                       int nb2)
 {
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  const int64_t s0 = rowptr[row], s1 = rowptr[row + 1];
-  double s = 0.0;
-  for (int64_t k = s0 + lane; k < s1; k += 32) s = fma(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const double s = spmv_row(rowptr, cols, vals, x, row, lane, nb0, nb1, nb2);
   if (lane == 0) y[row] = s;
 }
 
@@ -130,8 +128,9 @@ static unsigned vec_blocks(int64_t n)
 int spmv(Context *c, const double *vals, const double *x, double *y)
 {
   const int64_t n = c->ndof;
-  spmv_csr_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols,
-                                                                            vals, x, y, n);
+  const int nb0 = c->batch ? 0 : c->nbasis[0];  // a batch's rows belong to different lattices
+  spmv_csr_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n,
+                                                                            nb0, c->nbasis[1], c->nbasis[2]);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;
