@@ -13,6 +13,7 @@
 //               CSR slots and residual rows they add into are disjoint.
 // Slots are computed arithmetically from the clipped structured stencil.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include "common.cuh"
 #include "laws.cuh"
 #include "element.cuh"
@@ -573,11 +574,111 @@ int launch_pattern_cols_at(Context *c, const int64_t *rowptr, int32_t *cols, int
 }
 
 // ------------------------------------------------------------ launches
+// ------------------------------------------------- law at every point
+// One CTA per (element, chunk of 8 points), one warp per point: geometry,
+// state and the law as in the element kernel's phase A; the weighted law
+// outputs (rr, D) go to global memory.  The law of a point does not depend on
+// the colouring, so all points run in one launch, where the colour launches
+// would evaluate one colour's elements at a time.
+struct LawPtSmem {
+  ElemData E;
+  PointScratch Pt[PW];
+  double R[PW][NB * NDD];
+  double rr[PW][30];
+  double D[PW][900];
+};
+
 template <int LAWK, bool RES, bool TAN>
-static int run_colours(Context *c, double *RR, double *vals)
+__global__ void __launch_bounds__(PW * 32, 1)
+    law_points_kernel(DevMesh m, DevLaw L, const double *__restrict__ Uhist, double *__restrict__ preR,
+                      double *__restrict__ preD)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LawPtSmem &S = *reinterpret_cast<LawPtSmem *>(smem_raw);
+  LawSmem<LAWK> &LS = *reinterpret_cast<LawSmem<LAWK> *>(smem_raw + sizeof(LawPtSmem));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nchunk = (m.npts + PW - 1) / PW;
+  const int64_t e = blockIdx.x / nchunk;
+  const int ch = (int)(blockIdx.x % nchunk);
+  const int ez = (int)(e % m.nelem[2]), ey = (int)((e / m.nelem[2]) % m.nelem[1]),
+            ex = (int)(e / ((int64_t)m.nelem[1] * m.nelem[2]));
+  load_element(S.E, m, L.nhist, Uhist, ex, ey, ez, tid, PW * 32);
+  __syncthreads();
+  point_setup<LAWK, RES, TAN, double>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp, ch * PW + warp, lane,
+                                      S.R[warp], S.rr[warp], S.D[warp]);
+  __syncthreads();
+  const int q0 = ch * PW;
+  const int nv = m.npts - q0 < PW ? m.npts - q0 : PW;
+  const int64_t p0 = e * m.npts + q0;
+  if (RES)
+    for (int i = tid; i < nv * 30; i += PW * 32) preR[p0 * 30 + i] = S.rr[i / 30][i % 30];
+  if (TAN)
+    for (int i = tid; i < nv * 900; i += PW * 32) preD[p0 * 900 + i] = S.D[i / 900][i % 900];
+}
+
+template <int LAWK, bool RES, bool TAN>
+static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
-  const DevLaw L = c->devlaw();
+  const size_t smem = sizeof(LawPtSmem) + sizeof(LawSmem<LAWK>);
+  auto kern = law_points_kernel<LAWK, RES, TAN>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  const int nchunk = (m.npts + PW - 1) / PW;
+  const int64_t nblk = c->nelem_total * nchunk;
+  kern<<<(unsigned)nblk, PW * 32, smem, c->stream>>>(m, L, c->d_Uhist, c->d_preR, c->d_preD);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
+{
+  if (c->law == IGAPGPU_LAW_LINGRAD || (!do_res && !do_tan)) return IGAPGPU_OK;
+  if (c->pre_state < 0) {
+    // decided once, outside any capture: the buffers are allocated when they
+    // take at most a quarter of the free memory; IGAPGPU_LAW_PRECOMPUTE=0 turns
+    // the precomputation off
+    c->pre_state = 0;
+    const char *env = getenv("IGAPGPU_LAW_PRECOMPUTE");
+    const size_t npt = (size_t)c->nelem_total * c->nquad * c->nquad * c->nquad;
+    size_t freeb = 0, totb = 0;
+    if (!c->capturing && !(env && env[0] == '0') && cudaMemGetInfo(&freeb, &totb) == cudaSuccess &&
+        npt * 930 * sizeof(double) < freeb / 4) {
+      if (cudaMalloc(&c->d_preR, npt * 30 * sizeof(double)) == cudaSuccess &&
+          cudaMalloc(&c->d_preD, npt * 900 * sizeof(double)) == cudaSuccess) {
+        c->pre_state = 1;
+      } else {
+        cudaGetLastError();
+        if (c->d_preR) cudaFree(c->d_preR);
+        c->d_preR = nullptr;
+      }
+    }
+  }
+  if (c->pre_state != 1) return IGAPGPU_OK;
+  int rc;
+  if (c->law == IGAPGPU_LAW_GRADELAST) {
+    rc = (do_res && do_tan) ? run_law_points<1, true, true>(c, L)
+         : do_res           ? run_law_points<1, true, false>(c, L)
+                            : run_law_points<1, false, true>(c, L);
+  } else {
+    rc = (do_res && do_tan) ? run_law_points<2, true, true>(c, L)
+         : do_res           ? run_law_points<2, true, false>(c, L)
+                            : run_law_points<2, false, true>(c, L);
+  }
+  if (rc) return rc;
+  L.preR = c->d_preR;
+  L.preD = c->d_preD;
+  return IGAPGPU_OK;
+}
+
+template <int LAWK, bool RES, bool TAN>
+static int run_colours(Context *c, const DevLaw &L, double *RR, double *vals)
+{
+  const DevMesh m = c->devmesh();
   const size_t smem = sizeof(typename ElemCfg<TAN>::Smem) + sizeof(LawSmem<LAWK>);
   auto kern = element_kernel<LAWK, RES, TAN>;
   static bool attr_set = false;
@@ -697,11 +798,16 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   }
   if (do_tan) IGAP_CUDA(cudaMemsetAsync(vals, 0, sizeof(double) * c->nnz, c->stream));
 #define IGAP_DISPATCH(LK)                                                   \
-  if (do_res && do_tan) rc = run_colours<LK, true, true>(c, RR, vals);      \
-  else if (do_res) rc = run_colours<LK, true, false>(c, RR, vals);          \
-  else rc = run_colours<LK, false, true>(c, RR, vals);
+  if (do_res && do_tan) rc = run_colours<LK, true, true>(c, L, RR, vals);   \
+  else if (do_res) rc = run_colours<LK, true, false>(c, L, RR, vals);       \
+  else rc = run_colours<LK, false, true>(c, L, RR, vals);
   // split precision: the residual stays FP64, the tangent goes to the tensor cores
   const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT;
+  // nonlinear laws: every point's law outputs in one launch, so that the
+  // colour launches do not evaluate the law colour after colour
+  DevLaw L = c->devlaw();
+  rc = launch_law_points(c, do_res, do_tan, L);
+  if (rc) return rc;
   const bool k_res = do_res, k_tan = fp64_tan;
   if (k_res || k_tan) {
     const bool do_res_k = k_res, do_tan_k = k_tan;
@@ -720,7 +826,7 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   if (rc) return rc;
   if (do_tan && !fp64_tan) {
     IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
-    rc = launch_tc_tangent(c, vals);
+    rc = launch_tc_tangent(c, vals, L);
     if (rc) return rc;
     if (!c->capturing) {  // a graph replay checks the error word itself
       int herr = 0;

@@ -71,6 +71,10 @@ struct DevLaw {
   const int *sl;           // [nnz]
   const float *sval;       // [nnz]
   int dnnz;
+  // weighted law outputs per point, [nelem][npts][30] and [nelem][npts][900],
+  // when computed for all points before the colour launches (else null)
+  const double *preR;
+  const double *preD;
 };
 
 struct GraphWork;
@@ -125,6 +129,9 @@ struct Context {
   double *d_neu = nullptr;     // traction table on the device [36]
   double *d_geo = nullptr;     // geometry cache (physical basis + weight per point)
   float *d_geof = nullptr;     // FP32 copy for the split-precision tangent
+  double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
+  double *d_preD = nullptr;
+  int pre_state = -1;          // -1 not decided, 0 off, 1 on
   int *d_dsparse = nullptr;    // sparse constant tangent: dptr | dcol | sptr | sl
   double *d_dval = nullptr;
   float *d_sval = nullptr;
@@ -195,6 +202,8 @@ struct Context {
     l.sl = d_dsparse ? d_dsparse + 31 + dnnz + 91 : nullptr;
     l.dval = d_dval;
     l.sval = d_sval;
+    l.preR = nullptr;
+    l.preD = nullptr;
     return l;
   }
 };
@@ -212,6 +221,9 @@ int context_free(Context *c);
 
 // assemble.cu
 int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
+// law outputs at every point of a nonlinear law in one launch; sets preR/preD
+// of `L` when the buffers exist (else leaves them null)
+int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L);
 int launch_basis_tables(Context *c);
 int launch_lingrad_dconst(Context *c);
 int launch_neumann(Context *c, const double nfac[NFACE][2]);
@@ -225,7 +237,7 @@ int launch_dirichlet_matrix_batch(Context *c, const int *d_inst, const int *d_nb
 int launch_geometry_cache(Context *c);
 int launch_geometry_cache_f32(Context *c);
 // tc_tangent.cu
-int launch_tc_tangent(Context *c, double *vals);
+int launch_tc_tangent(Context *c, double *vals, const DevLaw &L);
 // tc_gram.cu (linear isotropic law with the FP32 geometry cache)
 int launch_tc_gram(Context *c, double *vals);
 int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals);

@@ -210,6 +210,17 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
     wt = point_geometry(E, P, m, ex, ey, ez, q, lane, R);
   }
   if (lane == 0) P.wt = wt;
+  if constexpr (LAWK != 0) {
+    if (L.preR) {  // law outputs of every point computed beforehand (law_points_kernel)
+      const int64_t pq = (((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez) * m.npts + q;
+      if (RES)
+        for (int i = lane; i < 30; i += 32) rr[i] = __ldg(L.preR + pq * 30 + i);
+      if (TAN && fill_D)
+        for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preD + pq * 900 + i);
+      __syncwarp();
+      return;
+    }
+  }
   // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
   const int nh = L.nhist;
   constexpr bool NEED_U = RES || LAWK != 0;

@@ -433,10 +433,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 template <int LAWK>
-static int run_tc(Context *c, double *vals)
+static int run_tc(Context *c, const DevLaw &L, double *vals)
 {
   const DevMesh m = c->devmesh();
-  const DevLaw L = c->devlaw();
   const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
   auto kern = tc_tangent_kernel<LAWK>;
   static bool attr = false;
@@ -502,12 +501,12 @@ int launch_tc_batch(Context *c, const BatchArgs &a, int law, int grid, const dou
   return IGAPGPU_ERR_LAW;
 }
 
-int launch_tc_tangent(Context *c, double *vals)
+int launch_tc_tangent(Context *c, double *vals, const DevLaw &L)
 {
   if (c->law == IGAPGPU_LAW_LINGRAD && c->d_geof && !getenv("IGAPGPU_TC_DENSE")) return launch_tc_gram(c, vals);
-  if (c->law == IGAPGPU_LAW_LINGRAD) return run_tc<0>(c, vals);
-  if (c->law == IGAPGPU_LAW_GRADELAST) return run_tc<1>(c, vals);
-  if (c->law == IGAPGPU_LAW_GRADELASTTIME) return run_tc<2>(c, vals);
+  if (c->law == IGAPGPU_LAW_LINGRAD) return run_tc<0>(c, L, vals);
+  if (c->law == IGAPGPU_LAW_GRADELAST) return run_tc<1>(c, L, vals);
+  if (c->law == IGAPGPU_LAW_GRADELASTTIME) return run_tc<2>(c, L, vals);
   set_error("unknown law %d", c->law);
   return IGAPGPU_ERR_LAW;
 }
