@@ -115,7 +115,7 @@ def main():
     from .predictor import LearnedPredictor
 
     nelem = tuple(int(v) for v in a.nelem.split(","))
-    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30)
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30, use_graphs=1)
     A, _ = transient_problem(nelem, a.dt)
     t0 = time.perf_counter()
     trajs = generate(A, range(1000, 1000 + a.train), a.steps, a.dt, a.amax, opts)

@@ -71,7 +71,7 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     # the context works on torch's current stream, so residuals read by torch
     # (the predictor's acceptance test) are ordered after the kernels
     A.set_stream(torch.cuda.current_stream(dev).cuda_stream)
-    o = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30)
+    o = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30, use_graphs=1)
     if opts:
         o.update(opts)
     zero = torch.zeros(A.ndof, dtype=torch.float64, device=dev)

@@ -67,7 +67,7 @@ def test_trained_predictor_reduces_newton_iterations():
     from igap4_gb300.predictor import LearnedPredictor
 
     nelem, dt, amax, steps = (8, 2, 2), 1e-2, 1e-3, 25
-    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30)
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30, use_graphs=1)
     A, _ = tp.transient_problem(nelem, dt)
     trajs = tp.generate(A, [11, 12, 13], steps, dt, amax, opts)
     X, Y = tp.build_dataset(trajs)
