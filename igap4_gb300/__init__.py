@@ -80,6 +80,7 @@ def lib():
         L.igapgpu_sizes.argtypes = [vp] + [ctypes.c_void_p] * 4
         L.igapgpu_pattern.argtypes = [vp, vp, vp]
         L.igapgpu_dirichlet.argtypes = [vp, vp, vp, vp]
+        L.igapgpu_density.argtypes = [vp, vp, vp]
         L.igapgpu_impose_dirichlet.argtypes = [vp, vp]
         for f in ("igapgpu_set_history", "igapgpu_get_history"):
             getattr(L, f).argtypes = [vp, ctypes.c_int, vp]
@@ -253,6 +254,14 @@ class Assembly:
         if n.value:
             _check(lib().igapgpu_dirichlet(self.h, ctypes.byref(n), _ptr(rows), _ptr(vals)))
         return rows, vals
+
+    def density(self):
+        """Densities of the law integrated over the body on the current state
+        (iga_intdensity of the reference)."""
+        HH = np.zeros(16)
+        n = ctypes.c_int()
+        _check(lib().igapgpu_density(self.h, _ptr(HH), ctypes.byref(n)))
+        return HH[:n.value].copy()
 
     def impose_dirichlet(self, U):
         """U[r] = g_r on the Dirichlet rows, in place (host array or CUDA tensor)."""

@@ -132,6 +132,7 @@ struct Context {
   double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
   double *d_preD = nullptr;
   int pre_state = -1;          // -1 not decided, 0 off, 1 on
+  double *d_dens = nullptr;    // per-element density sums + result (igapgpu_density, lazy)
   int *d_dsparse = nullptr;    // sparse constant tangent: dptr | dcol | sptr | sl
   double *d_dval = nullptr;
   float *d_sval = nullptr;

@@ -123,6 +123,13 @@ int igapgpu_dirichlet(igapgpu_t ctx, int64_t *count, int64_t *rows, double *valu
  * iterate meets the constraints the Newton correction does not move. */
 int igapgpu_impose_dirichlet(igapgpu_t ctx, double *U);
 
+/* iga_intdensity (src/postcore_iga.c:13-377): the law's densities integrated
+ * over the body on the current U_hist, minus the traction term on the Neumann
+ * faces.  HH receives *ndensity values (at most 16): the static gradient law
+ * 13 (energy, 2 dpsi/dE_ab, sector fractions), the transient law 2 (energy
+ * incl. kinetic, volume), the linear law 2 (energy, volume). */
+int igapgpu_density(igapgpu_t ctx, double *HH, int *ndensity);
+
 /* State history U_hist[level] (level 0 current, 1 = u_n, 2 = u_{n-1}). */
 int igapgpu_set_history(igapgpu_t ctx, int level, const double *U);
 int igapgpu_get_history(igapgpu_t ctx, int level, double *U);

@@ -77,3 +77,39 @@ void lingrad_tangent(double *tt, double *u, double *par)
     for (int r = 0; r < 30; r++) tt[30 * r + c] = col[r];
   }
 }
+
+/* Densities for the integral of the law over the body, in the layout of the
+ * reference's density callbacks (include/physimpl.h:9-10): h[0] the stored
+ * energy psi above, h[1] = 1 (the integral is the volume).  Boundary: h[0] =
+ * u0 * traction (the traction's work term), h[1] = 0. */
+void lingrad_density(double h[], double u[], double *par)
+{
+  const double lam = par[0], mu = par[1], ell = par[2];
+  double eps[3][3], kap[3][3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      eps[i][j] = 0.5 * (u[10 * i + 1 + j] + u[10 * j + 1 + i]);
+      for (int m = 0; m < 3; m++)
+        kap[i][j][m] = 0.5 * (u[10 * i + 4 + sym_index(j, m)] + u[10 * j + 4 + sym_index(i, m)]);
+    }
+  double tr = eps[0][0] + eps[1][1] + eps[2][2], ee = 0.0, kk = 0.0, tk = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      ee += eps[i][j] * eps[i][j];
+      for (int m = 0; m < 3; m++) kk += kap[i][j][m] * kap[i][j][m];
+    }
+  for (int m = 0; m < 3; m++) {
+    const double t = kap[0][0][m] + kap[1][1][m] + kap[2][2][m];
+    tk += t * t;
+  }
+  h[0] = 0.5 * lam * tr * tr + mu * ee + ell * ell * (0.5 * lam * tk + mu * kk);
+  h[1] = 1.0;
+}
+
+void lingrad_densityb(double h[], double u[], double traction, double *par, int order)
+{
+  (void)par;
+  (void)order;
+  h[0] = u[0] * traction;
+  h[1] = 0.0;
+}

@@ -85,6 +85,7 @@ def ref():
                   "ref_case_global_idx"):
             getattr(_ref, f).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _ref.ref_case_tangent_csr.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
+        _ref.ref_case_density.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _ref.ref_case_mesh_info.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_case_mesh_arrays.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_gauss_legendre.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D]
@@ -254,6 +255,13 @@ class RefCase:
         RR = np.zeros(self.ndof)
         ref().ref_case_residual(self.h, RR.ctypes.data)
         return RR
+
+    def density(self, U_hist):
+        """iga_intdensity of the reference on this state (its densities)."""
+        self.set_state(U_hist)
+        HH = np.zeros(16)
+        n = ref().ref_case_density(self.h, HH.ctypes.data)
+        return HH[:n].copy()
 
     def tangent(self, U_hist):
         self.set_state(U_hist)

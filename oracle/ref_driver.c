@@ -29,6 +29,7 @@
 #include "interface.h"
 #include "physgradelast.h"
 #include "physgradelasttime.h"
+#include "postcore.h"
 #include "meshigabeam.h"
 #include "meshigabeamtest.h"
 #include "gradelast.h"
@@ -108,8 +109,8 @@ static Mesh mesh_beam_dir(const int nelem[3], const double L[3], int porder, con
 }
 
 /* ---- project linear law plugin, same struct as PhysGradElast ---------- */
-static void lingrad_density(double h[], double u[], double *par) { (void)u; (void)par; h[0] = 0; h[1] = 1; }
-static void lingrad_densityb(double h[], double u[], double t, double *par, int o) { (void)h; (void)u; (void)t; (void)par; (void)o; }
+void lingrad_density(double h[], double u[], double *par);
+void lingrad_densityb(double h[], double u[], double t, double *par, int o);
 static void lingrad_field(double *f, double *u, double *par) { (void)f; (void)u; (void)par; }
 static void lingrad_assert(double *par) { (void)par; }
 
@@ -181,6 +182,15 @@ void *ref_case_create(const int nelem[3], const double L[3], int porder, const i
   c->torder = c->igap->core->phys[0]->torder;
   c->ndof_total = c->igap->iocomm->nDof;
   return c;
+}
+
+/* iga_intdensity (src/postcore_iga.c:13-377) on the current U_hist; returns
+ * the number of densities written to HH. */
+int ref_case_density(void *h, double *HH)
+{
+  RefCase *c = (RefCase *)h;
+  iga_intdensity(HH, c->igap->core);
+  return c->igap->core->phys[0]->ndensity;
 }
 
 int ref_case_ndof(void *h) { return ((RefCase *)h)->ndof_total; }

@@ -2,7 +2,8 @@
 
 The reference sources are compiled unchanged (oracle/build_ref.sh) into
 oracle/_ref/libigapref.so and driven through its public set-up
-(IGAPAssmInit) and its SNES callbacks (Residual_iga / Tangent_iga).  The
+(IGAPAssmInit), its SNES callbacks (Residual_iga / Tangent_iga) and its
+density integral (iga_intdensity, stored as HH).  The
 fixtures are what the reference outputs for seeded inputs, so tests on a
 machine without the reference tree still compare against the reference.
 
@@ -54,7 +55,7 @@ def main():
         rowptr, cols, vals = case.tangent(U)
         meta = dict(nelem=np.array(prob.nelem), L=np.array(prob.L), law=prob.law,
                     perturb=int(prob.perturb), seed=seed, par=prob.params(),
-                    bc_type=prob.bc_type, neumann=prob.neumann, U=U, RR=RR)
+                    bc_type=prob.bc_type, neumann=prob.neumann, U=U, RR=RR, HH=case.density(U))
         if name in FULL_CASES:
             meta.update(rowptr=rowptr, cols=cols, vals=vals)
         else:

@@ -321,3 +321,16 @@ def test_law_at_every_point_identical(law, monkeypatch):
     np.testing.assert_array_equal(out["1"][0], out["0"][0])
     np.testing.assert_array_equal(out["1"][1], out["0"][1])
     assert rel(out["1"][2], out["0"][2]) <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["g_static_2x2x2", "g_lingrad_4x2x2", "g_transient_3x2x2",
+                                  "g_static_beamtest_4x4x4", "g_lingrad_8x2x2"])
+def test_density_integral_vs_reference(name):
+    """igapgpu_density against the reference's iga_intdensity (golden HH):
+    energies, stresses, sector fractions, volume, traction work."""
+    g = load(name)
+    A = gpu_case(problem_from_golden(g))
+    A.set_state(g["U"])
+    HH = A.density()
+    assert HH.shape == g["HH"].shape
+    np.testing.assert_allclose(HH, g["HH"], rtol=1e-12, atol=1e-12 * np.abs(g["HH"]).max())

@@ -205,3 +205,22 @@ def test_global_idx_identity_on_one_rank():
     prob = po.Problem(nelem=(3, 2, 2))
     g = po.RefCase(prob).global_idx()
     np.testing.assert_array_equal(g, np.arange(prob.ndof))
+
+
+@pytest.mark.skipif(not po.ref_available(), reason="needs oracle/_ref (reference sources)")
+def test_reference_density_volume_known_answer():
+    """The reference's density integral: its volume density integrates to the
+    volume of the beam geometry, L_d (1 + 1/n_d) per direction for the
+    control-net formula of mesh/igabeam.c:68-70."""
+    for law, nelem, L in ((po.LAW_GRADELASTTIME, (3, 2, 2), (1.0, 1.0, 1.0)),
+                          (po.LAW_LINGRAD, (4, 2, 3), (4.0, 1.0, 1.0))):
+        prob = po.Problem(nelem=nelem, L=L, law=law)
+        HH = po.RefCase(prob).density(po.random_state(prob, 5))
+        vol = np.prod([l * (1.0 + 1.0 / n) for l, n in zip(L, nelem)])
+        assert abs(HH[1] - vol) <= 1e-12 * vol
+
+
+def test_golden_densities_present():
+    for name in ("g_static_2x2x2", "g_lingrad_4x2x2", "g_transient_3x2x2"):
+        g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+        assert "HH" in g.files and np.all(np.isfinite(g["HH"]))
