@@ -81,6 +81,8 @@ def lib():
         L.igapgpu_pattern.argtypes = [vp, vp, vp]
         L.igapgpu_dirichlet.argtypes = [vp, vp, vp, vp]
         L.igapgpu_density.argtypes = [vp, vp, vp]
+        L.igapgpu_save_solution.argtypes = [vp, ctypes.c_char_p]
+        L.igapgpu_load_solution.argtypes = [vp, ctypes.c_char_p]
         L.igapgpu_impose_dirichlet.argtypes = [vp, vp]
         for f in ("igapgpu_set_history", "igapgpu_get_history"):
             getattr(L, f).argtypes = [vp, ctypes.c_int, vp]
@@ -262,6 +264,14 @@ class Assembly:
         n = ctypes.c_int()
         _check(lib().igapgpu_density(self.h, _ptr(HH), ctypes.byref(n)))
         return HH[:n.value].copy()
+
+    def save_solution(self, fname):
+        """Write the reference's solution file (IGAPSolvSaveSolution layout)."""
+        _check(lib().igapgpu_save_solution(self.h, os.fsencode(fname)))
+
+    def load_solution(self, fname):
+        """Read a solution file written by the reference or by save_solution."""
+        _check(lib().igapgpu_load_solution(self.h, os.fsencode(fname)))
 
     def impose_dirichlet(self, U):
         """U[r] = g_r on the Dirichlet rows, in place (host array or CUDA tensor)."""

@@ -149,6 +149,7 @@ struct Context {
   double *d_Z = nullptr;       // [restart][ndof] (right-preconditioned directions)
   double *d_work = nullptr;    // [4][ndof]
   double *d_diag = nullptr;    // [ndof]
+  double *d_bdiag = nullptr;   // [3 ndof] inverted 3 x 3 point blocks (point-block Jacobi)
   double *d_red = nullptr;     // device scalars (norms, Hessenberg column) [red_cap]
   double *h_red = nullptr;     // pinned host mirror of d_red [red_cap]
   double *d_partial = nullptr; // per-block partial sums of the reductions

@@ -164,7 +164,7 @@ static int free_ctx(Context *c)
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
-                  c->d_diag, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
+                  c->d_diag, c->d_bdiag, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int d = 0; d < 3; d++) {
@@ -586,6 +586,68 @@ int igapgpu_impose_dirichlet(igapgpu_t c, double *U)
   int r = launch_impose_dirichlet(c, c->d_RR);
   if (r) return r;
   IGAP_CUDA(cudaMemcpyAsync(U, c->d_RR, sizeof(double) * c->ndof, cudaMemcpyDeviceToHost, c->stream));
+  IGAP_CUDA(cudaStreamSynchronize(c->stream));
+  return IGAPGPU_OK;
+}
+
+// Solution files of IGAPSolvSaveSolution / IGAPSolvLoadSolution
+// (src/interface.c:271-300, write_solution / read_solution, src/ioutil.c:90-159):
+// raw FP64 history levels in the universal DOF order, which on one rank with a
+// non-periodic mesh is the DOF numbering 3 cp + d.  Static laws store level 0,
+// the transient law levels 1..torder (loading also sets level 0 = level 1).
+static void solution_levels(const Context *c, int *l0, int *l1)
+{
+  *l0 = c->torder == 0 ? 0 : 1;
+  *l1 = c->torder == 0 ? 1 : c->torder + 1;
+}
+
+int igapgpu_save_solution(igapgpu_t c, const char *fname)
+{
+  if (!c || !fname) return IGAPGPU_ERR_ARG;
+  int l0, l1;
+  solution_levels(c, &l0, &l1);
+  const size_t n = (size_t)(l1 - l0) * c->ndof;
+  std::vector<double> h(n);
+  IGAP_CUDA(cudaMemcpyAsync(h.data(), c->d_Uhist + (size_t)l0 * c->ndof, sizeof(double) * n,
+                            cudaMemcpyDeviceToHost, c->stream));
+  IGAP_CUDA(cudaStreamSynchronize(c->stream));
+  FILE *f = fopen(fname, "wb");
+  if (!f) {
+    set_error("cannot open %s for writing", fname);
+    return IGAPGPU_ERR_ARG;
+  }
+  const size_t w = fwrite(h.data(), sizeof(double), n, f);
+  fclose(f);
+  if (w != n) {
+    set_error("short write to %s", fname);
+    return IGAPGPU_ERR_ARG;
+  }
+  return IGAPGPU_OK;
+}
+
+int igapgpu_load_solution(igapgpu_t c, const char *fname)
+{
+  if (!c || !fname) return IGAPGPU_ERR_ARG;
+  int l0, l1;
+  solution_levels(c, &l0, &l1);
+  const size_t n = (size_t)(l1 - l0) * c->ndof;
+  std::vector<double> h(n);
+  FILE *f = fopen(fname, "rb");
+  if (!f) {
+    set_error("cannot open %s", fname);
+    return IGAPGPU_ERR_ARG;
+  }
+  const size_t r = fread(h.data(), sizeof(double), n, f);
+  fclose(f);
+  if (r != n) {
+    set_error("%s holds %zu of the %zu values of this problem's solution file", fname, r, n);
+    return IGAPGPU_ERR_ARG;
+  }
+  IGAP_CUDA(cudaMemcpyAsync(c->d_Uhist + (size_t)l0 * c->ndof, h.data(), sizeof(double) * n,
+                            cudaMemcpyHostToDevice, c->stream));
+  if (l0 == 1)
+    IGAP_CUDA(cudaMemcpyAsync(c->d_Uhist, c->d_Uhist + c->ndof, sizeof(double) * c->ndof,
+                              cudaMemcpyDeviceToDevice, c->stream));
   IGAP_CUDA(cudaStreamSynchronize(c->stream));
   return IGAPGPU_OK;
 }

@@ -103,6 +103,10 @@ __global__ void gm_scale_div(double *y, const double *x, const double *den, int6
 __global__ void gm_precond(double *z, const double *v, const double *diag, int pc, int64_t n, const GmState *st)
 {
   if (st->done) return;
+  if (pc == 2) {  // point-block Jacobi: diag holds the inverted 3 x 3 blocks
+    bdiag_apply(z, v, diag, n / 3);
+    return;
+  }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double d = pc ? diag[i] : 1.0;
     z[i] = v[i] / (d != 0.0 ? d : 1.0);
@@ -234,7 +238,7 @@ static int build_gmres_graph(Context *c, int m, int pc)
       alloc(&gw->V, (size_t)(m + 1) * n) || alloc(&gw->Z, (size_t)m * n) ||
       alloc(&gw->H, (size_t)(m + 1) * m) || alloc(&gw->cs, m) || alloc(&gw->sn, m) ||
       alloc(&gw->g, m + 1) || alloc(&gw->y, m) || alloc(&gw->scal, m + 2) || alloc(&gw->partial, RB) ||
-      alloc(&gw->diag, n) || cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
+      alloc(&gw->diag, 3 * n) || cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
       cudaMallocHost(&gw->h_st, sizeof(GmState)) != cudaSuccess) {
     cudaGetLastError();
     free_graph(gw);
@@ -304,7 +308,7 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
                     double *rnorm_out)
 {
   const int m = o->ksp_restart > 0 ? o->ksp_restart : 30;
-  const int pc = o->pc == 1 ? 1 : 0;
+  const int pc = (o->pc == 1 || o->pc == 2) ? o->pc : 0;
   if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc) {
     int r = build_gmres_graph(c, m, pc);
     if (r) return r;
@@ -314,8 +318,13 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
   cudaStream_t s = c->stream;
   IGAP_CUDA(cudaMemcpyAsync(gw->b, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   IGAP_CUDA(cudaMemcpyAsync(gw->x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  if (pc) {
+  if (pc == 1) {
     get_diag_kernel_g<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->diag, n);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+  } else if (pc == 2) {
+    bdiag_invert_kernel<<<(unsigned)((n / 3 + 255) / 256), 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->diag,
+                                                                      n / 3);
     count_launch();
     IGAP_CHECK_LAUNCH();
   }

@@ -105,6 +105,11 @@ __global__ void scale_div_kernel(double *y, const double *x, const double *pden,
     y[i] = x[i] * inv;
 }
 // z = v / diag (Jacobi; zero diagonal -> 1, as PCJACOBI)
+__global__ void bdiag_kernel(double *z, const double *v, const double *inv, int64_t ncp)
+{
+  bdiag_apply(z, v, inv, ncp);
+}
+
 __global__ void jacobi_kernel(double *z, const double *v, const double *diag, int64_t n)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -150,7 +155,8 @@ static int ensure_krylov(Context *c, int restart)
 {
   if (c->d_work == nullptr) {
     if (cudaMalloc(&c->d_work, sizeof(double) * 4 * c->ndof) != cudaSuccess ||
-        cudaMalloc(&c->d_diag, sizeof(double) * c->ndof) != cudaSuccess) {
+        cudaMalloc(&c->d_diag, sizeof(double) * c->ndof) != cudaSuccess ||
+        cudaMalloc(&c->d_bdiag, sizeof(double) * 3 * c->ndof) != cudaSuccess) {
       cudaGetLastError();
       set_error("Krylov workspace allocation failed");
       return IGAPGPU_ERR_NOMEM;
@@ -211,6 +217,11 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
   if (o->pc == 1) {
     get_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, c->d_vals, c->d_diag, n);
     count_launch();
+  } else if (o->pc == 2) {  // point-block Jacobi: inverted 3 x 3 blocks, 9 per control point
+    bdiag_invert_kernel<<<(unsigned)((n / 3 + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, c->d_vals,
+                                                                               c->d_bdiag, n / 3);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
   }
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   double rnorm0 = -1.0, rnorm = 0.0;
@@ -246,6 +257,9 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
       double *vj = V + (size_t)j * n, *zj = Z + (size_t)j * n, *vn = V + (size_t)(j + 1) * n;
       if (o->pc == 1) {
         jacobi_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_diag, n);
+        count_launch();
+      } else if (o->pc == 2) {
+        bdiag_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_bdiag, n / 3);
         count_launch();
       } else {
         IGAP_CUDA(cudaMemcpyAsync(zj, vj, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));

@@ -61,3 +61,59 @@ __device__ __forceinline__ double spmv_row(const int64_t *__restrict__ rowptr, c
 }
 
 }  // namespace igap
+
+namespace igap {
+
+// Point-block Jacobi: the 3x3 diagonal block of every control point (rows and
+// columns 3 cp .. 3 cp + 2; a control point's columns are consecutive in its
+// rows), inverted in FP64.  A block with zero or non-finite determinant falls
+// back to the inverse of its diagonal (1 where that is zero).
+static __global__ void bdiag_invert_kernel(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                    const double *__restrict__ vals, double *__restrict__ inv, int64_t ncp)
+{
+  const int64_t cp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cp >= ncp) return;
+  double a[9];
+  for (int d = 0; d < 3; d++) {
+    const int64_t r = 3 * cp + d;
+    int64_t lo = rowptr[r], hi = rowptr[r + 1];
+    const int64_t target = 3 * cp;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (cols[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    const bool ok = lo + 2 < rowptr[r + 1] && cols[lo] == target;
+    for (int e = 0; e < 3; e++) a[3 * d + e] = ok ? vals[lo + e] : (d == e ? 1.0 : 0.0);
+  }
+  const double c0 = a[4] * a[8] - a[5] * a[7], c1 = a[2] * a[7] - a[1] * a[8], c2 = a[1] * a[5] - a[2] * a[4];
+  const double c3 = a[5] * a[6] - a[3] * a[8], c4 = a[0] * a[8] - a[2] * a[6], c5 = a[2] * a[3] - a[0] * a[5];
+  const double c6 = a[3] * a[7] - a[4] * a[6], c7 = a[1] * a[6] - a[0] * a[7], c8 = a[0] * a[4] - a[1] * a[3];
+  const double det = a[0] * c0 + a[1] * c3 + a[2] * c6;
+  double *o = inv + 9 * cp;
+  if (det != 0.0 && isfinite(det)) {
+    const double id = 1.0 / det;
+    o[0] = c0 * id; o[1] = c1 * id; o[2] = c2 * id;
+    o[3] = c3 * id; o[4] = c4 * id; o[5] = c5 * id;
+    o[6] = c6 * id; o[7] = c7 * id; o[8] = c8 * id;
+  } else {
+    for (int i = 0; i < 9; i++) o[i] = 0.0;
+    for (int d = 0; d < 3; d++) o[4 * d] = a[4 * d] != 0.0 ? 1.0 / a[4 * d] : 1.0;
+  }
+}
+
+// z = B^-1 v with the inverted blocks
+__device__ __forceinline__ void bdiag_apply(double *__restrict__ z, const double *__restrict__ v,
+                                            const double *__restrict__ inv, int64_t ncp)
+{
+  for (int64_t cp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cp < ncp;
+       cp += (int64_t)gridDim.x * blockDim.x) {
+    const double *b = inv + 9 * cp;
+    const double v0 = v[3 * cp], v1 = v[3 * cp + 1], v2 = v[3 * cp + 2];
+    z[3 * cp] = b[0] * v0 + b[1] * v1 + b[2] * v2;
+    z[3 * cp + 1] = b[3] * v0 + b[4] * v1 + b[5] * v2;
+    z[3 * cp + 2] = b[6] * v0 + b[7] * v1 + b[8] * v2;
+  }
+}
+
+}  // namespace igap

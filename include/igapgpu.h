@@ -85,7 +85,7 @@ typedef struct {
   double ksp_abstol;
   double ksp_dtol;
   int ksp_max_it;
-  int pc;              /* 0 = none, 1 = Jacobi */
+  int pc;              /* 0 = none, 1 = Jacobi, 2 = point-block Jacobi (3 x 3 blocks of each control point) */
   int use_graphs;      /* 1: assembly and GMRES cycles replayed as CUDA graphs */
 } igapgpu_solver_opts;
 
@@ -129,6 +129,13 @@ int igapgpu_impose_dirichlet(igapgpu_t ctx, double *U);
  * 13 (energy, 2 dpsi/dE_ab, sector fractions), the transient law 2 (energy
  * incl. kinetic, volume), the linear law 2 (energy, volume). */
 int igapgpu_density(igapgpu_t ctx, double *HH, int *ndensity);
+
+/* IGAPSolvSaveSolution / IGAPSolvLoadSolution (src/interface.c:271-300): the
+ * reference's solution file (write_solution / read_solution, src/ioutil.c:
+ * 90-159), raw FP64 levels in DOF order; static laws level 0, the transient
+ * law levels 1..torder (load also sets level 0 = level 1). */
+int igapgpu_save_solution(igapgpu_t ctx, const char *fname);
+int igapgpu_load_solution(igapgpu_t ctx, const char *fname);
 
 /* State history U_hist[level] (level 0 current, 1 = u_n, 2 = u_{n-1}). */
 int igapgpu_set_history(igapgpu_t ctx, int level, const double *U);

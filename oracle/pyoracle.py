@@ -86,6 +86,8 @@ def ref():
             getattr(_ref, f).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _ref.ref_case_tangent_csr.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_case_density.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        _ref.ref_case_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        _ref.ref_case_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         _ref.ref_case_mesh_info.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_case_mesh_arrays.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_gauss_legendre.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D]
@@ -255,6 +257,12 @@ class RefCase:
         RR = np.zeros(self.ndof)
         ref().ref_case_residual(self.h, RR.ctypes.data)
         return RR
+
+    def save(self, fname):
+        ref().ref_case_save(self.h, os.fsencode(fname))
+
+    def load(self, fname):
+        ref().ref_case_load(self.h, os.fsencode(fname))
 
     def density(self, U_hist):
         """iga_intdensity of the reference on this state (its densities)."""

@@ -30,6 +30,7 @@
 #include "physgradelast.h"
 #include "physgradelasttime.h"
 #include "postcore.h"
+#include "ioutil.h"
 #include "meshigabeam.h"
 #include "meshigabeamtest.h"
 #include "gradelast.h"
@@ -191,6 +192,23 @@ int ref_case_density(void *h, double *HH)
   RefCase *c = (RefCase *)h;
   iga_intdensity(HH, c->igap->core);
   return c->igap->core->phys[0]->ndensity;
+}
+
+/* IGAPSolvSaveSolution / IGAPSolvLoadSolution of the reference (src/interface.c:271-300). */
+void ref_case_save(void *h, const char *fname) { IGAPSolvSaveSolution(((RefCase *)h)->igap, fname); }
+/* IGAPSolvLoadSolution minus its final copy into the SNES vector (no solver
+ * here): read_solution (src/ioutil.c:127) on the same levels. */
+void ref_case_load(void *h, const char *fname)
+{
+  RefCase *c = (RefCase *)h;
+  double *U = c->igap->core->U_hist;
+  const int n = c->igap->iocomm->nDof;
+  if (c->torder == 0) {
+    read_solution(fname, U, c->igap->iocomm, 0, 1);
+  } else {
+    read_solution(fname, U, c->igap->iocomm, 1, c->torder + 1);
+    for (int i = 0; i < n; i++) U[i] = U[n + i];
+  }
 }
 
 int ref_case_ndof(void *h) { return ((RefCase *)h)->ndof_total; }

@@ -334,3 +334,61 @@ def test_density_integral_vs_reference(name):
     HH = A.density()
     assert HH.shape == g["HH"].shape
     np.testing.assert_allclose(HH, g["HH"], rtol=1e-12, atol=1e-12 * np.abs(g["HH"]).max())
+
+
+@pytest.mark.parametrize("law", [po.LAW_GRADELAST, po.LAW_GRADELASTTIME])
+def test_solution_file_round_trip(law, tmp_path):
+    """save_solution writes the reference's solution file (raw FP64 levels in
+    DOF order, pinned against the reference's writer in test_oracle.py);
+    load_solution reads it back, also from a file written by numpy."""
+    prob = po.Problem(nelem=(3, 2, 2), law=law)
+    A = gpu_case(prob)
+    U = po.random_state(prob, 31)
+    A.set_state(U)
+    f = tmp_path / "U.bin"
+    A.save_solution(str(f))
+    raw = np.fromfile(f, dtype="<f8")
+    exp = U[0] if A.torder == 0 else U[1:].ravel()
+    np.testing.assert_array_equal(raw, exp)
+    A.set_state(np.zeros_like(U))
+    g = tmp_path / "V.bin"
+    V = np.random.default_rng(32).standard_normal(exp.size)
+    V.astype("<f8").tofile(g)
+    A.load_solution(str(g))
+    levels = V.reshape(-1, A.ndof)
+    if A.torder == 0:
+        np.testing.assert_array_equal(A.get_history(0), levels[0])
+    else:
+        for lvl in range(1, A.torder + 1):
+            np.testing.assert_array_equal(A.get_history(lvl), levels[lvl - 1])
+        np.testing.assert_array_equal(A.get_history(0), levels[0])
+    with pytest.raises(ig.IgapGpuError):
+        A.load_solution(str(tmp_path / "missing.bin"))
+
+
+def test_point_block_jacobi_gmres():
+    """GMRES with 3x3 point-block Jacobi (pc=2) solves the linear beam to the
+    direct solution, in the host-driven and the graph-replayed cycles, in no
+    more iterations than scalar Jacobi."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(8, 3, 2), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, perturb=True, bc_type=bct,
+                      neumann=neu)
+    A = gpu_case(prob)
+    A.tangent_internal(np.zeros(A.ndof))
+    rowptr, cols = A.pattern()
+    K = sp.csr_matrix((A.tangent(), cols, rowptr), shape=(A.ndof, A.ndof))
+    b = np.random.default_rng(4).standard_normal(A.ndof)
+    xs = spl.spsolve(K.tocsc(), b)
+    its = {}
+    for pc in (1, 2):
+        for graphs in (0, 1):
+            x = np.zeros(A.ndof)
+            n, rn = A.ksp_solve(b, x, ksp_rtol=1e-10, ksp_restart=200, ksp_max_it=40000, pc=pc,
+                                use_graphs=graphs)
+            assert np.linalg.norm(K @ x - b) <= 1e-9 * np.linalg.norm(b)
+            assert rel(x, xs) <= 1e-6
+            its[(pc, graphs)] = n
+    assert its[(2, 0)] == its[(2, 1)]
+    assert its[(2, 0)] <= its[(1, 0)], its

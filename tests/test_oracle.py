@@ -224,3 +224,31 @@ def test_golden_densities_present():
     for name in ("g_static_2x2x2", "g_lingrad_4x2x2", "g_transient_3x2x2"):
         g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
         assert "HH" in g.files and np.all(np.isfinite(g["HH"]))
+
+
+@pytest.mark.skipif(not po.ref_available(), reason="needs oracle/_ref (reference sources)")
+def test_reference_solution_file_layout(tmp_path):
+    """The reference's solution file (IGAPSolvSaveSolution) is the raw FP64
+    history levels in DOF order: level 0 for a static law, levels 1..torder
+    for the transient law; its reader restores them (level 0 = level 1)."""
+    for law, nelem in ((po.LAW_GRADELAST, (3, 2, 2)), (po.LAW_GRADELASTTIME, (2, 3, 2))):
+        prob = po.Problem(nelem=nelem, law=law)
+        rc = po.RefCase(prob)
+        U = po.random_state(prob, 9)
+        rc.set_state(U)
+        f = str(tmp_path / f"U_{law}.bin")
+        rc.save(f)
+        raw = np.fromfile(f, dtype="<f8")
+        levels = U.reshape(-1, rc.ndof)
+        exp = levels[0] if law == po.LAW_GRADELAST else levels[1:].ravel()
+        np.testing.assert_array_equal(raw, exp)
+        rc.set_state(np.zeros_like(U))
+        rc.load(f)
+        got = np.zeros_like(U)
+        po.ref().ref_case_get_state(rc.h, got.ctypes.data)
+        got = got.reshape(-1, rc.ndof)
+        if law == po.LAW_GRADELAST:
+            np.testing.assert_array_equal(got[0], levels[0])
+        else:
+            np.testing.assert_array_equal(got[1:], levels[1:])
+            np.testing.assert_array_equal(got[0], levels[1])
