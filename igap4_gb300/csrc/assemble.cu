@@ -187,19 +187,25 @@ __device__ __forceinline__ void element_body(typename ElemCfg<TAN>::Smem &S, Law
       }
     }
     if constexpr (ISO) {
+      // weighted derivatives of every basis function, once per point (the
+      // tangent-integrand buffer is free in this form)
+      for (int t = tid; t < PW * NB * 9; t += NT) {
+        const int w = t / (NB * 9), r = t % (NB * 9);
+        S.Dw[w][r] = S.Pt[w].wt * S.R[w][NDD * (r / 9) + 1 + r % 9];
+      }
+      __syncthreads();
       if (tid < NPAIR) {
         for (int w = 0; w < PW; w++) {
-          const double *rb = S.R[w] + NDD * pb, *rc = S.R[w] + NDD * pc;
-          const double wt = S.Pt[w].wt;
+          const double *sb = S.Dw[w] + 9 * pb, *rc = S.R[w] + NDD * pc;  // sb: weighted slots 1..9 of b
           double gb[3], gc[3], hb[3][3], hc[3][3];
 #pragma unroll
           for (int i = 0; i < 3; i++) {
-            gb[i] = wt * rb[1 + i];
+            gb[i] = sb[i];
             gc[i] = rc[1 + i];
           }
           // Hessian components (xx, xy, xz, yy, yz, zz) -> symmetric 3 x 3
-          hb[0][0] = wt * rb[4]; hb[0][1] = hb[1][0] = wt * rb[5]; hb[0][2] = hb[2][0] = wt * rb[6];
-          hb[1][1] = wt * rb[7]; hb[1][2] = hb[2][1] = wt * rb[8]; hb[2][2] = wt * rb[9];
+          hb[0][0] = sb[3]; hb[0][1] = hb[1][0] = sb[4]; hb[0][2] = hb[2][0] = sb[5];
+          hb[1][1] = sb[6]; hb[1][2] = hb[2][1] = sb[7]; hb[2][2] = sb[8];
           hc[0][0] = rc[4]; hc[0][1] = hc[1][0] = rc[5]; hc[0][2] = hc[2][0] = rc[6];
           hc[1][1] = rc[7]; hc[1][2] = hc[2][1] = rc[8]; hc[2][2] = rc[9];
 #pragma unroll
