@@ -43,9 +43,10 @@ SEED = 20261203
 TAN_FLOP_PER_ELEM = 2 * 64 * (30 * 27 * 3 * 10 + 81 * 81 * 10)  # 11,508,480
 RES_FLOP_PER_ELEM = 2 * 64 * (27 * 30 + 27 * 30)                 # 207,360
 # FLOPs the kernels execute for the linear law (Gram form of the tangent):
-# FP64 kernel: 378 basis pairs x 64 points x 81 (Gram sums) + 64 x 3,420
-# (state interpolation, law, projection) + block formation and scatter
-EXEC_FLOP_FP64_ELEM = 378 * 64 * 81 + 64 * 3420 + 30_000         # ~2.21 M
+# FP64 kernel: 378 basis pairs x 64 points x 72 (Gram sums) + 64 x 243
+# (weighted derivatives) + 64 x 3,420 (state interpolation, law, projection)
+# + block formation and scatter
+EXEC_FLOP_FP64_ELEM = 378 * 64 * 72 + 64 * 243 + 64 * 3420 + 30_000  # ~2.0 M
 # tensor-core kernel: 3 TF32 products of M128 x N96 x K256 per element
 EXEC_FLOP_TC_ELEM = 3 * 2 * 128 * 96 * 256                         # 18.9 M
 # DRAM traffic per launch of the FP64 element kernel at 128x32x32, from the

@@ -59,23 +59,70 @@ __device__ __forceinline__ bool tc_wait_ge(const int *p, int target)
 }  // namespace
 
 struct TcgSmem {
-  unsigned char A[2][2 * GA_PIECE];  // [buffer][hi, lo][K-step][4096 B]
-  unsigned char B[2][2 * GB_PIECE];  // [buffer][hi, lo][K-step][3072 B]
+  unsigned char A[2 * GA_PIECE];     // [hi, lo][K-step][4096 B]; the Gram matrix is staged here after the MMAs
+  unsigned char B[2 * GB_PIECE];     // [hi, lo][K-step][3072 B]
   float Rf[2][PW * PT_FLOATS];       // [buffer] 8 cached point rows
-  float G[GROWS * GPAD];             // staged Gram matrix
+  int pos[NB * NB];                  // stencil position of column point c in the row of point b
   int64_t rowp[NE];
-  uint64_t mbar_mma[2];
+  uint64_t mbar_mma;
   uint64_t mbar_cp[2];
   uint32_t taddr;
   int abort;
   int64_t base;
 };
+static_assert(GROWS * GPAD * 4 <= 2 * GA_PIECE, "the staged Gram matrix fits in the A buffer");
 
 // Barrier phase bookkeeping of one CTA (uniform across its threads).
 struct TcgState {
-  uint32_t mma_n[2];  // commits issued to mbar_mma[b]
+  uint32_t mma_n;     // commits issued to mbar_mma
   uint32_t cp_n[2];   // copies issued to mbar_cp[b]
 };
+
+// Operand tasks of one thread, fixed for the whole kernel: task j covers
+// 4 consecutive K slots of one row of A or B in one K-step.  dst: byte offset
+// in its operand (bit 31 set for B), 0xffffffff if the thread has no task j;
+// code: per slot the source float in the chunk's point rows (12 bits), the
+// point (3 bits), whether it is a Hessian slot (1 bit).
+constexpr int NTASK = (2 * GROWS * GKS * 2 + G_THREADS - 1) / G_THREADS;  // 6
+struct TcgTasks {
+  uint32_t dst[NTASK];
+  uint64_t code[NTASK];
+};
+
+__device__ __forceinline__ void tcg_make_tasks(TcgTasks &T)
+{
+#pragma unroll
+  for (int j = 0; j < NTASK; j++) {
+    const int t = threadIdx.x + j * G_THREADS;
+    if (t >= 2 * GROWS * GKS * 2) {
+      T.dst[j] = 0xffffffffu;
+      T.code[j] = 0;
+      continue;
+    }
+    const int mat = t / (GROWS * GKS * 2), u = t % (GROWS * GKS * 2);
+    const int r = u % GROWS, ks = (u / GROWS) % GKS, half = u / (GROWS * GKS);
+    const int bsf = r / 3, i = r % 3;
+    T.dst[j] = (uint32_t)(ks * (mat == 0 ? GA_TILE : GB_TILE)) + tc::kmajor_off(r, half * 4) |
+               (mat ? 0x80000000u : 0u);
+    uint64_t code = 0;
+    for (int jj = 0; jj < 4; jj++) {
+      const int k = ks * 8 + half * 4 + jj;
+      int p, idx, hess;
+      if (k < PW) {  // gradient part: one slot per point
+        p = k;
+        idx = 1 + i;
+        hess = 0;
+      } else {       // Hessian part: three slots per point
+        p = (k - PW) / 3;
+        idx = 4 + hess_slot(i, (k - PW) % 3);
+        hess = 1;
+      }
+      const uint64_t cj = (uint64_t)(p * PT_FLOATS + NDD * bsf + idx) | ((uint64_t)p << 12) | ((uint64_t)hess << 15);
+      code |= cj << (16 * jj);
+    }
+    T.code[j] = code;
+  }
+}
 
 __device__ __forceinline__ void tcg_issue_copy(TcgSmem &S, TcgState &st, const float *gsrc, int npts, int ch)
 {
@@ -92,9 +139,9 @@ __device__ __forceinline__ void tcg_issue_copy(TcgSmem &S, TcgState &st, const f
 
 // One element.  Returns false when a bounded wait expired (S.abort set).
 template <bool COH>
-__device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevMesh &m, const DevLaw &L, int ex,
-                                            int ey, int ez, double *__restrict__ vals, uint32_t taddr,
-                                            uint32_t a_base, uint32_t b_base)
+__device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const TcgTasks &T, const DevMesh &m,
+                                            const DevLaw &L, int ex, int ey, int ez, double *__restrict__ vals,
+                                            uint32_t taddr, uint32_t a_base, uint32_t b_base)
 {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
@@ -111,51 +158,45 @@ __device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevM
     const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
     S.rowp[tid] = __ldg(m.rowptr + 3 * cpb + dd);
   }
+  for (int t = tid; t < NB * NB; t += G_THREADS) {
+    const int b = t / NB, c = t % NB;
+    S.pos[t] = (int)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9, ey + (c / 3) % 3,
+                                ez + c % 3, nbv);
+  }
   for (int ch = 0; ch < nchunk; ch++) {
-    const int rb = ch & 1, ob = ch & 1;
+    const int rb = ch & 1;
     if (ch + 1 < nchunk) tcg_issue_copy(S, st, gsrc, npts, ch + 1);  // its buffer was last read by chunk ch-1
     bool ok = tc::mbar_wait(&S.mbar_cp[rb], (st.cp_n[rb] - 1) & 1, G_WAIT_LIMIT);
-    if (ok && st.mma_n[ob] > 0) ok = tc::mbar_wait(&S.mbar_mma[ob], (st.mma_n[ob] - 1) & 1, G_WAIT_LIMIT);
+    // the operands are single buffered: the previous MMAs must be done
+    if (ok && st.mma_n > 0) ok = tc::mbar_wait(&S.mbar_mma, (st.mma_n - 1) & 1, G_WAIT_LIMIT);
     if (!ok) S.abort = 1;
     __syncthreads();
     if (S.abort) return false;
-    // operands of this chunk: task = (matrix, row, K-step, half) -> 4 consecutive k
     const float *R = S.Rf[rb];
     const int q0 = ch * PW;
-    for (int t = tid; t < 2 * GROWS * GKS * 2; t += G_THREADS) {
-      const int mat = t / (GROWS * GKS * 2);  // 0: A, 1: B
-      const int u = t % (GROWS * GKS * 2);
-      const int r = u % GROWS, ks = (u / GROWS) % GKS, half = u / (GROWS * GKS);
-      const int bsf = r / 3, i = r % 3;
+#pragma unroll
+    for (int j = 0; j < NTASK; j++) {
+      const uint32_t dst = T.dst[j];
+      if (dst == 0xffffffffu) continue;
+      const bool isB = (dst >> 31) != 0;
       float4 hi, lo;
       float *ph = &hi.x, *pl = &lo.x;
 #pragma unroll
       for (int jj = 0; jj < 4; jj++) {
-        const int k = ks * 8 + half * 4 + jj;
-        int p, idx;
-        float scale;
-        if (k < PW) {  // gradient part: one slot per point
-          p = k;
-          idx = 1 + i;
-          scale = 1.f;
-        } else {       // Hessian part: three slots per point
-          p = (k - PW) / 3;
-          idx = 4 + hess_slot(i, (k - PW) % 3);
-          scale = l2;
-        }
-        const float *row = R + p * PT_FLOATS;
+        const uint32_t code = (uint32_t)(T.code[j] >> (16 * jj)) & 0xffffu;
+        const int src = (int)(code & 4095u), p = (int)((code >> 12) & 7u);
         float v = 0.f;
         if (q0 + p < npts) {
-          v = row[NDD * bsf + idx];
-          if (mat == 0) v *= scale * row[NB * NDD];  // A carries w_q (and ell^2)
+          v = R[src];
+          if (!isB) v *= ((code >> 15) ? l2 : 1.f) * R[p * PT_FLOATS + NB * NDD];  // A carries w_q (and ell^2)
         }
         const float h = tc::to_tf32(v);
         ph[jj] = h;
         pl[jj] = tc::to_tf32(v - h);
       }
-      unsigned char *base = mat == 0 ? S.A[ob] : S.B[ob];
-      const int piece = mat == 0 ? GA_PIECE : GB_PIECE;
-      const uint32_t off = (uint32_t)(ks * (mat == 0 ? GA_TILE : GB_TILE)) + tc::kmajor_off(r, half * 4);
+      unsigned char *base = isB ? S.B : S.A;
+      const int piece = isB ? GB_PIECE : GA_PIECE;
+      const uint32_t off = dst & 0x7fffffffu;
       *reinterpret_cast<float4 *>(base + off) = hi;
       *reinterpret_cast<float4 *>(base + piece + off) = lo;
     }
@@ -164,26 +205,23 @@ __device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevM
     __syncthreads();
     if (tid == 0) {
       tc::fence_after_sync();
-      const uint32_t ab = a_base + (uint32_t)(ob * 2 * GA_PIECE), bb = b_base + (uint32_t)(ob * 2 * GB_PIECE);
       for (int ks = 0; ks < GKS; ks++)
         for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
           const int pa = (pp == 2) ? 1 : 0, pb = (pp == 1) ? 1 : 0;
-          const uint64_t ad = tc::smem_desc(ab + (uint32_t)(pa * GA_PIECE + ks * GA_TILE), 128, 256);
-          const uint64_t bd = tc::smem_desc(bb + (uint32_t)(pb * GB_PIECE + ks * GB_TILE), 128, 256);
+          const uint64_t ad = tc::smem_desc(a_base + (uint32_t)(pa * GA_PIECE + ks * GA_TILE), 128, 256);
+          const uint64_t bd = tc::smem_desc(b_base + (uint32_t)(pb * GB_PIECE + ks * GB_TILE), 128, 256);
           tc::mma_tf32(taddr, ad, bd, idesc, (ch == 0 && ks == 0 && pp == 0) ? 0u : 1u);
         }
-      tc::mma_commit(&S.mbar_mma[ob]);
+      tc::mma_commit(&S.mbar_mma);
     }
-    st.mma_n[ob]++;
+    st.mma_n++;
   }
   // epilogue: the last commit covers every MMA of the element
-  {
-    const int lb = (nchunk - 1) & 1;
-    if (!tc::mbar_wait(&S.mbar_mma[lb], (st.mma_n[lb] - 1) & 1, G_WAIT_LIMIT)) S.abort = 1;
-  }
+  if (!tc::mbar_wait(&S.mbar_mma, (st.mma_n - 1) & 1, G_WAIT_LIMIT)) S.abort = 1;
   tc::fence_after_sync();
   __syncthreads();
   if (S.abort) return false;
+  float *G = reinterpret_cast<float *>(S.A);  // operands are no longer read
   {
     // warp w reads TMEM lane quarter (w % 4), columns [32 (w / 4), +32) and, for
     // w < 4, also [64, 96)
@@ -195,7 +233,7 @@ __device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevM
       if (r < GROWS)
 #pragma unroll
         for (int j = 0; j < 32; j++)
-          if (cb * 32 + j < GROWS) S.G[r * GPAD + cb * 32 + j] = __uint_as_float(v[j]);
+          if (cb * 32 + j < GROWS) G[r * GPAD + cb * 32 + j] = __uint_as_float(v[j]);
     }
   }
   tc::fence_before_sync();
@@ -210,18 +248,16 @@ __device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const DevM
 #pragma unroll
       for (int s = 0; s < 9; s++) {
         const int t = t0 + s * G_THREADS;
-        slot[s] = -1;
+        slot[s] = 0;
         kv[s] = 0.f;
         if (t < NE * NE) {
-          const int rr = t / NE, cc = t % NE;
-          const int b = rr / 3, d = rr % 3, c = cc / 3, e = cc % 3;
-          float kk = lam * S.G[(3 * b + d) * GPAD + 3 * c + e] + mu * S.G[(3 * b + e) * GPAD + 3 * c + d];
+          const int rr = t / NE, cc = t - NE * rr;
+          const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
+          float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
           if (d == e)
-            kk += mu * (S.G[(3 * b) * GPAD + 3 * c] + S.G[(3 * b + 1) * GPAD + 3 * c + 1] +
-                        S.G[(3 * b + 2) * GPAD + 3 * c + 2]);
-          const int rx = ex + b / 9, ry = ey + (b / 3) % 3, rz = ez + b % 3;
-          const int sx = ex + c / 9, sy = ey + (c / 3) % 3, sz = ez + c % 3;
-          slot[s] = S.rowp[rr] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
+            kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] +
+                        G[(3 * b + 2) * GPAD + 3 * c + 2]);
+          slot[s] = S.rowp[rr] + 3 * S.pos[NB * b + c] + e;
           kv[s] = kk;
           cnt = s + 1;
         }
@@ -246,13 +282,12 @@ __device__ __forceinline__ void tcg_setup(TcgSmem &S)
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
-      tc::mbar_init(&S.mbar_mma[b], 1);
-      tc::mbar_init(&S.mbar_cp[b], 1);
-    }
+    tc::mbar_init(&S.mbar_mma, 1);
+    for (int b = 0; b < 2; b++) tc::mbar_init(&S.mbar_cp[b], 1);
     S.abort = 0;
   }
-  // padding rows 81..127 of A and 81..95 of B stay zero for the whole kernel
+  // padding rows 81..95 of B stay zero for the whole kernel; rows 81..127 of A
+  // only feed accumulator rows that are never read
   for (int i = tid; i < (int)(sizeof(S.A) / 4); i += G_THREADS) reinterpret_cast<float *>(S.A)[i] = 0.f;
   for (int i = tid; i < (int)(sizeof(S.B) / 4); i += G_THREADS) reinterpret_cast<float *>(S.B)[i] = 0.f;
   tc::fence_before_sync();
@@ -269,13 +304,14 @@ __device__ __forceinline__ void tcg_teardown(TcgSmem &S, const TcgState &st, int
   if (S.abort) {
     for (int b = 0; b < 2; b++)
       if (st.cp_n[b] > 0) tc::mbar_wait(&S.mbar_cp[b], (st.cp_n[b] - 1) & 1, G_WAIT_LIMIT);
+    if (st.mma_n > 0) tc::mbar_wait(&S.mbar_mma, (st.mma_n - 1) & 1, G_WAIT_LIMIT);
     if (threadIdx.x == 0) atomicCAS(err, 0, 2);
   }
   __syncthreads();
   if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(S.taddr, G_TMEM_COLS);
 }
 
-__global__ void __launch_bounds__(G_THREADS, 1)
+__global__ void __launch_bounds__(G_THREADS, 2)
     tcg_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
                int *err)
 {
@@ -283,11 +319,13 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   TcgSmem &S = *reinterpret_cast<TcgSmem *>(smem_raw);
   tcg_setup(S);
   const uint32_t taddr = S.taddr, a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
-  TcgState st = {{0, 0}, {0, 0}};
+  TcgState st = {0, {0, 0}};
+  TcgTasks T;
+  tcg_make_tasks(T);
   const int nelem_c = ncx * ncy * ncz;
   for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
     const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
-    if (!tcg_element<false>(S, st, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, vals, taddr, a_base, b_base))
+    if (!tcg_element<false>(S, st, T, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, vals, taddr, a_base, b_base))
       break;
     tc::fence_before_sync();
     __syncthreads();
@@ -296,14 +334,16 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 }
 
 // Batched: elements from the colour-major queue (see element_batch_kernel).
-__global__ void __launch_bounds__(G_THREADS, 1) tcg_batch_kernel(BatchArgs ba, double *__restrict__ vals)
+__global__ void __launch_bounds__(G_THREADS, 2) tcg_batch_kernel(BatchArgs ba, double *__restrict__ vals)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TcgSmem &S = *reinterpret_cast<TcgSmem *>(smem_raw);
   const int tid = threadIdx.x;
   tcg_setup(S);
   const uint32_t taddr = S.taddr, a_base = tc::smem_u32(S.A), b_base = tc::smem_u32(S.B);
-  TcgState st = {{0, 0}, {0, 0}};
+  TcgState st = {0, {0, 0}};
+  TcgTasks T;
+  tcg_make_tasks(T);
   int cur = -1;
   DevMesh m;
   DevLaw L;
@@ -336,7 +376,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) tcg_batch_kernel(BatchArgs ba, d
         ok = false;
         break;
       }
-      ok = tcg_element<true>(S, st, m, L, w.ex, w.eyz >> 16, w.eyz & 0xffff, vals, taddr, a_base, b_base);
+      ok = tcg_element<true>(S, st, T, m, L, w.ex, w.eyz >> 16, w.eyz & 0xffff, vals, taddr, a_base, b_base);
       if (!ok) break;
       tc::fence_before_sync();
       __syncthreads();
@@ -377,7 +417,7 @@ int launch_tc_gram(Context *c, double *vals)
                   ncz = (c->nelem[2] - cz + 2) / 3;
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
-        const int grid = nel < nsm ? nel : nsm;
+        const int grid = nel < 2 * nsm ? nel : 2 * nsm;  // two CTAs per SM
         tcg_kernel<<<grid, G_THREADS, tcg_smem(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
         count_launch();
         IGAP_CHECK_LAUNCH();
