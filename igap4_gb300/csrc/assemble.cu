@@ -180,9 +180,10 @@ __device__ __forceinline__ void element_body(typename ElemCfg<TAN>::Smem &S, Law
     __syncthreads();
     if (RES && tid < NE) {
       const int bb = tid / 3, d = tid % 3;
+      constexpr int K0 = LAWK == 0 ? 1 : 0;  // the linear law's value slot of rr is zero
       for (int w = 0; w < PW; w++) {
         double s = 0.0;
-        for (int k = 0; k < NDD; k++) s += S.R[w][NDD * bb + k] * S.rr[w][NDD * d + k];
+        for (int k = K0; k < NDD; k++) s += S.R[w][NDD * bb + k] * S.rr[w][NDD * d + k];
         racc += s;
       }
     }

@@ -224,7 +224,11 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
   // (g) interpolated state of every history level, src/assmcore_iga.c:209-229
   const int nh = L.nhist;
   constexpr bool NEED_U = RES || LAWK != 0;
-  if (NEED_U && lane < 30) {
+  // the linear law's tangent has no value column: its value slots (k = 0) are
+  // set to zero instead of interpolated
+  if (LAWK == 0 && NEED_U && lane < 30 && lane % NDD == 0)
+    for (int h = 0; h < L.nhist; h++) P.u[30 * h + lane] = 0.0;
+  if (NEED_U && lane < 30 && (LAWK != 0 || lane % NDD != 0)) {
     const int d = lane / NDD, k = lane % NDD;
     for (int h = 0; h < nh; h++) {
       double s = 0.0;
