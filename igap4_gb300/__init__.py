@@ -108,6 +108,7 @@ def lib():
         L.igapgpu_profile_read_kind.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.igapgpu_measure_fp64_peak.argtypes = [vp]
         L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
+        L.igapgpu_wait_selftest.argtypes = [ctypes.c_int, ctypes.c_uint, vp]
         L.igapgpu_batch_init.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(MeshDesc),
                                          ctypes.POINTER(PhysDesc), ctypes.POINTER(BCDesc), ctypes.c_int]
         L.igapgpu_batch_info.argtypes = [vp, vp, vp, vp]
@@ -495,3 +496,11 @@ def batch_instances(n=256, seed=0, nx=(8, 64), nyz=(2, 16), lam=(0.5, 2.0), mu=(
         par = [rng.uniform(*lam), rng.uniform(*mu), rng.uniform(*ell), 0, 0, 0, 0, 0, 0]
         out.append(dict(nelem=nelem, knots=knots, w=w, X=X, par=par, bc_type=bct, neumann=neu))
     return out
+
+
+def wait_selftest(target, limit=1 << 16):
+    """Bounded device wait on a counter that nothing increments (target 1) or
+    that is already reached (target 0); returns the device error word."""
+    st = ctypes.c_int(-1)
+    _check(lib().igapgpu_wait_selftest(int(target), int(limit), ctypes.byref(st)))
+    return st.value

@@ -336,15 +336,27 @@ __device__ __forceinline__ void release_add(int *p, int v)
 }
 
 // Waits (bounded) until *p >= target; acquire at GPU scope.
-__device__ __forceinline__ bool wait_count_ge(const int *p, int target)
+__device__ __forceinline__ bool wait_count_ge(const int *p, int target, uint32_t limit = BATCH_WAIT_LIMIT)
 {
-  for (uint32_t i = 0; i < BATCH_WAIT_LIMIT; i++) {
+  for (uint32_t i = 0; i < limit; i++) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     if (v >= target) return true;
     __nanosleep(128);
   }
   return false;
+}
+
+// Self-test of the expiry path of the bounded waits: thread 0 of every CTA
+// waits for a counter that nothing increments, with a short poll limit, and
+// the CTA reports the outcome in the error-word convention of the batched
+// kernels (3 = a wait expired).  No fault and no hang: the kernel returns.
+__global__ void wait_selftest_kernel(const int *counter, int target, uint32_t limit, int *err)
+{
+  __shared__ int expired;
+  if (threadIdx.x == 0) expired = wait_count_ge(counter, target, limit) ? 0 : 1;
+  __syncthreads();
+  if (threadIdx.x == 0 && expired) atomicExch(err, 3);
 }
 
 // Persistent CTAs take elements of every instance from one colour-major
@@ -1003,5 +1015,32 @@ extern "C" int igapgpu_measure_fp64_peak(double *tflops)
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(d);
+  return IGAPGPU_OK;
+}
+
+// Runs wait_selftest_kernel on a zeroed counter: target 0 (satisfied at once)
+// or 1 (never reached, the wait expires after `limit` polls).  *status gets the
+// device error word: 0, or 3 for an expired wait.
+extern "C" int igapgpu_wait_selftest(int target, unsigned int limit, int *status)
+{
+  using namespace igap;
+  if (!status || target < 0 || target > 1 || limit > (1u << 24)) {
+    set_error("wait self-test: target must be 0 or 1, limit at most 2^24 polls");
+    return IGAPGPU_ERR_ARG;
+  }
+  int *d = nullptr;
+  IGAP_CUDA(cudaMalloc(&d, 2 * sizeof(int)));
+  cudaError_t e = cudaMemset(d, 0, 2 * sizeof(int));
+  if (e == cudaSuccess) {
+    wait_selftest_kernel<<<2, 64>>>(d, target, limit, d + 1);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(status, d + 1, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error("wait self-test: %s", cudaGetErrorString(e));
+    return IGAPGPU_ERR_CUDA;
+  }
   return IGAPGPU_OK;
 }

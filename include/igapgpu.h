@@ -229,6 +229,13 @@ int igapgpu_tc_selftest(int variant, float *out);
 /* Measured FP64 FMA throughput of this GPU (TFLOP/s) from a register-only
  * kernel; used as the denominator of FP64-bound roofline fractions. */
 int igapgpu_measure_fp64_peak(double *tflops);
+/* Failure-detection self-test (no counterpart in the reference): a kernel
+ * waits, with the bounded acquire-poll loop of the batched kernels, for a
+ * zeroed counter to reach `target` (0: at once; 1: never, so the wait expires
+ * after `limit` <= 2^24 polls).  *status receives the device error word: 0, or
+ * 3 when the wait expired.  The kernel always returns; the context stays
+ * usable. */
+int igapgpu_wait_selftest(int target, unsigned int limit, int *status);
 
 
 /* ---------------------------------------------------------------------

@@ -178,3 +178,16 @@ def test_batch_spmv_matches_single_instances():
         a, e = B.dof_off[i], B.dof_off[i + 1]
         A.tangent_internal(np.ascontiguousarray(U[a:e]))
         np.testing.assert_array_equal(y[a:e], A.matmult(np.ascontiguousarray(x[a:e])))
+
+
+def test_bounded_wait_expires_and_context_survives():
+    """Failure detection without a fault: a device wait on a counter that
+    nothing increments gives up after its poll limit and reports error word 3;
+    a wait that is satisfied reports 0; a batch assembles correctly afterwards."""
+    assert ig.wait_selftest(1, 1 << 14) == 3
+    assert ig.wait_selftest(0, 1 << 14) == 0
+    law = ig.LAW_LINGRAD
+    insts = instances(law, seed=17, sizes=SIZES[:3])
+    B = ig.BatchAssembly(insts, law=law)
+    As = singles(insts, law, ig.PREC_FP64)
+    compare_to_singles(B, As, batch_state(B, 18))
