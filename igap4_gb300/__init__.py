@@ -81,6 +81,7 @@ def lib():
         L.igapgpu_pattern.argtypes = [vp, vp, vp]
         L.igapgpu_dirichlet.argtypes = [vp, vp, vp, vp]
         L.igapgpu_density.argtypes = [vp, vp, vp]
+        L.igapgpu_sample_field.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
         L.igapgpu_save_solution.argtypes = [vp, ctypes.c_char_p]
         L.igapgpu_load_solution.argtypes = [vp, ctypes.c_char_p]
         L.igapgpu_impose_dirichlet.argtypes = [vp, vp]
@@ -265,6 +266,21 @@ class Assembly:
         n = ctypes.c_int()
         _check(lib().igapgpu_density(self.h, _ptr(HH), ctypes.byref(n)))
         return HH[:n.value].copy()
+
+    def sample_field(self, nppe):
+        """The law's field on the plot lattice of iga_plotfield (nppe samples
+        per element and direction plus the far faces) at the current state:
+        field [NX, NY, NZ, nfield], knot coordinates xq and positions X
+        [NX, NY, NZ, 3], NX = nppe * nelem[0] + 1."""
+        nf = ctypes.c_int()
+        npts = ctypes.c_int64()
+        _check(lib().igapgpu_sample_field(self.h, int(nppe), None, None, None, ctypes.byref(nf), ctypes.byref(npts)))
+        shape = tuple(int(nppe) * int(n) + 1 for n in self.nelem)
+        F = np.zeros(shape + (nf.value,))
+        xq = np.zeros(shape + (3,))
+        X = np.zeros(shape + (3,))
+        _check(lib().igapgpu_sample_field(self.h, int(nppe), _ptr(F), _ptr(xq), _ptr(X), None, None))
+        return F, xq, X
 
     def save_solution(self, fname):
         """Write the reference's solution file (IGAPSolvSaveSolution layout)."""

@@ -42,31 +42,7 @@ __global__ void basis_table_kernel(const double *knots, int nelem, const double 
   double x0 = kv[P], x1 = kv[P + 1];
   double c = xq01[iq];
   double x = (-c + 1.0) * x0 + c * x1;
-  const double mt = with_mtol ? MTOL : 0.0;
-  double lev[P + 1][2 * P + 1], dlev[P + 1][2 * P + 1];
-  for (int i = 0; i < 2 * P + 1; i++) { lev[0][i] = 0.0; dlev[0][i] = 0.0; }
-  lev[0][P] = 1.0;
-  for (int q = 1; q <= P; q++)
-    for (int i = 0; i < 2 * P + 1 - q; i++) {
-      double dl = kv[i + q] - kv[i] + mt, dr = kv[i + q + 1] - kv[i + 1] + mt;
-      double a = (dl != 0.0) ? (x - kv[i]) / dl * lev[q - 1][i] : 0.0;
-      double b = (dr != 0.0) ? (kv[i + q + 1] - x) / dr * lev[q - 1][i + 1] : 0.0;
-      lev[q][i] = a + b;
-      double da = (dl != 0.0) ? (double)q / dl * lev[q - 1][i] : 0.0;
-      double db = (dr != 0.0) ? (double)q / dr * lev[q - 1][i + 1] : 0.0;
-      dlev[q][i] = da - db;
-    }
-  double *o = tab + (size_t)t * TAB;
-  for (int i = 0; i <= P; i++) {
-    o[i] = lev[P][i];
-    o[P1 + i] = dlev[P][i];
-    double dl = kv[i + P] - kv[i] + mt, dr = kv[i + P + 1] - kv[i + 1] + mt;
-    double a = (dl != 0.0) ? (double)P / dl * dlev[P - 1][i] : 0.0;
-    double b = (dr != 0.0) ? (double)P / dr * dlev[P - 1][i + 1] : 0.0;
-    o[2 * P1 + i] = a - b;
-  }
-  o[3 * P1] = x;
-  o[3 * P1 + 1] = x1 - x0;
+  basis_1d(kv, x, with_mtol ? MTOL : 0.0, tab + (size_t)t * TAB);
 }
 
 // ------------------------------------------------------------ pattern

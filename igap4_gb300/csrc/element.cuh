@@ -41,6 +41,38 @@ struct LawSmem<2> {
   LawScratch<4> s[PW];
 };
 
+// One entry of a 1-D basis table at knot coordinate x of the span whose
+// local knots are kv[0..2P+1] (Cox-de Boor with derivatives, every knot-span
+// denominator shifted by mt; the 1-D factor of eval_Bspline,
+// src/meshcore_iga.c:243-310): o[0..2] N, o[3..5] dN, o[6..8] ddN of the
+// span's three functions, o[9] = x, o[10] = the span length.
+__device__ inline void basis_1d(const double *kv, double x, double mt, double *o)
+{
+  double lev[P + 1][2 * P + 1], dlev[P + 1][2 * P + 1];
+  for (int i = 0; i < 2 * P + 1; i++) { lev[0][i] = 0.0; dlev[0][i] = 0.0; }
+  lev[0][P] = 1.0;
+  for (int q = 1; q <= P; q++)
+    for (int i = 0; i < 2 * P + 1 - q; i++) {
+      double dl = kv[i + q] - kv[i] + mt, dr = kv[i + q + 1] - kv[i + 1] + mt;
+      double a = (dl != 0.0) ? (x - kv[i]) / dl * lev[q - 1][i] : 0.0;
+      double b = (dr != 0.0) ? (kv[i + q + 1] - x) / dr * lev[q - 1][i + 1] : 0.0;
+      lev[q][i] = a + b;
+      double da = (dl != 0.0) ? (double)q / dl * lev[q - 1][i] : 0.0;
+      double db = (dr != 0.0) ? (double)q / dr * lev[q - 1][i + 1] : 0.0;
+      dlev[q][i] = da - db;
+    }
+  for (int i = 0; i <= P; i++) {
+    o[i] = lev[P][i];
+    o[P1 + i] = dlev[P][i];
+    double dl = kv[i + P] - kv[i] + mt, dr = kv[i + P + 1] - kv[i + 1] + mt;
+    double a = (dl != 0.0) ? (double)P / dl * dlev[P - 1][i] : 0.0;
+    double b = (dr != 0.0) ? (double)P / dr * dlev[P - 1][i + 1] : 0.0;
+    o[2 * P1 + i] = a - b;
+  }
+  o[3 * P1] = x;
+  o[3 * P1 + 1] = kv[P + 1] - kv[P];
+}
+
 __device__ __forceinline__ void load_element(ElemData &E, const DevMesh &m, int nh,
                                              const double *__restrict__ Uhist, int ex, int ey,
                                              int ez, int tid, int nthreads)

@@ -130,6 +130,20 @@ int igapgpu_impose_dirichlet(igapgpu_t ctx, double *U);
  * incl. kinetic, volume), the linear law 2 (energy, volume). */
 int igapgpu_density(igapgpu_t ctx, double *HH, int *ndensity);
 
+/* Field sampling of iga_plotfield (src/mgl/plotcore_iga.c:16-282) into a
+ * headless buffer instead of a MathGL frame: the law's field callback
+ * (include/physimpl.h:8) on the current U_hist at a lattice of nppe samples
+ * per element and direction plus the far faces, (nppe nelem[d] + 1) points
+ * per direction, x-major, z fastest.  field [npoints][nfield]: the static
+ * gradient law 33 (u[0..29], e1, e2, sector code: phys/gradelast.c:1105), the
+ * transient law 6 (midpoint displacement, e1, e2, sector code:
+ * phys/gradelasttime.c:9242), the linear law 33 (u[0..29], tr eps, |dev eps|,
+ * psi).  xq [npoints][3]: the knot coordinates the reference plots against;
+ * X [npoints][3]: physical positions.  Outputs may be NULL, host or device;
+ * with all three NULL only *nfield and *npoints are set.  1 <= nppe <= 64. */
+int igapgpu_sample_field(igapgpu_t ctx, int nppe, double *field, double *xq, double *X, int *nfield,
+                         int64_t *npoints);
+
 /* IGAPSolvSaveSolution / IGAPSolvLoadSolution (src/interface.c:271-300): the
  * reference's solution file (write_solution / read_solution, src/ioutil.c:
  * 90-159), raw FP64 levels in DOF order; static laws level 0, the transient

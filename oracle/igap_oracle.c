@@ -678,3 +678,33 @@ void orc_case_tangent(const OracleCase *c, const double *U_hist, double *vals)
       if (flag[r] || flag[c->cols[s]]) vals[s] = (flag[r] && c->cols[s] == r) ? 1.0 : 0.0;
   free(flag);
 }
+
+/* ------------------------------------------------------- field sampling -- */
+/* iga_plotfield's sampling loop (src/mgl/plotcore_iga.c:16-282, restated in
+ * field_sampling.h) with this file's basis and inverse and the restated
+ * field callbacks of laws.c. */
+#include "field_sampling.h"
+
+int orc_law_field(int law, double *f, const double *u, const double *par);
+static void fs_orc_basis(double *N, double *kv[3], int p, double xq[3])
+{
+  const double *k[3] = {kv[0], kv[1], kv[2]};
+  orc_eval_bspline(N, k, p, xq);
+}
+static void fs_field_gradelast(double *f, double *u, double *par) { orc_law_field(ORC_LAW_GRADELAST, f, u, par); }
+static void fs_field_gradelasttime(double *f, double *u, double *par)
+{
+  orc_law_field(ORC_LAW_GRADELASTTIME, f, u, par);
+}
+static void fs_field_lingrad(double *f, double *u, double *par) { orc_law_field(ORC_LAW_LINGRAD, f, u, par); }
+
+int orc_case_field(OracleCase *c, const double *U_hist, int nppe, double *field, double *xq, double *X)
+{
+  const int nf = c->law == ORC_LAW_GRADELASTTIME ? 6 : 33;
+  fs_field_fn fn = c->law == ORC_LAW_GRADELAST       ? fs_field_gradelast
+                   : c->law == ORC_LAW_GRADELASTTIME ? fs_field_gradelasttime
+                                                     : fs_field_lingrad;
+  fs_sample(c->p, c->nelem, c->knots, c->w, c->X, U_hist, c->ndof, c->torder + 1, c->par, nf, nppe, fs_orc_basis,
+            inv3, fn, field, xq, X);
+  return nf;
+}

@@ -64,6 +64,13 @@ void orc_case_tangent_elements(const OracleCase *c, const double *U_hist, double
 void orc_case_residual_elements(const OracleCase *c, const double *U_hist, double *RR, long e0,
                                 long e1);
 
+/* The law's field on the plot lattice of iga_plotfield (restates
+ * src/mgl/plotcore_iga.c:16-282 without MathGL; oracle/field_sampling.h):
+ * field [npoints][nfield], xq / X [npoints][3]; returns nfield. */
+int orc_case_field(OracleCase *c, const double *U_hist, int nppe, double *field, double *xq, double *X);
+/* Field callback of a law (33 values, 6 for gradelasttime); returns the count. */
+int orc_law_field(int law, double *f, const double *u, const double *par);
+
 /* Laws (per point): residual rr[30], tangent tt[900] of u[(torder+1)*30]. */
 void orc_law_residual(int law, double *rr, const double *u, const double *par);
 void orc_law_tangent(int law, double *tt, const double *u, const double *par);

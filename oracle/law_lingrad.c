@@ -17,6 +17,7 @@
  * Test infrastructure (oracle): the device law in the product is written
  * independently and checked against this file.
  */
+#include <math.h>
 #include <string.h>
 
 static const int SYM_J[6] = {0, 0, 0, 1, 1, 2};
@@ -112,4 +113,27 @@ void lingrad_densityb(double h[], double u[], double traction, double *par, int 
   (void)order;
   h[0] = u[0] * traction;
   h[1] = 0.0;
+}
+
+/* Field callback of the linear law (field_ptr, include/physimpl.h:8), 33
+ * values in the static gradient law's layout: f[0..29] = u, f[30] = tr eps,
+ * f[31] = |dev eps|, f[32] = psi. */
+void lingrad_field(double *f, double *u, double *par)
+{
+  for (int i = 0; i < 30; i++) f[i] = u[i];
+  double eps[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) eps[i][j] = 0.5 * (u[10 * i + 1 + j] + u[10 * j + 1 + i]);
+  const double tr = eps[0][0] + eps[1][1] + eps[2][2];
+  double dd = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      const double v = eps[i][j] - (i == j ? tr / 3.0 : 0.0);
+      dd += v * v;
+    }
+  double h[2];
+  lingrad_density(h, u, par);
+  f[30] = tr;
+  f[31] = sqrt(dd);
+  f[32] = h[0];
 }

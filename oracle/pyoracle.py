@@ -62,6 +62,7 @@ def orc():
         _orc.orc_evalN.argtypes = [_D, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_double]
         _orc.orc_gauss_legendre.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D]
+        _orc.orc_case_field.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
     return _orc
 
 
@@ -86,6 +87,7 @@ def ref():
             getattr(_ref, f).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _ref.ref_case_tangent_csr.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
         _ref.ref_case_density.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        _ref.ref_case_field.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
         _ref.ref_case_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         _ref.ref_case_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         _ref.ref_case_mesh_info.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 3
@@ -219,6 +221,17 @@ class OracleCase:
         orc().orc_case_tangent_elements(self.h, U.ctypes.data, vals.ctypes.data, e0, e1)
         return vals
 
+    def field(self, U_hist, nppe):
+        """Field on the plot lattice: (field [NX,NY,NZ,nfield], xq, X [NX,NY,NZ,3])."""
+        U = np.ascontiguousarray(U_hist, np.float64)
+        shape = field_lattice(self.prob, nppe)
+        nf = 6 if self.prob.law == LAW_GRADELASTTIME else 33
+        F = np.zeros(shape + (nf,))
+        xq = np.zeros(shape + (3,))
+        X = np.zeros(shape + (3,))
+        orc().orc_case_field(self.h, U.ctypes.data, int(nppe), F.ctypes.data, xq.ctypes.data, X.ctypes.data)
+        return F, xq, X
+
     def residual_elements(self, U_hist, e0, e1):
         U = np.ascontiguousarray(U_hist, np.float64)
         RR = np.zeros(self.ndof)
@@ -271,6 +284,19 @@ class RefCase:
         n = ref().ref_case_density(self.h, HH.ctypes.data)
         return HH[:n].copy()
 
+    def field(self, U_hist, nppe):
+        """The reference's basis, inverse and field callback on the plot
+        lattice (restated loop): (field, xq, X) as OracleCase.field."""
+        self.set_state(U_hist)
+        shape = field_lattice(self.prob, nppe)
+        nf = 6 if self.prob.law == LAW_GRADELASTTIME else 33
+        F = np.zeros(shape + (nf,))
+        xq = np.zeros(shape + (3,))
+        X = np.zeros(shape + (3,))
+        got = ref().ref_case_field(self.h, int(nppe), F.ctypes.data, xq.ctypes.data, X.ctypes.data)
+        assert got == nf
+        return F, xq, X
+
     def tangent(self, U_hist):
         self.set_state(U_hist)
         nnz = ref().ref_case_tangent(self.h)
@@ -298,6 +324,12 @@ class RefCase:
         X = np.zeros(3 * ncp)
         ref().ref_case_mesh_arrays(self.h, knots.ctypes.data, w.ctypes.data, X.ctypes.data)
         return nelem, nknot, nbasis, knots, w, X
+
+
+def field_lattice(prob: Problem, nppe: int):
+    """Plot lattice of iga_plotfield: nppe samples per element and direction
+    plus the far faces."""
+    return tuple(int(nppe) * int(n) + 1 for n in prob.nelem)
 
 
 def law_eval(which, law, u, par):

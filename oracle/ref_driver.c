@@ -112,14 +112,14 @@ static Mesh mesh_beam_dir(const int nelem[3], const double L[3], int porder, con
 /* ---- project linear law plugin, same struct as PhysGradElast ---------- */
 void lingrad_density(double h[], double u[], double *par);
 void lingrad_densityb(double h[], double u[], double t, double *par, int o);
-static void lingrad_field(double *f, double *u, double *par) { (void)f; (void)u; (void)par; }
+void lingrad_field(double *f, double *u, double *par);
 static void lingrad_assert(double *par) { (void)par; }
 
 static Phys phys_lingrad(const double *par)
 {
   Phys phys = (Phys)malloc(sizeof(struct __Phys));
   phys->ndim = 3; phys->ndof = 3; phys->torder = 0; phys->sorder = 2;
-  phys->ndensity = 2; phys->nfield = 0;
+  phys->ndensity = 2; phys->nfield = 33;
   phys->par_mat = (double *)calloc(9, sizeof(double));
   double def[3] = {1.0, 1.0, 0.1}; /* lambda, mu, ell */
   for (int i = 0; i < 3; i++) phys->par_mat[i] = par ? par[i] : def[i];
@@ -209,6 +209,33 @@ void ref_case_load(void *h, const char *fname)
     read_solution(fname, U, c->igap->iocomm, 1, c->torder + 1);
     for (int i = 0; i < n; i++) U[i] = U[n + i];
   }
+}
+
+/* Field sampling: the reference's basis (eval_Bspline, src/meshcore_iga.c:
+ * 243-327), 3 x 3 inverse (matinv, src/mathutil.c:17-41) and the law's field
+ * callback (phys->field) driven by the restated plot loop of
+ * oracle/field_sampling.h (the reference's own plotcore_iga.c does not
+ * compile), on the ghosted local state of plotcore_iga.c:62-80. */
+#include "field_sampling.h"
+void matinv(double *mat, int n);
+static void fs_ref_basis(double *N, double *kv[3], int p, double xq[3]) { eval_Bspline(N, kv, p, xq); }
+static void fs_ref_inverse(double *G) { matinv(G, 3); }
+
+int ref_case_field(void *h, int nppe, double *field, double *xq, double *X)
+{
+  RefCase *c = (RefCase *)h;
+  Core core = c->igap->core;
+  Mesh m = core->mesh[0];
+  Phys ph = core->phys[0];
+  Comm cm = core->comm[0];
+  const int nself = cm->nselfIdx, nloc = cm->nselfIdx + cm->nrecvIdx, nlev = ph->torder + 1;
+  double *U = (double *)calloc((size_t)nlev * nloc, sizeof(double));
+  for (int l = 0; l < nlev; l++)
+    for (int i = 0; i < nself; i++) U[(size_t)l * nloc + cm->selfIdx[i]] = core->U_hist[(size_t)l * nself + i];
+  fs_sample(m->porder, m->nelem, m->knotVector, m->wVector, m->XVector, U, nloc, nlev, ph->par_mat, ph->nfield, nppe,
+            fs_ref_basis, fs_ref_inverse, ph->field, field, xq, X);
+  free(U);
+  return ph->nfield;
 }
 
 int ref_case_ndof(void *h) { return ((RefCase *)h)->ndof_total; }

@@ -2,8 +2,11 @@
 
 The reference sources are compiled unchanged (oracle/build_ref.sh) into
 oracle/_ref/libigapref.so and driven through its public set-up
-(IGAPAssmInit), its SNES callbacks (Residual_iga / Tangent_iga) and its
-density integral (iga_intdensity, stored as HH).  The
+(IGAPAssmInit), its SNES callbacks (Residual_iga / Tangent_iga), its
+density integral (iga_intdensity, stored as HH) and, for the small cases, the
+field callbacks on the plot lattice of iga_plotfield (the reference's basis,
+inverse and field callback in a restated loop, since plotcore_iga.c does not
+compile; stored as field / field_xq / field_X at FIELD_SCALE x the state).  The
 fixtures are what the reference outputs for seeded inputs, so tests on a
 machine without the reference tree still compare against the reference.
 
@@ -40,6 +43,8 @@ SUMMARY_CASES = {
     "g_lingrad_8x2x2": dict(nelem=(8, 2, 2), law=po.LAW_LINGRAD, seed=22),
 }
 NSAMPLE = 4096
+FIELD_NPPE = 2
+FIELD_SCALE = 10.0  # large enough strains to reach every sector code
 
 
 def main():
@@ -58,6 +63,8 @@ def main():
                     bc_type=prob.bc_type, neumann=prob.neumann, U=U, RR=RR, HH=case.density(U))
         if name in FULL_CASES:
             meta.update(rowptr=rowptr, cols=cols, vals=vals)
+            F, xq, X = case.field(FIELD_SCALE * U, FIELD_NPPE)
+            meta.update(field_nppe=FIELD_NPPE, field_scale=FIELD_SCALE, field=F, field_xq=xq, field_X=X)
         else:
             rng = np.random.default_rng(seed)
             idx = np.sort(rng.choice(len(vals), NSAMPLE, replace=False))

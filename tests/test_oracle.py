@@ -252,3 +252,62 @@ def test_reference_solution_file_layout(tmp_path):
         else:
             np.testing.assert_array_equal(got[1:], levels[1:])
             np.testing.assert_array_equal(got[0], levels[1])
+
+
+# ----------------------------------------------------------- field sampling
+FIELD_CASES = ("g_static_2x2x2", "g_lingrad_4x2x2", "g_transient_3x2x2")
+
+
+def field_close(F, G, tol=1e-12):
+    """Per field column: |F - G| <= tol * max |G| of that column (sector codes exact)."""
+    scale = np.maximum(np.abs(G).reshape(-1, G.shape[-1]).max(axis=0), 1e-300)
+    return np.all(np.abs(F - G) <= tol * scale)
+
+
+@pytest.mark.parametrize("name", FIELD_CASES)
+def test_field_sampling_golden(name):
+    """The restated plot loop with the restated basis and field callbacks
+    (liborc) against the reference's basis, inverse and field callbacks
+    (golden field at field_scale x the state, plot lattice of nppe = 2)."""
+    g = load(name)
+    prob = problem_from_golden(g)
+    F, xq, X = po.OracleCase(prob).field(float(g["field_scale"]) * g["U"], int(g["field_nppe"]))
+    assert F.shape == g["field"].shape
+    np.testing.assert_array_equal(xq, g["field_xq"])
+    np.testing.assert_allclose(X, g["field_X"], rtol=0, atol=1e-14)
+    assert field_close(F, g["field"])
+    if prob.law != po.LAW_LINGRAD:  # sector codes: exact, and more than one occurs
+        np.testing.assert_array_equal(F[..., -1], g["field"][..., -1])
+        assert len(np.unique(g["field"][..., -1])) > 1
+
+
+@needs_ref
+@pytest.mark.parametrize("law,perturb", [(po.LAW_GRADELAST, True), (po.LAW_GRADELASTTIME, False),
+                                         (po.LAW_LINGRAD, True)])
+def test_field_sampling_vs_reference_callbacks(law, perturb):
+    prob = po.Problem(nelem=(3, 2, 4), L=(2.0, 1.0, 1.5), law=law, perturb=perturb)
+    U = 20.0 * po.random_state(prob, 31)
+    Fr, xr, Xr = po.RefCase(prob).field(U, 3)
+    Fo, xo, Xo = po.OracleCase(prob).field(U, 3)
+    np.testing.assert_array_equal(xo, xr)
+    np.testing.assert_allclose(Xo, Xr, rtol=0, atol=1e-14)
+    assert field_close(Fo, Fr)
+
+
+def test_field_sampling_linear_state_known_answer():
+    """A state linear in the control-point positions, U_b = A x_b, is
+    reproduced exactly by the (unit-weight) spline space: the sampled value is
+    A x at the sample position, the gradient A, the Hessian 0; the lattice
+    points sit 1e-15 inside the element spans."""
+    prob = po.Problem(nelem=(4, 2, 3), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, perturb=True)
+    _, _, Xc = po.mesh_beam(prob)
+    A = np.array([[1e-3, 2e-3, -1e-3], [0.5e-3, -1e-3, 3e-3], [2e-3, 1e-3, 1e-3]])
+    U = (Xc.reshape(-1, 3) @ A.T).reshape(1, -1)
+    F, xq, X = po.OracleCase(prob).field(U, 2)
+    u = F[..., :30].reshape(F.shape[:3] + (3, 10))
+    np.testing.assert_allclose(u[..., 0], X @ A.T, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(u[..., 1:4], np.broadcast_to(A, u.shape[:3] + (3, 3)), rtol=0, atol=1e-13)
+    assert np.abs(u[..., 4:]).max() <= 1e-12
+    k0, k1 = 0.75, 1.0  # last knot span in x
+    assert xq[0, 0, 0, 0] == 1e-15
+    assert xq[-1, 0, 0, 0] == k0 + 1e-15 + (k1 - k0) * 2 / 2 - 2 * 1e-15 * 1 and xq[-1, 0, 0, 0] < 1.0
