@@ -49,6 +49,7 @@ struct Batch {
   igapgpu_batch_schedule sched{1, 1, 1, 0};
   int nsm = 0;
   bool all_geof = false;  // every instance has the FP32 geometry cache
+  bool all_gop = false;   // every instance has its cached Gram operands
   size_t ctrl_bytes() const { return sizeof(int) * (64 + 2 * (size_t)ninst); }
 };
 
@@ -198,7 +199,7 @@ static int batch_kernels(Context *c, bool do_res, bool do_tan, double *RR, doubl
       IGAP_CUDA(cudaEventRecord(e0, c->stream));
     }
     int r = (c->law == IGAPGPU_LAW_LINGRAD && b->all_geof && !getenv("IGAPGPU_TC_DENSE"))
-                ? launch_tc_gram_batch(c, batch_args(c, 1, nitems), 2 * b->nsm, vals)
+                ? launch_tc_gram_batch(c, batch_args(c, 1, nitems), 2 * b->nsm, vals, b->all_gop)
                 : launch_tc_batch(c, batch_args(c, 1, nitems), c->law, b->nsm, c->d_Uhist, vals);
     if (r) return r;
     if (c->prof) {
@@ -277,6 +278,26 @@ __global__ void __launch_bounds__(256) segment_norm_kernel(const double *__restr
 
 // Rough device bytes of the batch besides the geometry caches: CSR values and
 // columns, state, Krylov basis (restart 100), staging.
+// Split precision on a batch: cached Gram operands for every instance (linear
+// law); the cached-operand kernel runs only when every instance has them.
+int batch_prepare_split(Context *c)
+{
+  Batch *b = c->batch;
+  bool all = true;
+  for (Context *s : b->subs) {
+    const int r = ensure_gram_operands(s);
+    if (r) return r;
+    all = all && s->d_gop != nullptr;
+  }
+  b->all_gop = all;
+  if (!all) return IGAPGPU_OK;
+  std::vector<DevMesh> hm(b->ninst);
+  IGAP_CUDA(cudaMemcpy(hm.data(), b->d_mesh, sizeof(DevMesh) * b->ninst, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < b->ninst; i++) hm[i].gop = b->subs[i]->d_gop;
+  IGAP_CUDA(cudaMemcpy(b->d_mesh, hm.data(), sizeof(DevMesh) * b->ninst, cudaMemcpyHostToDevice));
+  return IGAPGPU_OK;
+}
+
 static size_t batch_other_bytes(int64_t nnz, int64_t ndof, int torder)
 {
   return (size_t)nnz * 12 + (size_t)ndof * 8 * (size_t)(torder + 1 + 8 + 2 * 101);

@@ -55,6 +55,7 @@ struct DevMesh {
   int64_t dof_off;         // first DOF of this mesh in the state / residual vectors
   const double *geo;       // geometry cache [nelem][npts][272] or null
   const float *geof;       // FP32 copy of the geometry cache (split tangent) or null
+  const float *gop;        // Gram operands of the linear law in MMA layout (split tangent) or null
 };
 
 struct DevLaw {
@@ -129,6 +130,8 @@ struct Context {
   double *d_neu = nullptr;     // traction table on the device [36]
   double *d_geo = nullptr;     // geometry cache (physical basis + weight per point)
   float *d_geof = nullptr;     // FP32 copy for the split-precision tangent
+  float *d_gop = nullptr;      // linear law: sqrt(w)-weighted Gram operands in MMA layout (split tangent)
+  int gop_state = -1;          // -1 not decided, 0 off, 1 on
   double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
   double *d_preD = nullptr;
   int pre_state = -1;          // -1 not decided, 0 off, 1 on
@@ -189,6 +192,7 @@ struct Context {
     m.dof_off = 0;
     m.geo = d_geo;
     m.geof = d_geof;
+    m.gop = d_gop;
     return m;
   }
   DevLaw devlaw() const {
@@ -242,7 +246,10 @@ int launch_geometry_cache_f32(Context *c);
 int launch_tc_tangent(Context *c, double *vals, const DevLaw &L);
 // tc_gram.cu (linear isotropic law with the FP32 geometry cache)
 int launch_tc_gram(Context *c, double *vals);
-int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals);
+// cached: every instance has its Gram operands (d_gop)
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals, bool cached);
+// builds d_gop once (linear law, FP64 geometry cache present, memory allows)
+int ensure_gram_operands(Context *c);
 // krylov.cu
 int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
@@ -252,6 +259,7 @@ int dev_norm2(Context *c, const double *x, double *out);
 int launch_batch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
 void batch_release(Context *c);
 int batch_set_neumann(Context *c, const double *table);
+int batch_prepare_split(Context *c);
 // element kernels over a batch work queue (assemble.cu, tc_tangent.cu)
 int launch_element_batch(Context *c, const BatchArgs &a, int law, bool do_res, bool do_tan, int grid,
                          const double *Uhist, double *RR, double *vals);

@@ -19,6 +19,7 @@
 // chunk n run.  The epilogue stages G in shared memory, forms K and adds it
 // into the FP64 CSR values.  Every mbarrier wait is bounded.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 #include "element.cuh"
@@ -389,11 +390,449 @@ __global__ void __launch_bounds__(G_THREADS, 2) tcg_batch_kernel(BatchArgs ba, d
   tcg_teardown(S, st, ba.err);
 }
 
+// ------------------------------------------------- cached-operand variant
+// With the point weight split symmetrically, the Gram matrix is S S^T,
+//   S[(b,i), (q,0)]   = sqrt(w_q) dN_b/dx_i,
+//   S[(b,i), (q,1+m)] = sqrt(w_q) ell d2N_b/dx_i dx_m,
+// which depends only on the geometry and ell.  It is built once per context
+// in FP32, already in the MMA operand layout: per element and chunk of 8
+// points, 4 K-steps of 11 row groups (rows 0..87, rows 81..87 zero) of
+// 8 rows x 32 B.  Each chunk is then one bulk copy; the kernel only splits it
+// into TF32 hi + lo, and the same shared-memory tile is both MMA operands.
+// An MMA of M = 128 (N = 96) rows reads past row 87 into the next K-step's
+// rows: those products land in accumulator rows (columns) >= 88, never read.
+constexpr int S_RG = 11;                                     // row groups with rows 0..87
+constexpr int S_KS_BYTES = S_RG * 256;                       // 2816: one K-step
+constexpr int S_CH_BYTES = GKS * S_KS_BYTES;                 // 11264: one chunk of 8 points
+constexpr int S_OP_BYTES = (GKS - 1) * S_KS_BYTES + 128 * 32; // 12544: the last K-step's M = 128 read stays inside
+constexpr int S_NS = 4;                                      // bulk-copy stages
+
+// out[e][chunk][K-step][row group][K half][row][4]; bad = 1 when a point
+// weight is not positive (the symmetric split needs sqrt(w)).
+__global__ void gram_operand_kernel(const double *__restrict__ geo, int npts, int nchunk, int64_t nelem, double ell,
+                                    float *__restrict__ out, int *__restrict__ bad)
+{
+  constexpr int CHF = S_CH_BYTES / 4, KSF = S_KS_BYTES / 4;
+  const int64_t per_elem = (int64_t)nchunk * CHF;
+  const int64_t total = nelem * per_elem;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / per_elem;
+    int u = (int)(t - e * per_elem);
+    const int ch = u / CHF;
+    u -= ch * CHF;
+    const int ks = u / KSF;
+    u -= ks * KSF;
+    const int rg = u / 64, half = (u % 64) / 32, r8 = (u % 32) / 4, f = u % 4;
+    const int r = rg * 8 + r8, kk = ks * 8 + half * 4 + f;
+    float v = 0.f;
+    if (r < GROWS) {
+      const int b = r / 3, i = r % 3;
+      int p, slot;
+      bool hess;
+      if (kk < PW) {
+        p = kk;
+        slot = 1 + i;
+        hess = false;
+      } else {
+        p = (kk - PW) / 3;
+        slot = 4 + hess_slot(i, (kk - PW) % 3);
+        hess = true;
+      }
+      const int q = ch * PW + p;
+      if (q < npts) {
+        const double *g = geo + (e * npts + q) * GEO_STRIDE;
+        const double w = g[NB * NDD];
+        if (w > 0.0)
+          v = (float)(sqrt(w) * (hess ? ell : 1.0) * g[NDD * b + slot]);
+        else
+          atomicExch(bad, 1);
+      }
+    }
+    out[t] = v;
+  }
+}
+
+struct TcsSmem {
+  unsigned char op[2][2][S_OP_BYTES];  // [buffer][hi, lo]; the Gram matrix is staged here after the MMAs
+  unsigned char val[S_NS][S_CH_BYTES]; // bulk-copy stages
+  int pos[NB * NB];
+  int64_t rowp[NE];
+  uint64_t mbar_cp[S_NS];
+  uint64_t mbar_mma[2];
+  uint32_t taddr;
+  int abort;
+  int64_t base;
+};
+static_assert(GROWS * GPAD * 4 <= 2 * 2 * S_OP_BYTES, "the staged Gram matrix fits in the operand buffers");
+
+// Pipeline counters of one CTA (uniform across its threads): the chunk
+// stream runs over the CTA's elements; copies are issued up to S_NS chunks
+// ahead of the chunk being consumed, across element boundaries when the next
+// element is known.
+struct TcsState {
+  uint32_t cp_n[S_NS];  // copies issued per stage
+  uint32_t mma_n[2];    // commits per operand buffer
+  uint32_t issued, consumed, elem_start;
+};
+
+__device__ __forceinline__ void tcs_issue(TcsSmem &S, TcsState &st, const unsigned char *src)
+{
+  const int sg = (int)(st.issued % S_NS);
+  if (threadIdx.x == 0) {
+    tc::fence_proxy_async();
+    tc::mbar_arrive_expect_tx(&S.mbar_cp[sg], (uint32_t)S_CH_BYTES);
+    tc::bulk_g2s(S.val[sg], src, (uint32_t)S_CH_BYTES, &S.mbar_cp[sg]);
+  }
+  st.cp_n[sg]++;
+  st.issued++;
+}
+
+// One element from its cached operands esrc (nsrc: the next element of this
+// CTA, prefetched, or null).  Returns false when a bounded wait expired.
+template <bool COH>
+__device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevMesh &m, const DevLaw &L, int ex,
+                                            int ey, int ez, const unsigned char *esrc, const unsigned char *nsrc,
+                                            double *__restrict__ vals, uint32_t taddr, uint32_t op_base)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  const int nbv[3] = {m.nbasis[0], nb1, nb2};
+  const uint32_t nchunk = (uint32_t)((m.npts + PW - 1) / PW);
+  const uint32_t idesc = tc::instr_desc(2, 128, GN);
+  if (tid < NE) {
+    const int b = tid / 3, dd = tid % 3;
+    const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    S.rowp[tid] = __ldg(m.rowptr + 3 * cpb + dd);
+  }
+  for (int t = tid; t < NB * NB; t += G_THREADS) {
+    const int b = t / NB, c = t % NB;
+    S.pos[t] = (int)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9, ey + (c / 3) % 3,
+                                ez + c % 3, nbv);
+  }
+  for (uint32_t c = 0; c < nchunk; c++) {
+    while (st.issued - st.consumed < (uint32_t)S_NS) {  // stages freed by the chunks already split
+      const uint32_t k = st.issued - st.elem_start;
+      if (k < nchunk)
+        tcs_issue(S, st, esrc + (size_t)k * S_CH_BYTES);
+      else if (nsrc && k < 2 * nchunk)
+        tcs_issue(S, st, nsrc + (size_t)(k - nchunk) * S_CH_BYTES);
+      else
+        break;
+    }
+    const int sg = (int)(st.consumed % S_NS), ob = (int)(st.consumed & 1);
+    bool ok = tc::mbar_wait(&S.mbar_cp[sg], (st.cp_n[sg] - 1) & 1, G_WAIT_LIMIT);
+    // operand buffer ob was last read by the MMAs of the chunk before the previous one
+    if (ok && st.mma_n[ob] > 0) ok = tc::mbar_wait(&S.mbar_mma[ob], (st.mma_n[ob] - 1) & 1, G_WAIT_LIMIT);
+    if (!ok) S.abort = 1;
+    __syncthreads();
+    if (S.abort) return false;
+    {
+      const float4 *src = reinterpret_cast<const float4 *>(S.val[sg]);
+      float4 *hi = reinterpret_cast<float4 *>(S.op[ob][0]);
+      float4 *lo = reinterpret_cast<float4 *>(S.op[ob][1]);
+      for (int i = tid; i < S_CH_BYTES / 16; i += G_THREADS) {
+        const float4 v = src[i];
+        float4 h, l;
+        h.x = tc::to_tf32(v.x);
+        h.y = tc::to_tf32(v.y);
+        h.z = tc::to_tf32(v.z);
+        h.w = tc::to_tf32(v.w);
+        l.x = tc::to_tf32(v.x - h.x);
+        l.y = tc::to_tf32(v.y - h.y);
+        l.z = tc::to_tf32(v.z - h.z);
+        l.w = tc::to_tf32(v.w - h.w);
+        hi[i] = h;
+        lo[i] = l;
+      }
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t hb = op_base + (uint32_t)(ob * 2 * S_OP_BYTES), lb = hb + (uint32_t)S_OP_BYTES;
+      for (int ks = 0; ks < GKS; ks++)
+        for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
+          const uint32_t a = (pp == 2 ? lb : hb) + (uint32_t)(ks * S_KS_BYTES);
+          const uint32_t b = (pp == 1 ? lb : hb) + (uint32_t)(ks * S_KS_BYTES);
+          tc::mma_tf32(taddr, tc::smem_desc(a, 128, 256), tc::smem_desc(b, 128, 256), idesc,
+                       (c == 0 && ks == 0 && pp == 0) ? 0u : 1u);
+        }
+      tc::mma_commit(&S.mbar_mma[ob]);
+    }
+    st.mma_n[ob]++;
+    st.consumed++;
+  }
+  st.elem_start += nchunk;
+  // epilogue: the last commit covers every MMA of the element
+  const int lob = (int)((st.consumed - 1) & 1);
+  if (!tc::mbar_wait(&S.mbar_mma[lob], (st.mma_n[lob] - 1) & 1, G_WAIT_LIMIT)) S.abort = 1;
+  tc::fence_after_sync();
+  __syncthreads();
+  if (S.abort) return false;
+  float *G = reinterpret_cast<float *>(&S.op[0][0][0]);  // operands are no longer read
+  {
+    const int quarter = warp & 3;
+    const int r = quarter * 32 + lane;
+    for (int cb = warp >> 2; cb < 3; cb += 2) {
+      uint32_t v[32];
+      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cb * 32), v);
+      if (r < GROWS)
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (cb * 32 + j < GROWS) G[r * GPAD + cb * 32 + j] = __uint_as_float(v[j]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  {
+    const float lam = (float)L.par[0], mu = (float)L.par[1];
+    for (int t0 = tid; t0 < NE * NE; t0 += 9 * G_THREADS) {
+      int64_t slot[9];
+      float kv[9];
+      int cnt = 0;
+#pragma unroll
+      for (int s = 0; s < 9; s++) {
+        const int t = t0 + s * G_THREADS;
+        slot[s] = 0;
+        kv[s] = 0.f;
+        if (t < NE * NE) {
+          const int rr = t / NE, cc = t - NE * rr;
+          const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
+          float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
+          if (d == e)
+            kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] +
+                        G[(3 * b + 2) * GPAD + 3 * c + 2]);
+          slot[s] = S.rowp[rr] + 3 * S.pos[NB * b + c] + e;
+          kv[s] = kk;
+          cnt = s + 1;
+        }
+      }
+      double old[9];
+#pragma unroll
+      for (int s = 0; s < 9; s++)
+        if (s < cnt) old[s] = COH ? __ldcg(vals + slot[s]) : vals[slot[s]];
+#pragma unroll
+      for (int s = 0; s < 9; s++)
+        if (s < cnt) vals[slot[s]] = old[s] + (double)kv[s];
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tcs_setup(TcsSmem &S)
+{
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, G_TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; b++) tc::mbar_init(&S.mbar_mma[b], 1);
+    for (int b = 0; b < S_NS; b++) tc::mbar_init(&S.mbar_cp[b], 1);
+    S.abort = 0;
+  }
+  // the tail of each operand buffer past the split chunk (read only into
+  // accumulator rows that are never read) stays zero
+  for (int i = tid; i < (int)(sizeof(S.op) / 4); i += G_THREADS) reinterpret_cast<float *>(&S.op[0][0][0])[i] = 0.f;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+}
+
+// On an abort, waits (bounded) for the copies and MMAs in flight before the
+// shared memory is released; then frees TMEM.
+__device__ __forceinline__ void tcs_teardown(TcsSmem &S, const TcsState &st, int *err)
+{
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort) {
+    for (int b = 0; b < S_NS; b++)
+      if (st.cp_n[b] > 0) tc::mbar_wait(&S.mbar_cp[b], (st.cp_n[b] - 1) & 1, G_WAIT_LIMIT);
+    for (int b = 0; b < 2; b++)
+      if (st.mma_n[b] > 0) tc::mbar_wait(&S.mbar_mma[b], (st.mma_n[b] - 1) & 1, G_WAIT_LIMIT);
+    if (threadIdx.x == 0) atomicCAS(err, 0, 2);
+  }
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(S.taddr, G_TMEM_COLS);
+}
+
+__global__ void __launch_bounds__(G_THREADS, 2)
+    tcs_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
+               int *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcsSmem &S = *reinterpret_cast<TcsSmem *>(smem_raw);
+  tcs_setup(S);
+  const uint32_t taddr = S.taddr, op_base = tc::smem_u32(&S.op[0][0][0]);
+  TcsState st = {};
+  const int nelem_c = ncx * ncy * ncz;
+  const size_t ebytes = (size_t)((m.npts + PW - 1) / PW) * S_CH_BYTES;
+  const unsigned char *cache = reinterpret_cast<const unsigned char *>(m.gop);
+  auto src_of = [&](int ei, int &ex, int &ey, int &ez) {
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    ex = cx + 3 * ix;
+    ey = cy + 3 * iy;
+    ez = cz + 3 * iz;
+    const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+    return cache + (size_t)eg * ebytes;
+  };
+  for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
+    int ex, ey, ez, nx, ny, nz;
+    const unsigned char *esrc = src_of(ei, ex, ey, ez);
+    const unsigned char *nsrc = ei + (int)gridDim.x < nelem_c ? src_of(ei + gridDim.x, nx, ny, nz) : nullptr;
+    if (!tcs_element<false>(S, st, m, L, ex, ey, ez, esrc, nsrc, vals, taddr, op_base)) break;
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  tcs_teardown(S, st, err);
+}
+
+// Batched: elements from the colour-major queue (see element_batch_kernel);
+// copies prefetch within an element only.
+__global__ void __launch_bounds__(G_THREADS, 2) tcs_batch_kernel(BatchArgs ba, double *__restrict__ vals)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcsSmem &S = *reinterpret_cast<TcsSmem *>(smem_raw);
+  const int tid = threadIdx.x;
+  tcs_setup(S);
+  const uint32_t taddr = S.taddr, op_base = tc::smem_u32(&S.op[0][0][0]);
+  TcsState st = {};
+  int cur = -1;
+  DevMesh m;
+  DevLaw L;
+  int64_t next = 0;
+  if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+  for (;;) {
+    if (tid == 0) S.base = next;
+    __syncthreads();
+    const int64_t base = S.base;
+    __syncthreads();
+    if (base >= ba.nitems || S.abort) break;
+    if (tid == 0) next = atomicAdd(ba.head, ba.grab);
+    const int64_t end = base + ba.grab < ba.nitems ? base + ba.grab : ba.nitems;
+    bool ok = true;
+    for (int64_t it = base; it < end; it++) {
+      const BatchItem w = ba.items[it];
+      if (w.inst != cur) {
+        m = ba.meshes[w.inst];
+        L = ba.laws[w.inst];
+        cur = w.inst;
+      }
+      if (tid == 0 && w.col > 0) {
+        if (!tc_wait_ge(ba.done + w.inst, ba.need[27 * w.inst + w.col])) {
+          S.abort = 1;
+          atomicExch(ba.err, 3);
+        }
+      }
+      __syncthreads();
+      if (S.abort) {
+        ok = false;
+        break;
+      }
+      const int ey = w.eyz >> 16, ez = w.eyz & 0xffff;
+      const int64_t eg = ((int64_t)w.ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+      const unsigned char *esrc = reinterpret_cast<const unsigned char *>(m.gop) +
+                                  (size_t)eg * ((m.npts + PW - 1) / PW) * S_CH_BYTES;
+      ok = tcs_element<true>(S, st, m, L, w.ex, ey, ez, esrc, nullptr, vals, taddr, op_base);
+      if (!ok) break;
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0)  // release at GPU scope after the barrier
+        asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.s32 [%0], 1;" ::"l"(ba.done + w.inst)
+                     : "memory");
+    }
+    if (!ok) break;
+  }
+  tcs_teardown(S, st, ba.err);
+}
+
 // ------------------------------------------------------------- launches
 static size_t tcg_smem() { return sizeof(TcgSmem) + 1024; }
+static size_t tcs_smem() { return sizeof(TcsSmem) + 1024; }
+
+int ensure_gram_operands(Context *c)
+{
+  if (c->gop_state >= 0 || c->law != IGAPGPU_LAW_LINGRAD || !c->d_geo) return IGAPGPU_OK;
+  const char *env = getenv("IGAPGPU_TC_GRAM_CACHE");
+  c->gop_state = 0;
+  if (env && env[0] == '0') return IGAPGPU_OK;
+  const int npts = c->nquad * c->nquad * c->nquad, nchunk = (npts + PW - 1) / PW;
+  const size_t bytes = (size_t)c->nelem_total * nchunk * S_CH_BYTES;
+  size_t freeb = 0, totb = 0;
+  IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
+  if (bytes + ((size_t)4 << 30) > freeb) return IGAPGPU_OK;  // the plain Gram kernel stays in use
+  if (cudaMalloc(&c->d_gop, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    c->d_gop = nullptr;
+    return IGAPGPU_OK;
+  }
+  IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  gram_operand_kernel<<<nsm * 16, 256, 0, c->stream>>>(c->d_geo, npts, nchunk, c->nelem_total, c->par[2], c->d_gop,
+                                                       c->d_err);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  int bad = 0;
+  IGAP_CUDA(cudaMemcpyAsync(&bad, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  IGAP_CUDA(cudaStreamSynchronize(c->stream));
+  IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+  if (bad) {  // a non-positive point weight: keep the plain Gram kernel
+    cudaFree(c->d_gop);
+    c->d_gop = nullptr;
+    return IGAPGPU_OK;
+  }
+  c->gop_state = 1;
+  return IGAPGPU_OK;
+}
+
+static int launch_tc_gop(Context *c, double *vals)
+{
+  const DevMesh m = c->devmesh();
+  const DevLaw L = c->devlaw();
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcs_smem()));
+    attr = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  for (int cx = 0; cx < 3; cx++)
+    for (int cy = 0; cy < 3; cy++)
+      for (int cz = 0; cz < 3; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        const int nel = ncx * ncy * ncz;
+        if (nel <= 0) continue;
+        const int grid = nel < 2 * nsm ? nel : 2 * nsm;  // two CTAs per SM
+        tcs_kernel<<<grid, G_THREADS, tcs_smem(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
+        count_launch();
+        IGAP_CHECK_LAUNCH();
+        if (c->prof) {
+          c->prof_launches[1]++;
+          c->prof_elements[1] += nel;
+        }
+      }
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[1].emplace_back(e0, e1);
+  }
+  return IGAPGPU_OK;
+}
 
 int launch_tc_gram(Context *c, double *vals)
 {
+  if (c->d_gop) return launch_tc_gop(c, vals);
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
   static bool attr = false;
@@ -433,8 +872,20 @@ int launch_tc_gram(Context *c, double *vals)
   return IGAPGPU_OK;
 }
 
-int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals)
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals, bool cached)
 {
+  if (cached) {
+    static bool attr_s = false;
+    if (!attr_s) {
+      IGAP_CUDA(cudaFuncSetAttribute(tcs_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tcs_smem()));
+      attr_s = true;
+    }
+    tcs_batch_kernel<<<grid, G_THREADS, tcs_smem(), c->stream>>>(a, vals);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+    return IGAPGPU_OK;
+  }
   static bool attr = false;
   if (!attr) {
     IGAP_CUDA(cudaFuncSetAttribute(tcg_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -61,13 +61,15 @@ def compare_to_singles(B, As, U):
     return RR, vals
 
 
-@pytest.mark.parametrize("law", [ig.LAW_LINGRAD, ig.LAW_GRADELAST])
+@pytest.mark.parametrize("law,cached", [(ig.LAW_LINGRAD, "1"), (ig.LAW_LINGRAD, "0"), (ig.LAW_GRADELAST, "1")])
 @pytest.mark.parametrize("prec", [ig.PREC_FP64, ig.PREC_SPLIT])
-def test_batch_bit_identical_to_single_instances(law, prec, monkeypatch):
+def test_batch_bit_identical_to_single_instances(law, cached, prec, monkeypatch):
     # batches evaluate nonlinear laws inside the element kernels; so do the
     # single instances here (their all-points law launch is compared with this
     # in test_gpu_assembly.py: identical in FP64, within the split bound in split)
     monkeypatch.setenv("IGAPGPU_LAW_PRECOMPUTE", "0")
+    # linear law, split: Gram operands cached (sqrt(w) folded in) or built in the kernel
+    monkeypatch.setenv("IGAPGPU_TC_GRAM_CACHE", cached)
     insts = instances(law, seed=3)
     B = ig.BatchAssembly(insts, law=law)
     B.set_precision(prec)

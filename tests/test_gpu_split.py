@@ -3,8 +3,9 @@
 * the tcgen05 self-test GEMM reproduces an exact integer product;
 * the split tangent agrees with the FP64 tangent within the stated bound
   (relative 2-norm error <= 1e-5, measured ~4e-6; TF32 hi+lo operands keep ~21 bits, the
-  FP32 tensor-memory accumulation dominates), for all three laws and both GEMM forms
-  of the linear law (Gram form, and the two-stage form used by the other laws);
+  FP32 tensor-memory accumulation dominates), for all three laws and every GEMM form
+  of the linear law (Gram form from cached sqrt(w)-weighted operands, Gram form built
+  from the FP32 geometry cache, and the two-stage form used by the other laws);
 * the residual of the split mode is the FP64 residual, unchanged.
 """
 import numpy as np
@@ -27,16 +28,19 @@ def test_tcgen05_selftest_exact():
     assert np.array_equal(D, E), f"max |D-E| = {np.abs(D - E).max()}"
 
 
-@pytest.mark.parametrize("law,nelem,perturb,dense", [
-    (po.LAW_LINGRAD, (8, 4, 3), False, False),   # Gram-form GEMM (tc_gram.cu)
-    (po.LAW_LINGRAD, (5, 3, 4), True, False),
-    (po.LAW_LINGRAD, (8, 4, 3), False, True),    # two-stage GEMM (tc_tangent.cu)
-    (po.LAW_GRADELAST, (4, 4, 4), True, False),
-    (po.LAW_GRADELASTTIME, (3, 3, 4), False, False),
+@pytest.mark.parametrize("law,nelem,perturb,form", [
+    (po.LAW_LINGRAD, (8, 4, 3), False, "cached"),  # Gram-form GEMM on cached operands (tc_gram.cu)
+    (po.LAW_LINGRAD, (5, 3, 4), True, "cached"),
+    (po.LAW_LINGRAD, (5, 3, 4), True, "gram"),     # Gram-form GEMM built from the FP32 geometry cache
+    (po.LAW_LINGRAD, (8, 4, 3), False, "dense"),   # two-stage GEMM (tc_tangent.cu)
+    (po.LAW_GRADELAST, (4, 4, 4), True, "dense"),
+    (po.LAW_GRADELASTTIME, (3, 3, 4), False, "dense"),
 ])
-def test_split_tangent_vs_fp64(law, nelem, perturb, dense, monkeypatch):
-    if dense:
+def test_split_tangent_vs_fp64(law, nelem, perturb, form, monkeypatch):
+    if form == "dense" and law == po.LAW_LINGRAD:
         monkeypatch.setenv("IGAPGPU_TC_DENSE", "1")
+    if form == "gram":
+        monkeypatch.setenv("IGAPGPU_TC_GRAM_CACHE", "0")
     bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     prob = po.Problem(nelem=nelem, law=law, perturb=perturb, bc_type=bct, neumann=neu)
     U = po.random_state(prob, 77)
@@ -45,7 +49,10 @@ def test_split_tangent_vs_fp64(law, nelem, perturb, dense, monkeypatch):
     A.set_state(U)
     K64 = A.tangent()
     R64 = A.residual()
+    n0 = ig.launch_count()
     A.set_precision(ig.PREC_SPLIT)
+    # the cached form builds its operands once, in one launch, when split precision is set
+    assert ig.launch_count() - n0 == (1 if law == po.LAW_LINGRAD and form != "gram" else 0)
     Ks = A.tangent()
     Rs = A.residual()
     e = rel(Ks, K64)
@@ -60,10 +67,13 @@ def test_split_tangent_vs_fp64(law, nelem, perturb, dense, monkeypatch):
     assert rel(V, K64) <= SPLIT_TOL
 
 
+@pytest.mark.parametrize("cached", ["1", "0"])
 @pytest.mark.parametrize("nquad", [3, 4])
-def test_split_gram_partial_chunks(nquad):
+def test_split_gram_partial_chunks(nquad, cached, monkeypatch):
     """Gram-form split tangent with 27 points per element (chunks of 8, 8, 8, 3)
-    and with 64, against the FP64 tangent of the same quadrature."""
+    and with 64, against the FP64 tangent of the same quadrature, from cached
+    operands and built in the kernel."""
+    monkeypatch.setenv("IGAPGPU_TC_GRAM_CACHE", cached)
     bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     knots, w, X = ig.beam_mesh((6, 3, 2), (4.0, 1.0, 1.0), 2, True)
     A = ig.Assembly((6, 3, 2), knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct,
