@@ -59,6 +59,40 @@ __device__ __forceinline__ bool tc_wait_ge(const int *p, int target)
 }
 }  // namespace
 
+// float -> double on the integer pipe (bit-exact with the conversion for
+// normal numbers and zeros; subnormals, infinities and NaN take the
+// conversion instruction): FP64 work is scarce on this GPU.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu)
+    return (b & 0x7fffffffu) == 0u ? __hiloint2double((int)(b & 0x80000000u), 0) : (double)f;
+  const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+// K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc
+// for every (b,d), (c,e) (6,561 slots, each once per element), added into the
+// FP64 CSR values by fire-and-forget reductions at L2: no load latency and no
+// FP64 add on the SM.  Within a colour no two elements share a slot and the
+// colours are ordered, so every slot still receives its contributions in
+// colour order (the same sums, bit for bit, as a read-modify-write).
+__device__ __forceinline__ void gram_scatter(const float *G, const int64_t *rowp, const int *pos, const DevLaw &L,
+                                             double *__restrict__ vals)
+{
+  const float lam = (float)L.par[0], mu = (float)L.par[1];
+  for (int t = threadIdx.x; t < NE * NE; t += G_THREADS) {
+    const int rr = t / NE, cc = t - NE * rr;
+    const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
+    float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
+    if (d == e)
+      kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] + G[(3 * b + 2) * GPAD + 3 * c + 2]);
+    double *dst = vals + rowp[rr] + 3 * pos[NB * b + c] + e;
+    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(f32_to_f64(kk)) : "memory");
+  }
+}
+
 struct TcgSmem {
   unsigned char A[2 * GA_PIECE];     // [hi, lo][K-step][4096 B]; the Gram matrix is staged here after the MMAs
   unsigned char B[2 * GB_PIECE];     // [hi, lo][K-step][3072 B]
@@ -239,39 +273,7 @@ __device__ __forceinline__ bool tcg_element(TcgSmem &S, TcgState &st, const TcgT
   }
   tc::fence_before_sync();
   __syncthreads();
-  // K[(b,d),(c,e)] for every (b,d), (c,e): 6561 slots, each written once
-  {
-    const float lam = (float)L.par[0], mu = (float)L.par[1];
-    for (int t0 = tid; t0 < NE * NE; t0 += 9 * G_THREADS) {
-      int64_t slot[9];
-      float kv[9];
-      int cnt = 0;
-#pragma unroll
-      for (int s = 0; s < 9; s++) {
-        const int t = t0 + s * G_THREADS;
-        slot[s] = 0;
-        kv[s] = 0.f;
-        if (t < NE * NE) {
-          const int rr = t / NE, cc = t - NE * rr;
-          const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
-          float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
-          if (d == e)
-            kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] +
-                        G[(3 * b + 2) * GPAD + 3 * c + 2]);
-          slot[s] = S.rowp[rr] + 3 * S.pos[NB * b + c] + e;
-          kv[s] = kk;
-          cnt = s + 1;
-        }
-      }
-      double old[9];
-#pragma unroll
-      for (int s = 0; s < 9; s++)
-        if (s < cnt) old[s] = COH ? __ldcg(vals + slot[s]) : vals[slot[s]];
-#pragma unroll
-      for (int s = 0; s < 9; s++)
-        if (s < cnt) vals[slot[s]] = old[s] + (double)kv[s];
-    }
-  }
+  gram_scatter(G, S.rowp, S.pos, L, vals);
   return true;
 }
 
@@ -586,38 +588,7 @@ __device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevM
   }
   tc::fence_before_sync();
   __syncthreads();
-  {
-    const float lam = (float)L.par[0], mu = (float)L.par[1];
-    for (int t0 = tid; t0 < NE * NE; t0 += 9 * G_THREADS) {
-      int64_t slot[9];
-      float kv[9];
-      int cnt = 0;
-#pragma unroll
-      for (int s = 0; s < 9; s++) {
-        const int t = t0 + s * G_THREADS;
-        slot[s] = 0;
-        kv[s] = 0.f;
-        if (t < NE * NE) {
-          const int rr = t / NE, cc = t - NE * rr;
-          const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
-          float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
-          if (d == e)
-            kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] +
-                        G[(3 * b + 2) * GPAD + 3 * c + 2]);
-          slot[s] = S.rowp[rr] + 3 * S.pos[NB * b + c] + e;
-          kv[s] = kk;
-          cnt = s + 1;
-        }
-      }
-      double old[9];
-#pragma unroll
-      for (int s = 0; s < 9; s++)
-        if (s < cnt) old[s] = COH ? __ldcg(vals + slot[s]) : vals[slot[s]];
-#pragma unroll
-      for (int s = 0; s < 9; s++)
-        if (s < cnt) vals[slot[s]] = old[s] + (double)kv[s];
-    }
-  }
+  gram_scatter(G, S.rowp, S.pos, L, vals);
   return true;
 }
 
