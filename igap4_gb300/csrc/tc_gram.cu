@@ -78,7 +78,8 @@ __device__ __forceinline__ double f32_to_f64(float f)
 // FP64 add on the SM.  Within a colour no two elements share a slot and the
 // colours are ordered, so every slot still receives its contributions in
 // colour order (the same sums, bit for bit, as a read-modify-write).
-__device__ __forceinline__ void gram_scatter(const float *G, const int64_t *rowp, const int *pos, const DevLaw &L,
+template <typename PosT>
+__device__ __forceinline__ void gram_scatter(const float *G, const int64_t *rowp, const PosT *pos, const DevLaw &L,
                                              double *__restrict__ vals)
 {
   const float lam = (float)L.par[0], mu = (float)L.par[1];
@@ -88,7 +89,7 @@ __device__ __forceinline__ void gram_scatter(const float *G, const int64_t *rowp
     float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
     if (d == e)
       kk += mu * (G[(3 * b) * GPAD + 3 * c] + G[(3 * b + 1) * GPAD + 3 * c + 1] + G[(3 * b + 2) * GPAD + 3 * c + 2]);
-    double *dst = vals + rowp[rr] + 3 * pos[NB * b + c] + e;
+    double *dst = vals + rowp[rr] + 3 * (int)pos[NB * b + c] + e;
     asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(f32_to_f64(kk)) : "memory");
   }
 }
@@ -407,7 +408,8 @@ constexpr int S_RG = 11;                                     // row groups with 
 constexpr int S_KS_BYTES = S_RG * 256;                       // 2816: one K-step
 constexpr int S_CH_BYTES = GKS * S_KS_BYTES;                 // 11264: one chunk of 8 points
 constexpr int S_OP_BYTES = (GKS - 1) * S_KS_BYTES + 128 * 32; // 12544: the last K-step's M = 128 read stays inside
-constexpr int S_NS = 4;                                      // bulk-copy stages
+// copy stages x CTAs per SM: 2 x 3 (default; measured 6.9 ms per tangent at
+// 128x32x32) or 4 x 2 (IGAPGPU_TCS_CTAS=2; 8.0 ms)
 
 // out[e][chunk][K-step][row group][K half][row][4]; bad = 1 when a point
 // weight is not positive (the symmetric split needs sqrt(w)).
@@ -455,32 +457,36 @@ __global__ void gram_operand_kernel(const double *__restrict__ geo, int npts, in
   }
 }
 
+template <int NS>
 struct TcsSmem {
   unsigned char op[2][2][S_OP_BYTES];  // [buffer][hi, lo]; the Gram matrix is staged here after the MMAs
-  unsigned char val[S_NS][S_CH_BYTES]; // bulk-copy stages
-  int pos[NB * NB];
+  unsigned char val[NS][S_CH_BYTES];   // bulk-copy stages
+  unsigned char pos[NB * NB];          // stencil position (< 125) of column point c in the row of point b
   int64_t rowp[NE];
-  uint64_t mbar_cp[S_NS];
+  uint64_t mbar_cp[NS];
   uint64_t mbar_mma[2];
   uint32_t taddr;
   int abort;
   int64_t base;
 };
 static_assert(GROWS * GPAD * 4 <= 2 * 2 * S_OP_BYTES, "the staged Gram matrix fits in the operand buffers");
+static_assert((2 * P + 1) * (2 * P + 1) * (2 * P + 1) <= 256, "stencil positions fit in a byte");
 
 // Pipeline counters of one CTA (uniform across its threads): the chunk
-// stream runs over the CTA's elements; copies are issued up to S_NS chunks
+// stream runs over the CTA's elements; copies are issued up to NS chunks
 // ahead of the chunk being consumed, across element boundaries when the next
 // element is known.
+template <int NS>
 struct TcsState {
-  uint32_t cp_n[S_NS];  // copies issued per stage
+  uint32_t cp_n[NS];    // copies issued per stage
   uint32_t mma_n[2];    // commits per operand buffer
   uint32_t issued, consumed, elem_start;
 };
 
-__device__ __forceinline__ void tcs_issue(TcsSmem &S, TcsState &st, const unsigned char *src)
+template <int NS>
+__device__ __forceinline__ void tcs_issue(TcsSmem<NS> &S, TcsState<NS> &st, const unsigned char *src)
 {
-  const int sg = (int)(st.issued % S_NS);
+  const int sg = (int)(st.issued % NS);
   if (threadIdx.x == 0) {
     tc::fence_proxy_async();
     tc::mbar_arrive_expect_tx(&S.mbar_cp[sg], (uint32_t)S_CH_BYTES);
@@ -492,8 +498,8 @@ __device__ __forceinline__ void tcs_issue(TcsSmem &S, TcsState &st, const unsign
 
 // One element from its cached operands esrc (nsrc: the next element of this
 // CTA, prefetched, or null).  Returns false when a bounded wait expired.
-template <bool COH>
-__device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevMesh &m, const DevLaw &L, int ex,
+template <int NS, bool COH>
+__device__ __forceinline__ bool tcs_element(TcsSmem<NS> &S, TcsState<NS> &st, const DevMesh &m, const DevLaw &L, int ex,
                                             int ey, int ez, const unsigned char *esrc, const unsigned char *nsrc,
                                             double *__restrict__ vals, uint32_t taddr, uint32_t op_base)
 {
@@ -509,11 +515,11 @@ __device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevM
   }
   for (int t = tid; t < NB * NB; t += G_THREADS) {
     const int b = t / NB, c = t % NB;
-    S.pos[t] = (int)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9, ey + (c / 3) % 3,
+    S.pos[t] = (unsigned char)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9, ey + (c / 3) % 3,
                                 ez + c % 3, nbv);
   }
   for (uint32_t c = 0; c < nchunk; c++) {
-    while (st.issued - st.consumed < (uint32_t)S_NS) {  // stages freed by the chunks already split
+    while (st.issued - st.consumed < (uint32_t)NS) {  // stages freed by the chunks already split
       const uint32_t k = st.issued - st.elem_start;
       if (k < nchunk)
         tcs_issue(S, st, esrc + (size_t)k * S_CH_BYTES);
@@ -522,13 +528,12 @@ __device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevM
       else
         break;
     }
-    const int sg = (int)(st.consumed % S_NS), ob = (int)(st.consumed & 1);
+    const int sg = (int)(st.consumed % NS), ob = (int)(st.consumed & 1);
     bool ok = tc::mbar_wait(&S.mbar_cp[sg], (st.cp_n[sg] - 1) & 1, G_WAIT_LIMIT);
     // operand buffer ob was last read by the MMAs of the chunk before the previous one
     if (ok && st.mma_n[ob] > 0) ok = tc::mbar_wait(&S.mbar_mma[ob], (st.mma_n[ob] - 1) & 1, G_WAIT_LIMIT);
+    // each thread waits for itself; a wait that expired is acted on after the barrier
     if (!ok) S.abort = 1;
-    __syncthreads();
-    if (S.abort) return false;
     {
       const float4 *src = reinterpret_cast<const float4 *>(S.val[sg]);
       float4 *hi = reinterpret_cast<float4 *>(S.op[ob][0]);
@@ -551,6 +556,7 @@ __device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevM
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
+    if (S.abort) return false;
     if (tid == 0) {
       tc::fence_after_sync();
       const uint32_t hb = op_base + (uint32_t)(ob * 2 * S_OP_BYTES), lb = hb + (uint32_t)S_OP_BYTES;
@@ -592,7 +598,8 @@ __device__ __forceinline__ bool tcs_element(TcsSmem &S, TcsState &st, const DevM
   return true;
 }
 
-__device__ __forceinline__ void tcs_setup(TcsSmem &S)
+template <int NS>
+__device__ __forceinline__ void tcs_setup(TcsSmem<NS> &S)
 {
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) {
@@ -601,7 +608,7 @@ __device__ __forceinline__ void tcs_setup(TcsSmem &S)
   }
   if (tid == 0) {
     for (int b = 0; b < 2; b++) tc::mbar_init(&S.mbar_mma[b], 1);
-    for (int b = 0; b < S_NS; b++) tc::mbar_init(&S.mbar_cp[b], 1);
+    for (int b = 0; b < NS; b++) tc::mbar_init(&S.mbar_cp[b], 1);
     S.abort = 0;
   }
   // the tail of each operand buffer past the split chunk (read only into
@@ -614,12 +621,13 @@ __device__ __forceinline__ void tcs_setup(TcsSmem &S)
 
 // On an abort, waits (bounded) for the copies and MMAs in flight before the
 // shared memory is released; then frees TMEM.
-__device__ __forceinline__ void tcs_teardown(TcsSmem &S, const TcsState &st, int *err)
+template <int NS>
+__device__ __forceinline__ void tcs_teardown(TcsSmem<NS> &S, const TcsState<NS> &st, int *err)
 {
   tc::fence_before_sync();
   __syncthreads();
   if (S.abort) {
-    for (int b = 0; b < S_NS; b++)
+    for (int b = 0; b < NS; b++)
       if (st.cp_n[b] > 0) tc::mbar_wait(&S.mbar_cp[b], (st.cp_n[b] - 1) & 1, G_WAIT_LIMIT);
     for (int b = 0; b < 2; b++)
       if (st.mma_n[b] > 0) tc::mbar_wait(&S.mbar_mma[b], (st.mma_n[b] - 1) & 1, G_WAIT_LIMIT);
@@ -629,15 +637,16 @@ __device__ __forceinline__ void tcs_teardown(TcsSmem &S, const TcsState &st, int
   if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(S.taddr, G_TMEM_COLS);
 }
 
-__global__ void __launch_bounds__(G_THREADS, 2)
+template <int NS, int MINB>
+__global__ void __launch_bounds__(G_THREADS, MINB)
     tcs_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
                int *err)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcsSmem &S = *reinterpret_cast<TcsSmem *>(smem_raw);
+  TcsSmem<NS> &S = *reinterpret_cast<TcsSmem<NS> *>(smem_raw);
   tcs_setup(S);
   const uint32_t taddr = S.taddr, op_base = tc::smem_u32(&S.op[0][0][0]);
-  TcsState st = {};
+  TcsState<NS> st = {};
   const int nelem_c = ncx * ncy * ncz;
   const size_t ebytes = (size_t)((m.npts + PW - 1) / PW) * S_CH_BYTES;
   const unsigned char *cache = reinterpret_cast<const unsigned char *>(m.gop);
@@ -653,7 +662,7 @@ __global__ void __launch_bounds__(G_THREADS, 2)
     int ex, ey, ez, nx, ny, nz;
     const unsigned char *esrc = src_of(ei, ex, ey, ez);
     const unsigned char *nsrc = ei + (int)gridDim.x < nelem_c ? src_of(ei + gridDim.x, nx, ny, nz) : nullptr;
-    if (!tcs_element<false>(S, st, m, L, ex, ey, ez, esrc, nsrc, vals, taddr, op_base)) break;
+    if (!tcs_element<NS, false>(S, st, m, L, ex, ey, ez, esrc, nsrc, vals, taddr, op_base)) break;
     tc::fence_before_sync();
     __syncthreads();
   }
@@ -662,14 +671,15 @@ __global__ void __launch_bounds__(G_THREADS, 2)
 
 // Batched: elements from the colour-major queue (see element_batch_kernel);
 // copies prefetch within an element only.
-__global__ void __launch_bounds__(G_THREADS, 2) tcs_batch_kernel(BatchArgs ba, double *__restrict__ vals)
+template <int NS, int MINB>
+__global__ void __launch_bounds__(G_THREADS, MINB) tcs_batch_kernel(BatchArgs ba, double *__restrict__ vals)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcsSmem &S = *reinterpret_cast<TcsSmem *>(smem_raw);
+  TcsSmem<NS> &S = *reinterpret_cast<TcsSmem<NS> *>(smem_raw);
   const int tid = threadIdx.x;
   tcs_setup(S);
   const uint32_t taddr = S.taddr, op_base = tc::smem_u32(&S.op[0][0][0]);
-  TcsState st = {};
+  TcsState<NS> st = {};
   int cur = -1;
   DevMesh m;
   DevLaw L;
@@ -706,7 +716,7 @@ __global__ void __launch_bounds__(G_THREADS, 2) tcs_batch_kernel(BatchArgs ba, d
       const int64_t eg = ((int64_t)w.ex * m.nelem[1] + ey) * m.nelem[2] + ez;
       const unsigned char *esrc = reinterpret_cast<const unsigned char *>(m.gop) +
                                   (size_t)eg * ((m.npts + PW - 1) / PW) * S_CH_BYTES;
-      ok = tcs_element<true>(S, st, m, L, w.ex, ey, ez, esrc, nullptr, vals, taddr, op_base);
+      ok = tcs_element<NS, true>(S, st, m, L, w.ex, ey, ez, esrc, nullptr, vals, taddr, op_base);
       if (!ok) break;
       tc::fence_before_sync();
       __syncthreads();
@@ -721,7 +731,15 @@ __global__ void __launch_bounds__(G_THREADS, 2) tcs_batch_kernel(BatchArgs ba, d
 
 // ------------------------------------------------------------- launches
 static size_t tcg_smem() { return sizeof(TcgSmem) + 1024; }
-static size_t tcs_smem() { return sizeof(TcsSmem) + 1024; }
+template <int NS>
+static size_t tcs_smem() { return sizeof(TcsSmem<NS>) + 1024; }
+
+// 3 CTAs per SM with 2 copy stages (default), or 2 CTAs per SM with 4
+static int tcs_ctas_per_sm()
+{
+  const char *env = getenv("IGAPGPU_TCS_CTAS");
+  return (env && env[0] == '2') ? 2 : 3;
+}
 
 int ensure_gram_operands(Context *c)
 {
@@ -760,13 +778,15 @@ int ensure_gram_operands(Context *c)
   return IGAPGPU_OK;
 }
 
-static int launch_tc_gop(Context *c, double *vals)
+template <int NS, int MINB>
+static int launch_tc_gop_cfg(Context *c, double *vals)
 {
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
+  auto kern = tcs_kernel<NS, MINB>;
   static bool attr = false;
   if (!attr) {
-    IGAP_CUDA(cudaFuncSetAttribute(tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcs_smem()));
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcs_smem<NS>()));
     attr = true;
   }
   int dev = 0, nsm = 0;
@@ -785,8 +805,8 @@ static int launch_tc_gop(Context *c, double *vals)
                   ncz = (c->nelem[2] - cz + 2) / 3;
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
-        const int grid = nel < 2 * nsm ? nel : 2 * nsm;  // two CTAs per SM
-        tcs_kernel<<<grid, G_THREADS, tcs_smem(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
+        const int grid = nel < MINB * nsm ? nel : MINB * nsm;  // MINB persistent CTAs per SM
+        kern<<<grid, G_THREADS, tcs_smem<NS>(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
@@ -799,6 +819,11 @@ static int launch_tc_gop(Context *c, double *vals)
     c->prof_ev[1].emplace_back(e0, e1);
   }
   return IGAPGPU_OK;
+}
+
+static int launch_tc_gop(Context *c, double *vals)
+{
+  return tcs_ctas_per_sm() == 3 ? launch_tc_gop_cfg<2, 3>(c, vals) : launch_tc_gop_cfg<4, 2>(c, vals);
 }
 
 int launch_tc_gram(Context *c, double *vals)
@@ -846,13 +871,17 @@ int launch_tc_gram(Context *c, double *vals)
 int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals, bool cached)
 {
   if (cached) {
-    static bool attr_s = false;
-    if (!attr_s) {
-      IGAP_CUDA(cudaFuncSetAttribute(tcs_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)tcs_smem()));
-      attr_s = true;
+    const bool three = tcs_ctas_per_sm() == 3;
+    auto kern = three ? tcs_batch_kernel<2, 3> : tcs_batch_kernel<4, 2>;
+    const size_t sm = three ? tcs_smem<2>() : tcs_smem<4>();
+    static bool attr_s[2] = {false, false};
+    if (!attr_s[three]) {
+      IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      attr_s[three] = true;
     }
-    tcs_batch_kernel<<<grid, G_THREADS, tcs_smem(), c->stream>>>(a, vals);
+    // grid: the caller's two CTAs per SM, or three
+    const int g = three ? grid / 2 * 3 : grid;
+    kern<<<g, G_THREADS, sm, c->stream>>>(a, vals);
     count_launch();
     IGAP_CHECK_LAUNCH();
     return IGAPGPU_OK;
