@@ -113,90 +113,6 @@ __device__ __forceinline__ double *dw_ptr(typename ElemCfg<TAN>::Smem &S, int w)
   else return nullptr;
 }
 
-// Residual of the linear law from the geometry cache with every thread busy
-// (the general path below maps a point to a warp, which leaves 5 of 32 lanes
-// idle in the state sums and 15 of 96 in the projection; on this GPU the
-// residual is bound by the FP64 pipe).  Per chunk of 8 points:
-//   state derivatives u[10d+k], k = 1..9: 8 x 27 sums of 27 products,
-//   the law rr = w D u (30 sparse rows per point),
-//   projection: output (b,d) in three parts of 24 of its 72 (point, k) terms,
-// the parts added in a fixed order at the end (deterministic; the batched
-// and single-instance launches share this code).
-template <bool COH>
-__device__ __forceinline__ void residual_lin(ResSmem &S, const DevMesh &m, const DevLaw &L, int ex, int ey, int ez,
-                                             double *__restrict__ RR)
-{
-  constexpr int NT = ElemCfg<false>::NT;
-  const int tid = threadIdx.x;
-  const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
-  const double *geo = m.geo + eg * m.npts * GEO_STRIDE;
-  const int nchunk = (m.npts + PW - 1) / PW;
-  // projection task: output o = 3b + d, part g of the (point, k) terms
-  const int o = tid % NE, g = tid / NE;  // g == 3: no projection work
-  const int bb = o / 3, dd = o % 3;
-  double racc = 0.0;
-  for (int ch = 0; ch < nchunk; ch++) {
-    const int q0 = ch * PW;
-    for (int i = tid; i < PW * GEO_STRIDE; i += NT) {
-      const int w = i / GEO_STRIDE, j = i - w * GEO_STRIDE;
-      const double v = q0 + w < m.npts ? __ldg(geo + (size_t)(q0 + w) * GEO_STRIDE + j) : 0.0;
-      if (j < NB * NDD)
-        S.R[w][j] = v;
-      else if (j == NB * NDD)
-        S.Pt[w].wt = v;
-    }
-    __syncthreads();
-    if (tid < PW * 27) {
-      const int w = tid / 27, j = tid - 27 * w, d = j / 9, k = 1 + j % 9;
-      const double *R = S.R[w];
-      double sum = 0.0;
-      for (int b = 0; b < NB; b++) sum += R[NDD * b + k] * S.E.U[3 * b + d];
-      S.Pt[w].u[NDD * d + k] = sum;
-    } else if (tid < PW * 30) {
-      const int t = tid - PW * 27;
-      S.Pt[t / 3].u[NDD * (t % 3)] = 0.0;  // value slots: the law has no value column
-    }
-    __syncthreads();
-    if (tid < PW * 30) {
-      const int w = tid / 30, row = tid - 30 * w;
-      const double *u = S.Pt[w].u;
-      double sum = 0.0;
-      if (L.dptr) {
-        const int j1 = __ldg(L.dptr + row + 1);
-        for (int j = __ldg(L.dptr + row); j < j1; j++) sum += __ldg(L.dval + j) * u[__ldg(L.dcol + j)];
-      } else {
-        for (int j = 0; j < 30; j++) sum += __ldg(L.Dconst + 30 * row + j) * u[j];
-      }
-      S.rr[w][row] = S.Pt[w].wt * sum;
-    }
-    __syncthreads();
-    if (g < 3) {
-      // terms t = 24g .. 24g+23 of t = 9 w + (k - 1)
-      int w = (24 * g) / 9, k = 1 + (24 * g) % 9;
-      double sum = 0.0;
-      for (int t = 0; t < 24; t++) {
-        sum += S.R[w][NDD * bb + k] * S.rr[w][NDD * dd + k];
-        if (++k == NDD) {
-          k = 1;
-          w++;
-        }
-      }
-      racc += sum;
-    }
-    __syncthreads();
-  }
-  double *part = &S.R[0][0];  // free after the last chunk
-  if (g < 3) part[g * NE + o] = racc;
-  __syncthreads();
-  if (tid < NE) {
-    const double r = (part[o] + part[NE + o]) + part[2 * NE + o];
-    const int i = bb / 9, j = (bb / 3) % 3, l = bb % 3;
-    const int64_t cp = ((int64_t)(ex + i) * m.nbasis[1] + (ey + j)) * m.nbasis[2] + (ez + l);
-    double *dst = RR + m.dof_off + 3 * cp + dd;
-    *dst = (COH ? __ldcg(dst) : *dst) + r;
-  }
-}
-
 // One element: load, quadrature (phase A, B1, B2) and the scatter into RR /
 // vals.  COH: the read-modify-write of RR / vals bypasses L1 (a batched
 // launch orders colours inside one kernel, through L2).
@@ -213,12 +129,6 @@ __device__ __forceinline__ void element_body(typename ElemCfg<TAN>::Smem &S, Law
   constexpr int NT = ElemCfg<TAN>::NT;
   load_element(S.E, m, nh, Uhist, ex, ey, ez, tid, NT);
   __syncthreads();
-  if constexpr (LAWK == 0 && RES && !TAN) {
-    if (m.geo) {
-      residual_lin<COH>(S, m, L, ex, ey, ez, RR);
-      return;
-    }
-  }
 
   double acc[9];
 #pragma unroll
