@@ -134,19 +134,30 @@ def features(u_n, u_nm1, dload, scales: Scales):
 class LearnedPredictor:
     """Callable (u_n, u_{n-1}, dload) -> guess for u_{n+1} (device float64)."""
 
-    def __init__(self, net: ConvNet, scales: Scales, dload_dir=(0.0, 0.0, 1.0)):
+    def __init__(self, net: ConvNet, scales: Scales, dload_dir=(0.0, 0.0, 1.0), scaled: bool = True):
         import torch
 
+        self.scaled = scaled
         self.net = net
         self.scales = scales
         self.dir = np.asarray(dload_dir, np.float64)
         self.out = torch.empty((1, net.P, 3), dtype=torch.float32, device="cuda")
 
-    def __call__(self, u_n, u_nm1, dload_scalar):
+    def correction(self, u_n, u_nm1, dload_scalar):
         x = features(u_n, u_nm1, self.dir * dload_scalar, self.scales)[None]
         self.net.forward(x, self.out)
-        corr = self.out.view(-1).double() * self.scales.out
-        return u_n + (u_n - u_nm1) + corr
+        return self.out.view(-1).double() * self.scales.out
+
+    def __call__(self, u_n, u_nm1, dload_scalar):
+        return u_n + (u_n - u_nm1) + self.correction(u_n, u_nm1, dload_scalar)
+
+    def candidates(self, u_n, u_nm1, dload_scalar):
+        """The network's guess and two shortened steps along its correction
+        (half of it, none: the linear extrapolation); the transient driver
+        keeps the one with the smallest residual, or u_n."""
+        ext = u_n + (u_n - u_nm1)
+        corr = self.correction(u_n, u_nm1, dload_scalar)
+        return [ext + corr, ext + 0.5 * corr, ext] if self.scaled else [ext + corr]
 
 
 def make_samples(states, loads, lattice_points):

@@ -8,7 +8,9 @@ command line).
 2. Samples (u_n, u_{n-1}, load increment) -> correction to linear extrapolation.
 3. Adam training with the library's own BF16 network kernels.
 4. Unseen load histories: Newton iterations and wall time per step, plain
-   Newton (guess u_n) vs the predictor (kept only when it lowers |F|).
+   Newton (guess u_n) vs the predictor: the network's guess and two shorter
+   steps along its correction, the best kept only when it lowers |F| below
+   that of u_n.
 Prints one JSON line.
 """
 from __future__ import annotations
@@ -109,6 +111,8 @@ def main():
     ap.add_argument("--amax", type=float, default=1e-3)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval-nelem", default=None, help="evaluate on another mesh (default: same)")
+    ap.add_argument("--compare-single", action="store_true",
+                    help="also evaluate the network's guess alone (no shortened steps)")
     a = ap.parse_args()
     import torch  # noqa: F401
 
@@ -136,12 +140,14 @@ def main():
     from .predictor import init_params
 
     extrap_net = type(net)(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
-    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, scales), opts)
+    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, scales, scaled=False), opts)
     learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales), opts)
+    single = (evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, scaled=False), opts)
+              if a.compare_single else None)
     out = {"train_mesh": list(nelem), "eval_mesh": list(A.nelem), "train_trajectories": a.train,
            "steps": a.steps, "samples": len(X), "generation_s": t_gen, "training_s": t_train,
            "loss_first": hist[0], "loss_last": hist[-1], "plain": plain,
-           "extrapolation_only": extrap, "learned": learned,
+           "extrapolation_only": extrap, "learned": learned, "learned_single_guess": single,
            "time_ratio_learned_vs_plain": learned["seconds_per_step"] / plain["seconds_per_step"],
            "its_ratio_learned_vs_plain": learned["newton_its_per_step"] / plain["newton_its_per_step"]}
     print(json.dumps(out))

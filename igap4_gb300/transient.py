@@ -62,8 +62,9 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     """Advance `nsteps` steps of size dt (dt must equal the law's par[7]).
 
     A: igap4_gb300.Assembly with the transient law.  predictor: optional
-    callable (u_n, u_nm1, dload) -> guess for u_{n+1}; its guess is kept only
-    if it lowers the residual norm below that of u_n (plain Newton fallback).
+    callable (u_n, u_nm1, dload) -> guess for u_{n+1}, or an object whose
+    candidates(u_n, u_nm1, dload) lists guesses; a guess is kept only if it
+    lowers the residual norm below that of u_n (plain Newton fallback).
     Returns (states [nsteps+1, ndof] or None, list of StepRecord)."""
     import torch
 
@@ -91,16 +92,22 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         used = False
         if predictor is not None:
             # the Newton correction leaves Dirichlet DOFs where the initial
-            # iterate puts them (their columns are cleared), so the guess
-            # carries the prescribed values exactly
-            guess = A.impose_dirichlet(predictor(u_n, u_nm1, load.value(t) - prev_load).contiguous())
+            # iterate puts them (their columns are cleared), so every guess
+            # carries the prescribed values exactly; a predictor may offer
+            # several guesses (the one with the smallest residual is taken)
+            dl = load.value(t) - prev_load
+            cands = predictor.candidates(u_n, u_nm1, dl) if hasattr(predictor, "candidates") \
+                else [predictor(u_n, u_nm1, dl)]
             A.residual(U, F)
-            f_plain = A.norm2(F)
-            A.residual(guess, F)
-            f_pred = A.norm2(F)
-            if f_pred < f_plain:
-                U = guess.clone()
-                used = True
+            best = A.norm2(F)
+            for g in cands:
+                guess = A.impose_dirichlet(g.contiguous())
+                A.residual(guess, F)
+                f_pred = A.norm2(F)
+                if f_pred < best:
+                    best = f_pred
+                    U = guess.clone()
+                    used = True
         st = A.solve(U, **o)
         A.synchronize()
         dtm = time.perf_counter() - t0
