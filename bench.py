@@ -55,7 +55,7 @@ TRAFFIC_FP64_LAUNCH = 1.5063e9
 # cached-operand tensor-core tangent: per element the operands (8 chunks x
 # 11,264 B) and the read-modify-write of its 6,561 FP64 CSR slots
 ALG_BYTES_TCS_ELEM = 8 * 11264 + 2 * 8 * 6561
-TRAFFIC_TCS_LAUNCH = None  # filled from the launch list once measured
+TRAFFIC_TCS_LAUNCH = 1.1635e9  # ncu launch list at 128x32x32, per colour launch
 
 
 def parse():
