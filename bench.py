@@ -310,6 +310,7 @@ def main():
 
     import torch
     import igap4_gb300 as ig
+    from igap4_gb300.replicas import job_rate, max_over_ranks
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -356,11 +357,7 @@ def main():
         kinds = {kd: A.profile_read(kd) for kd in (0, 1)}
         A.profile(False)
         step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-        dev_ms = sum(step_ms)
-        if world > 1:
-            t = torch.tensor([dev_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            dev_ms = t.item()
+        dev_ms = max_over_ranks(sum(step_ms), dev)
         return dev_ms / steps, step_ms, kinds, launches
 
     sampler = ClockSampler()
@@ -370,7 +367,7 @@ def main():
     headline_prec = ig.PREC_SPLIT if a.prec == "split" else fp64_prec
     ms_per_step, step_ms, kinds, launches = measure(headline_prec, a.steps, a.warmup)
     t_wall = time.perf_counter() - t_wall0
-    value = world * A.nelem_total / (ms_per_step * 1e-3)
+    value = job_rate(A.nelem_total, ms_per_step, world)
     elem_ms, elem_launches, elem_count = kinds[0] if headline_prec == fp64_prec else kinds[1]
     dev_ms = ms_per_step * a.steps
 
