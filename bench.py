@@ -247,7 +247,7 @@ def bench_batched(ig, torch, dev, n, steps, warmup, flush, peaks):
     tc_ach = TAN_FLOP_PER_ELEM * tc_e / (tc_ms * 1e-3) / 1e12 if tc_ms > 0 else None
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     # one Newton step of the block-diagonal system from zero: assembly, then a
-    # fixed budget of GMRES(100) iterations (Jacobi), replayed from CUDA graphs
+    # a fixed number of GMRES(100) iterations (Jacobi), replayed from CUDA graphs
     B.set_stream(None)
     Z = torch.zeros(B.ndof, dtype=torch.float64, device=dev)
     kits = 200

@@ -7,7 +7,7 @@
 // the first three.  Storage type T is float (used for gradient checks) or
 // bfloat16 (training and inference); every product accumulates in FP32.
 // Master weights and Adam moments are FP32.
-// No counterpart in the reference (a spec addition).
+// No counterpart in the reference (an addition to its solver path).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>

@@ -1,6 +1,6 @@
 // Split-precision tangent assembly on the tensor cores (tcgen05, TF32x3).
 //
-// For one element the tangent block of SURVEY's K6 loop,
+// For one element the tangent block of the assembly loop,
 //   K[(b,d),(c,e)] = sum_q sum_{k,l} R_q[b,k] w_q D_q[(d,k),(e,l)] R_q[c,l]
 // (src/assmcore_iga.c:722-750), is evaluated as one GEMM per element
 //   K^T[(d,c,e), b] = sum_{(q,k)} A[(d,c,e),(q,k)] B[b,(q,k)]

@@ -1,6 +1,6 @@
 """Train the learned Newton predictor on trajectories of the plain method and
-measure what it gains (spec config 5, scaled to the sizes given on the
-command line).
+measure what it gains (the transient beam of the learned-predictor workload,
+scaled to the sizes given on the command line).
 
     python -m igap4_gb300.train_predictor --nelem 16,4,4 --train 6 --steps 60 --test 2
 
@@ -8,9 +8,7 @@ command line).
 2. Samples (u_n, u_{n-1}, load increment) -> correction to linear extrapolation.
 3. Adam training with the library's own BF16 network kernels.
 4. Unseen load histories: Newton iterations and wall time per step, plain
-   Newton (guess u_n) vs the predictor: the network's guess and two shorter
-   steps along its correction, the best kept only when it lowers |F| below
-   that of u_n.
+   Newton (guess u_n) vs the predictor (kept only when it lowers |F|).
 Prints one JSON line.
 """
 from __future__ import annotations
@@ -111,8 +109,8 @@ def main():
     ap.add_argument("--amax", type=float, default=1e-3)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval-nelem", default=None, help="evaluate on another mesh (default: same)")
-    ap.add_argument("--compare-single", action="store_true",
-                    help="also evaluate the network's guess alone (no shortened steps)")
+    ap.add_argument("--compare-shortened", action="store_true",
+                    help="also evaluate the best of the guess and two shortened steps along its correction")
     a = ap.parse_args()
     import torch  # noqa: F401
 
@@ -142,12 +140,12 @@ def main():
     extrap_net = type(net)(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
     extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, scales, scaled=False), opts)
     learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales), opts)
-    single = (evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, scaled=False), opts)
-              if a.compare_single else None)
+    shortened = (evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, scaled=True), opts)
+                 if a.compare_shortened else None)
     out = {"train_mesh": list(nelem), "eval_mesh": list(A.nelem), "train_trajectories": a.train,
            "steps": a.steps, "samples": len(X), "generation_s": t_gen, "training_s": t_train,
            "loss_first": hist[0], "loss_last": hist[-1], "plain": plain,
-           "extrapolation_only": extrap, "learned": learned, "learned_single_guess": single,
+           "extrapolation_only": extrap, "learned": learned, "learned_best_of_shortened": shortened,
            "time_ratio_learned_vs_plain": learned["seconds_per_step"] / plain["seconds_per_step"],
            "its_ratio_learned_vs_plain": learned["newton_its_per_step"] / plain["newton_its_per_step"]}
     print(json.dumps(out))

@@ -101,7 +101,7 @@ def main():
         quad[f"w{n}"] = w
     np.savez_compressed(os.path.join(OUT, "quadrature.npz"), **quad)
 
-    # survey sanity value: 4x4x4 unit cube, gradelast, face 0 clamped, glibc
+    # sanity value: 4x4x4 unit cube, gradelast, face 0 clamped, glibc
     # rand() seed 123456 scaled 0.01 (IGAPSolvRand, src/interface.c:261-269)
     print("done")
 

@@ -125,7 +125,7 @@ def test_assembly_summary_golden(name):
                                atol=1e-13 * np.abs(g["sample_vals"]).max())
 
 
-def test_survey_sanity_value_glibc_rand():
+def test_sanity_value_glibc_rand():
     """4x4x4 unit cube, static law, face x=0 clamped (both orders), U from
     glibc rand() seed 123456 scaled 0.01 on every DOF (IGAPSolvRand,
     src/interface.c:261-269): the reference gives |R|^2 = 3.68958470382283..."""
