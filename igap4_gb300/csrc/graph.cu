@@ -40,11 +40,10 @@ __global__ void __launch_bounds__(256) gm_spmv(const int64_t *__restrict__ rowpt
                                                int nb1, int nb2)
 {
   if (st && st->done) return;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const double s = spmv_row(rowptr, cols, vals, x, row, lane, nb0, nb1, nb2);
-  if (lane == 0) y[row] = s;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_G;
+  const int sub = threadIdx.x % SPMV_G;
+  const double s = spmv_row(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
+  if (sub == 0 && row < n) y[row] = s;
 }
 
 __global__ void __launch_bounds__(RT) gm_dot_partial(const double *__restrict__ a, const double *__restrict__ b,
@@ -248,7 +247,7 @@ static int build_gmres_graph(Context *c, int m, int pc)
   gw->m = m;
   gw->pc = pc;
   const unsigned vb = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
-  const unsigned sb = (unsigned)((n * 32 + 255) / 256);
+  const unsigned sb = (unsigned)((n * SPMV_G + 255) / 256);
   cudaStream_t s = capture_stream(c);
   int64_t nodes = 0;
   IGAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));

@@ -18,7 +18,7 @@ namespace igap {
 constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
 constexpr int RED_THREADS = 512;
 
-// y = A x, one warp per row (spmv_row; structured columns when nb0 > 0).
+// y = A x, SPMV_G lanes per row (spmv_row; structured columns when nb0 > 0).
 __global__ void __launch_bounds__(256) spmv_csr_kernel(const int64_t *__restrict__ rowptr,
                                                        const int32_t *__restrict__ cols,
                                                        const double *__restrict__ vals,
@@ -26,11 +26,10 @@ __global__ void __launch_bounds__(256) spmv_csr_kernel(const int64_t *__restrict
                                                        double *__restrict__ y, int64_t n, int nb0, int nb1,
                                                        int nb2)
 {
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const double s = spmv_row(rowptr, cols, vals, x, row, lane, nb0, nb1, nb2);
-  if (lane == 0) y[row] = s;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_G;
+  const int sub = threadIdx.x % SPMV_G;
+  const double s = spmv_row(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
+  if (sub == 0 && row < n) y[row] = s;
 }
 
 __global__ void get_diag_kernel(const int64_t *rowptr, const int32_t *cols, const double *vals,
@@ -134,7 +133,7 @@ int spmv(Context *c, const double *vals, const double *x, double *y)
 {
   const int64_t n = c->ndof;
   const int nb0 = c->batch ? 0 : c->nbasis[0];  // a batch's rows belong to different lattices
-  spmv_csr_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n,
+  spmv_csr_kernel<<<(unsigned)((n * SPMV_G + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n,
                                                                             nb0, c->nbasis[1], c->nbasis[2]);
   count_launch();
   IGAP_CHECK_LAUNCH();
