@@ -498,7 +498,11 @@ def main():
             "roofline": roofline,
             "spmv": {"ms": spmv_ms, "GB_per_s": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
                      "frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / hbm_peak, "bytes": spmv_bytes,
-                     "repetitions": a.spmv},
+                     "repetitions": a.spmv,
+                     # one FP64 FMA per nonzero: on this GPU the FP64 pipe, not HBM, bounds the multiply
+                     "fp64_tflops": 2 * nnz_total / (spmv_ms * 1e-3) / 1e12,
+                     "frac_of_fp64": 2 * nnz_total / (spmv_ms * 1e-3) / 1e12 / fp64_peak,
+                     "bound": "fp64"},
             "cpu_baseline": cpu,
             "split": split,
             "batched": batched,
