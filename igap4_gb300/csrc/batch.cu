@@ -199,7 +199,7 @@ static int batch_kernels(Context *c, bool do_res, bool do_tan, double *RR, doubl
       IGAP_CUDA(cudaEventRecord(e0, c->stream));
     }
     int r = (c->law == IGAPGPU_LAW_LINGRAD && b->all_geof && !getenv("IGAPGPU_TC_DENSE"))
-                ? launch_tc_gram_batch(c, batch_args(c, 1, nitems), 2 * b->nsm, vals, b->all_gop)
+                ? launch_tc_gram_batch(c, batch_args(c, 1, nitems), b->nsm, vals, b->all_gop)
                 : launch_tc_batch(c, batch_args(c, 1, nitems), c->law, b->nsm, c->d_Uhist, vals);
     if (r) return r;
     if (c->prof) {

@@ -246,8 +246,8 @@ int launch_geometry_cache_f32(Context *c);
 int launch_tc_tangent(Context *c, double *vals, const DevLaw &L);
 // tc_gram.cu (linear isotropic law with the FP32 geometry cache)
 int launch_tc_gram(Context *c, double *vals);
-// cached: every instance has its Gram operands (d_gop)
-int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals, bool cached);
+// cached: every instance has its Gram operands (d_gop); persistent CTAs per SM of nsm
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int nsm, double *vals, bool cached);
 // builds d_gop once (linear law, FP64 geometry cache present, memory allows)
 int ensure_gram_operands(Context *c);
 // krylov.cu

@@ -757,18 +757,33 @@ int ensure_gram_operands(Context *c)
     c->d_gop = nullptr;
     return IGAPGPU_OK;
   }
-  IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
-  int dev = 0, nsm = 0;
-  IGAP_CUDA(cudaGetDevice(&dev));
-  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  gram_operand_kernel<<<nsm * 16, 256, 0, c->stream>>>(c->d_geo, npts, nchunk, c->nelem_total, c->par[2], c->d_gop,
-                                                       c->d_err);
-  count_launch();
-  IGAP_CHECK_LAUNCH();
+  int *d_bad = nullptr;
+  if (cudaMalloc(&d_bad, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(c->d_gop);
+    c->d_gop = nullptr;
+    return IGAPGPU_OK;
+  }
   int bad = 0;
-  IGAP_CUDA(cudaMemcpyAsync(&bad, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  IGAP_CUDA(cudaStreamSynchronize(c->stream));
-  IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+  cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+  int dev = 0, nsm = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    gram_operand_kernel<<<nsm * 16, 256, 0, c->stream>>>(c->d_geo, npts, nchunk, c->nelem_total, c->par[2],
+                                                         c->d_gop, d_bad);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_bad);
+  if (e != cudaSuccess) {
+    cudaFree(c->d_gop);
+    c->d_gop = nullptr;
+    set_error("gram operands: CUDA error %s", cudaGetErrorString(e));
+    return IGAPGPU_ERR_CUDA;
+  }
   if (bad) {  // a non-positive point weight: keep the plain Gram kernel
     cudaFree(c->d_gop);
     c->d_gop = nullptr;
@@ -868,7 +883,7 @@ int launch_tc_gram(Context *c, double *vals)
   return IGAPGPU_OK;
 }
 
-int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals, bool cached)
+int launch_tc_gram_batch(Context *c, const BatchArgs &a, int nsm, double *vals, bool cached)
 {
   if (cached) {
     const bool three = tcs_ctas_per_sm() == 3;
@@ -879,9 +894,7 @@ int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals,
       IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       attr_s[three] = true;
     }
-    // grid: the caller's two CTAs per SM, or three
-    const int g = three ? grid / 2 * 3 : grid;
-    kern<<<g, G_THREADS, sm, c->stream>>>(a, vals);
+    kern<<<(three ? 3 : 2) * nsm, G_THREADS, sm, c->stream>>>(a, vals);  // persistent CTAs per SM
     count_launch();
     IGAP_CHECK_LAUNCH();
     return IGAPGPU_OK;
@@ -892,7 +905,7 @@ int launch_tc_gram_batch(Context *c, const BatchArgs &a, int grid, double *vals,
                                    (int)tcg_smem()));
     attr = true;
   }
-  tcg_batch_kernel<<<grid, G_THREADS, tcg_smem(), c->stream>>>(a, vals);
+  tcg_batch_kernel<<<2 * nsm, G_THREADS, tcg_smem(), c->stream>>>(a, vals);  // two persistent CTAs per SM
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;
