@@ -153,6 +153,7 @@ struct Context {
   double *d_work = nullptr;    // [4][ndof]
   double *d_diag = nullptr;    // [ndof]
   double *d_bdiag = nullptr;   // [3 ndof] inverted 3 x 3 point blocks (point-block Jacobi)
+  double *d_cinv = nullptr;    // [cells][24 x 24] inverted cell blocks (cell-block Jacobi, lazy)
   double *d_red = nullptr;     // device scalars (norms, Hessenberg column) [red_cap]
   double *h_red = nullptr;     // pinned host mirror of d_red [red_cap]
   double *d_partial = nullptr; // per-block partial sums of the reductions
@@ -255,6 +256,9 @@ int spmv(Context *c, const double *vals, const double *x, double *y);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
               double *rnorm);
 int dev_norm2(Context *c, const double *x, double *out);
+struct CellGeom;
+CellGeom cell_geom(const Context *c);
+int ensure_cblock(Context *c, int64_t ncell);
 // batch.cu
 int launch_batch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
 void batch_release(Context *c);

@@ -99,11 +99,16 @@ __global__ void gm_scale_div(double *y, const double *x, const double *den, int6
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = x[i] * inv;
 }
-__global__ void gm_precond(double *z, const double *v, const double *diag, int pc, int64_t n, const GmState *st)
+__global__ void gm_precond(double *z, const double *v, const double *diag, int pc, int64_t n, CellGeom cg,
+                           const GmState *st)
 {
   if (st->done) return;
   if (pc == 2) {  // point-block Jacobi: diag holds the inverted 3 x 3 blocks
     bdiag_apply(z, v, diag, n / 3);
+    return;
+  }
+  if (pc == 3) {  // cell-block Jacobi: diag holds the inverted cell blocks
+    cblock_apply(z, v, diag, cg, cell_count(cg));
     return;
   }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -237,7 +242,8 @@ static int build_gmres_graph(Context *c, int m, int pc)
       alloc(&gw->V, (size_t)(m + 1) * n) || alloc(&gw->Z, (size_t)m * n) ||
       alloc(&gw->H, (size_t)(m + 1) * m) || alloc(&gw->cs, m) || alloc(&gw->sn, m) ||
       alloc(&gw->g, m + 1) || alloc(&gw->y, m) || alloc(&gw->scal, m + 2) || alloc(&gw->partial, RB) ||
-      alloc(&gw->diag, 3 * n) || cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
+      alloc(&gw->diag, pc == 3 ? (size_t)cell_count(cell_geom(c)) * CBS * CBS : (size_t)3 * n) ||
+      cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
       cudaMallocHost(&gw->h_st, sizeof(GmState)) != cudaSuccess) {
     cudaGetLastError();
     free_graph(gw);
@@ -264,7 +270,7 @@ static int build_gmres_graph(Context *c, int m, int pc)
   for (int j = 0; j < m; j++) {
     double *vj = gw->V + (size_t)j * n, *zj = gw->Z + (size_t)j * n, *vn = gw->V + (size_t)(j + 1) * n;
     double *hcol = gw->H + (size_t)j * (m + 1);
-    gm_precond<<<vb, 256, 0, s>>>(zj, vj, gw->diag, pc, n, gw->st);
+    gm_precond<<<vb, 256, 0, s>>>(zj, vj, gw->diag, pc, n, cell_geom(c), gw->st);
     gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st, nb0, c->nbasis[1],
                                c->nbasis[2]);
     nodes += 2;
@@ -307,7 +313,11 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
                     double *rnorm_out)
 {
   const int m = o->ksp_restart > 0 ? o->ksp_restart : 30;
-  const int pc = (o->pc == 1 || o->pc == 2) ? o->pc : 0;
+  const int pc = (o->pc >= 1 && o->pc <= 3) ? o->pc : 0;
+  if (pc == 3 && c->batch) {
+    set_error("cell-block Jacobi (pc = 3) needs a single lattice; a batch takes pc 0, 1 or 2");
+    return IGAPGPU_ERR_ARG;
+  }
   if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc) {
     int r = build_gmres_graph(c, m, pc);
     if (r) return r;
@@ -324,6 +334,13 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
   } else if (pc == 2) {
     bdiag_invert_kernel<<<(unsigned)((n / 3 + 255) / 256), 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->diag,
                                                                       n / 3);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+  } else if (pc == 3) {
+    const CellGeom cg = cell_geom(c);
+    const int64_t ncell = cell_count(cg);
+    cblock_invert_kernel<<<(unsigned)((ncell + CB_WARPS - 1) / CB_WARPS), 32 * CB_WARPS, 0, s>>>(c->d_rowptr, c->d_vals,
+                                                                                              gw->diag, cg, ncell);
     count_launch();
     IGAP_CHECK_LAUNCH();
   }

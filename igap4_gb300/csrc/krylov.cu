@@ -104,6 +104,11 @@ __global__ void scale_div_kernel(double *y, const double *x, const double *pden,
     y[i] = x[i] * inv;
 }
 // z = v / diag (Jacobi; zero diagonal -> 1, as PCJACOBI)
+__global__ void cblock_kernel(double *z, const double *v, const double *inv, CellGeom g, int64_t ncell)
+{
+  cblock_apply(z, v, inv, g, ncell);
+}
+
 __global__ void bdiag_kernel(double *z, const double *v, const double *inv, int64_t ncp)
 {
   bdiag_apply(z, v, inv, ncp);
@@ -203,6 +208,32 @@ int dev_norm2(Context *c, const double *x, double *out)
   return IGAPGPU_OK;
 }
 
+// Lattice cells of the cell-block Jacobi preconditioner (2 x 2 x 2 control points).
+CellGeom cell_geom(const Context *c)
+{
+  CellGeom g;
+  for (int d = 0; d < 3; d++) {
+    g.nb[d] = c->nbasis[d];
+    g.nc[d] = (c->nbasis[d] + 1) / 2;
+  }
+  return g;
+}
+
+int ensure_cblock(Context *c, int64_t ncell)
+{
+  if (c->batch) {
+    set_error("cell-block Jacobi (pc = 3) needs a single lattice; a batch takes pc 0, 1 or 2");
+    return IGAPGPU_ERR_ARG;
+  }
+  if (!c->d_cinv && cudaMalloc(&c->d_cinv, sizeof(double) * (size_t)ncell * CBS * CBS) != cudaSuccess) {
+    cudaGetLastError();
+    c->d_cinv = nullptr;
+    set_error("cell-block Jacobi: allocation of %lld blocks failed", (long long)ncell);
+    return IGAPGPU_ERR_NOMEM;
+  }
+  return IGAPGPU_OK;
+}
+
 // Right-preconditioned GMRES(m) with MGS, x in/out (device), b device.
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its_out,
               double *rnorm_out)
@@ -213,12 +244,20 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
   const int64_t n = c->ndof;
   double *V = c->d_V, *Z = c->d_Z, *w = c->d_work, *rvec = c->d_work + n;
   const unsigned vb = vec_blocks(n);
+  const CellGeom cg = cell_geom(c);
+  const int64_t ncell = cell_count(cg);
   if (o->pc == 1) {
     get_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, c->d_vals, c->d_diag, n);
     count_launch();
   } else if (o->pc == 2) {  // point-block Jacobi: inverted 3 x 3 blocks, 9 per control point
     bdiag_invert_kernel<<<(unsigned)((n / 3 + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, c->d_vals,
                                                                                c->d_bdiag, n / 3);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+  } else if (o->pc == 3) {  // cell-block Jacobi: inverted blocks of the 2 x 2 x 2 control-point cells
+    if ((r = ensure_cblock(c, ncell))) return r;
+    cblock_invert_kernel<<<(unsigned)((ncell + CB_WARPS - 1) / CB_WARPS), 32 * CB_WARPS, 0, c->stream>>>(
+        c->d_rowptr, c->d_vals, c->d_cinv, cg, ncell);
     count_launch();
     IGAP_CHECK_LAUNCH();
   }
@@ -259,6 +298,9 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
         count_launch();
       } else if (o->pc == 2) {
         bdiag_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_bdiag, n / 3);
+        count_launch();
+      } else if (o->pc == 3) {
+        cblock_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_cinv, cg, ncell);
         count_launch();
       } else {
         IGAP_CUDA(cudaMemcpyAsync(zj, vj, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));

@@ -15,6 +15,7 @@
 // for a group past the last row.
 #pragma once
 #include "common.cuh"
+#include "element.cuh"
 
 namespace igap {
 
@@ -108,6 +109,148 @@ static __global__ void bdiag_invert_kernel(const int64_t *__restrict__ rowptr, c
   } else {
     for (int i = 0; i < 9; i++) o[i] = 0.0;
     for (int d = 0; d < 3; d++) o[4 * d] = a[4 * d] != 0.0 ? 1.0 / a[4 * d] : 1.0;
+  }
+}
+
+// Cell-block Jacobi: the diagonal blocks of the 2 x 2 x 2 control-point cells
+// of the lattice (cells clipped at the far faces; up to 24 x 24, the cell's
+// DOFs in DOF order), inverted in FP64 by Gauss-Jordan elimination with
+// partial pivoting, one warp per cell.  A block whose pivot vanishes or is not
+// finite falls back to the inverse of its diagonal (1 where that is zero).
+// Entries are found from the structured stencil (the cell's control points
+// are within one of each other, so every entry exists in the pattern).
+constexpr int CBS = 24;  // largest block (8 control points x 3 DOFs)
+
+struct CellGeom {
+  int nb[3];     // control points per direction
+  int nc[3];     // cells per direction
+};
+
+__host__ __device__ inline int64_t cell_count(const CellGeom &g)
+{
+  return (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
+}
+
+// Control points of cell `cell` (x-major, z fastest) and their count.
+__device__ __forceinline__ int cell_points(const CellGeom &g, int64_t cell, int64_t cps[8])
+{
+  const int gz = (int)(cell % g.nc[2]);
+  const int64_t t = cell / g.nc[2];
+  const int gy = (int)(t % g.nc[1]), gx = (int)(t / g.nc[1]);
+  int n = 0;
+  for (int jx = 2 * gx; jx < 2 * gx + 2 && jx < g.nb[0]; jx++)
+    for (int jy = 2 * gy; jy < 2 * gy + 2 && jy < g.nb[1]; jy++)
+      for (int jz = 2 * gz; jz < 2 * gz + 2 && jz < g.nb[2]; jz++)
+        cps[n++] = ((int64_t)jx * g.nb[1] + jy) * g.nb[2] + jz;
+  return n;
+}
+
+constexpr int CB_WARPS = 4;  // cells per block of the inversion
+
+static __global__ void __launch_bounds__(32 * CB_WARPS) cblock_invert_kernel(const int64_t *__restrict__ rowptr,
+                                                                             const double *__restrict__ vals,
+                                                                             double *__restrict__ inv, CellGeom g,
+                                                                             int64_t ncell)
+{
+  __shared__ double Aug[CB_WARPS][CBS][2 * CBS + 1];  // per warp [A | I], padded row
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t cell = (int64_t)blockIdx.x * CB_WARPS + warp;
+  if (cell >= ncell) return;  // whole warp
+  double(*A)[2 * CBS + 1] = Aug[warp];
+  int64_t cps[8];
+  const int np = cell_points(g, cell, cps);
+  const int bs = 3 * np;
+  for (int t = lane; t < CBS * 2 * CBS; t += 32) {
+    const int a = t / (2 * CBS), b = t % (2 * CBS);
+    double v = 0.0;
+    if (a < bs && b < bs) {
+      const int p = a / 3, d = a % 3, q = b / 3, e = b % 3;
+      int ix, iy, iz, jx, jy, jz;
+      cp_coords(cps[p], g.nb, ix, iy, iz);
+      cp_coords(cps[q], g.nb, jx, jy, jz);
+      const int64_t r = 3 * cps[p] + d;
+      v = vals[rowptr[r] + 3 * stencil_pos(ix, iy, iz, jx, jy, jz, g.nb) + e];
+    } else if (b >= CBS) {
+      v = (b - CBS == a) ? 1.0 : 0.0;
+    }
+    A[a][b] = v;
+  }
+  __syncwarp();
+  bool ok = true;
+  for (int k = 0; k < bs && ok; k++) {
+    // pivot: the largest |A[i][k]|, i >= k
+    double best = (lane >= k && lane < bs) ? fabs(A[lane][k]) : -1.0;
+    int arg = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+      if (ob > best || (ob == best && oa < arg)) {
+        best = ob;
+        arg = oa;
+      }
+    }
+    if (!(best > 0.0) || !isfinite(best)) {
+      ok = false;
+      break;
+    }
+    if (arg != k)
+      for (int c = lane; c < 2 * CBS; c += 32) {
+        const double tmp = A[k][c];
+        A[k][c] = A[arg][c];
+        A[arg][c] = tmp;
+      }
+    __syncwarp();
+    const double piv = A[k][k];
+    double f[CBS];
+#pragma unroll
+    for (int i = 0; i < CBS; i++) f[i] = A[i][k];
+    __syncwarp();
+    for (int c = lane; c < 2 * CBS; c += 32) {
+      const double rk = A[k][c] / piv;
+      A[k][c] = rk;
+#pragma unroll
+      for (int i = 0; i < CBS; i++)
+        if (i != k && i < bs) A[i][c] -= f[i] * rk;
+    }
+    __syncwarp();
+  }
+  double *o = inv + (size_t)cell * CBS * CBS;
+  for (int t = lane; t < CBS * CBS; t += 32) {
+    const int a = t / CBS, b = t % CBS;
+    double v = 0.0;
+    if (a < bs && b < bs) {
+      if (ok) {
+        v = A[a][CBS + b];
+      } else if (a == b) {  // fallback: inverse of the diagonal
+        const int p = a / 3, d = a % 3;
+        int ix, iy, iz;
+        cp_coords(cps[p], g.nb, ix, iy, iz);
+        const int64_t r = 3 * cps[p] + d;
+        const double dg = vals[rowptr[r] + 3 * stencil_pos(ix, iy, iz, ix, iy, iz, g.nb) + d];
+        v = dg != 0.0 ? 1.0 / dg : 1.0;
+      }
+    }
+    o[t] = v;
+  }
+}
+
+// z = B^-1 v with the inverted cell blocks: a warp per cell, lane a < bs
+// computes the cell's DOF a (grid-stride over cells).
+__device__ __forceinline__ void cblock_apply(double *__restrict__ z, const double *__restrict__ v,
+                                             const double *__restrict__ inv, const CellGeom &g, int64_t ncell)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cell < ncell; cell += nw) {
+    int64_t cps[8];
+    const int np = cell_points(g, cell, cps);
+    const int bs = 3 * np;
+    if (lane < bs) {
+      const double *row = inv + (size_t)cell * CBS * CBS + (size_t)lane * CBS;
+      double s = 0.0;
+      for (int b = 0; b < bs; b++) s = fma(row[b], v[3 * cps[b / 3] + b % 3], s);
+      z[3 * cps[lane / 3] + lane % 3] = s;
+    }
   }
 }
 

@@ -4,8 +4,10 @@ profilers and quick timings).
     python -m igap4_gb300.run_case --nelem 64,16,16 --prec fp64 --what assemble --reps 2
 
 --what: assemble (residual + tangent), residual, tangent, spmv (after one
-assembly), batch (seeded uneven instances, --ninst of them).  Prints the
-wall time of each repetition after the first.
+assembly), batch (seeded uneven instances, --ninst of them), solve (Newton-
+GMRES from U = 0 with preconditioner --pc: 0 none, 1 Jacobi, 2 point-block
+Jacobi; prints Newton and Krylov iterations).  Prints the wall time of each
+repetition after the first.
 """
 from __future__ import annotations
 
@@ -19,7 +21,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nelem", default="64,16,16")
     ap.add_argument("--prec", default="fp64", choices=["fp64", "split"])
-    ap.add_argument("--what", default="assemble", choices=["assemble", "residual", "tangent", "spmv", "batch"])
+    ap.add_argument("--what", default="assemble",
+                    choices=["assemble", "residual", "tangent", "spmv", "batch", "solve"])
+    ap.add_argument("--pc", type=int, default=1)
+    ap.add_argument("--ksp-rtol", type=float, default=1e-6)
+    ap.add_argument("--abstol", type=float, default=1e-10)
     ap.add_argument("--law", default="lingrad", choices=["lingrad", "gradelast", "gradelasttime"])
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--ninst", type=int, default=32)
@@ -46,6 +52,19 @@ def main():
     y = torch.zeros_like(x)
     if a.what == "spmv":
         A.assemble(U, RR, None)
+    if a.what == "solve":
+        for k in range(a.reps):
+            Z = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+            A.synchronize()
+            t0 = time.perf_counter()
+            st = A.solve(Z, snes_abstol=a.abstol, ksp_rtol=a.ksp_rtol, ksp_restart=100, ksp_max_it=200000,
+                         snes_max_it=20, pc=a.pc, use_graphs=1)
+            A.synchronize()
+            print(f"rep {k}: {1e3 * (time.perf_counter() - t0):.1f} ms, newton {st['newton_its']}, "
+                  f"gmres {st['ksp_its_total']}, |F| {st['fnorm0']:.3e} -> {st['fnorm']:.3e}, "
+                  f"converged {st['converged']}")
+        print(f"elements {A.nelem_total} ndof {A.ndof} nnz {A.nnz} pc {a.pc}")
+        return
     for k in range(a.reps):
         A.synchronize()
         t0 = time.perf_counter()

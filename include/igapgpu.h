@@ -85,7 +85,8 @@ typedef struct {
   double ksp_abstol;
   double ksp_dtol;
   int ksp_max_it;
-  int pc;              /* 0 = none, 1 = Jacobi, 2 = point-block Jacobi (3 x 3 blocks of each control point) */
+  int pc;              /* 0 = none, 1 = Jacobi, 2 = point-block Jacobi (3 x 3 blocks of each control point),
+                          3 = cell-block Jacobi (blocks of 2 x 2 x 2 control points, up to 24 x 24; single lattice) */
   int use_graphs;      /* 1: assembly and GMRES cycles replayed as CUDA graphs */
 } igapgpu_solver_opts;
 

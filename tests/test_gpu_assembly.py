@@ -367,9 +367,12 @@ def test_solution_file_round_trip(law, tmp_path):
 
 
 def test_point_block_jacobi_gmres():
-    """GMRES with 3x3 point-block Jacobi (pc=2) solves the linear beam to the
-    direct solution, in the host-driven and the graph-replayed cycles, in no
-    more iterations than scalar Jacobi."""
+    """GMRES with 3x3 point-block Jacobi (pc=2) and with the 2x2x2-cell block
+    Jacobi (pc=3, blocks up to 24x24, clipped cells at the far faces: 8x3x2
+    elements give 10x5x4 control points) solves the linear beam to the direct
+    solution, in the host-driven and the graph-replayed cycles; point blocks
+    take no more iterations than scalar Jacobi, cell blocks fewer than point
+    blocks."""
     sp = pytest.importorskip("scipy.sparse")
     spl = pytest.importorskip("scipy.sparse.linalg")
     bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
@@ -382,7 +385,7 @@ def test_point_block_jacobi_gmres():
     b = np.random.default_rng(4).standard_normal(A.ndof)
     xs = spl.spsolve(K.tocsc(), b)
     its = {}
-    for pc in (1, 2):
+    for pc in (1, 2, 3):
         for graphs in (0, 1):
             x = np.zeros(A.ndof)
             n, rn = A.ksp_solve(b, x, ksp_rtol=1e-10, ksp_restart=200, ksp_max_it=40000, pc=pc,
@@ -390,8 +393,35 @@ def test_point_block_jacobi_gmres():
             assert np.linalg.norm(K @ x - b) <= 1e-9 * np.linalg.norm(b)
             assert rel(x, xs) <= 1e-6
             its[(pc, graphs)] = n
-    assert its[(2, 0)] == its[(2, 1)]
+    assert its[(2, 0)] == its[(2, 1)] and its[(3, 0)] == its[(3, 1)]
     assert its[(2, 0)] <= its[(1, 0)], its
+    assert its[(3, 0)] < its[(2, 0)], its
+
+
+def test_cell_block_jacobi_newton_static_law():
+    """The static gradient law (indefinite tangents away from the origin):
+    Newton-GMRES with cell-block Jacobi reaches the residual tolerance with no
+    more Krylov iterations than point-block Jacobi; a batch context refuses
+    pc=3."""
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(6, 3, 3), L=(2.0, 1.0, 1.0), law=po.LAW_GRADELAST, perturb=True, bc_type=bct,
+                      neumann=neu)
+    kits = {}
+    for pc in (2, 3):
+        A = gpu_case(prob)
+        U = np.zeros(A.ndof)
+        st = A.solve(U, snes_abstol=1e-10, ksp_rtol=1e-8, ksp_restart=100, ksp_max_it=100000, snes_max_it=20,
+                     pc=pc, use_graphs=1)
+        assert st["converged"] == 1, st
+        assert np.linalg.norm(A.residual(U.copy())) <= 1e-10
+        kits[pc] = st["ksp_its_total"]
+        A.close()
+    assert kits[3] <= kits[2], kits
+    insts = [dict(nelem=(3, 2, 2), knots=k, w=w, X=X, par=(1, 1, 0.1, 0, 0, 0, 0, 0, 0), bc_type=bct, neumann=neu)
+             for (k, w, X) in [ig.beam_mesh((3, 2, 2), (2.0, 1.0, 1.0))]]
+    B = ig.BatchAssembly(insts, law=ig.LAW_LINGRAD)
+    with pytest.raises(ig.IgapGpuError):
+        B.solve(np.zeros(B.ndof), pc=3, use_graphs=0)
 
 
 def field_close(F, G, tol=1e-12):
