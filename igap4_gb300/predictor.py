@@ -2,13 +2,16 @@
 reference; an addition to its solver path).
 
 A 3-D convolutional network on the control-point lattice predicts the next
-displacement increment from (u_n, u_{n-1}, load increment).  It is a
-correction to linear extrapolation,
+displacement increment.  It is a correction to linear extrapolation
+u_ext = u_n + (u_n - u_{n-1}),
 
-    guess = u_n + (u_n - u_{n-1}) + s_out * net([u_n / s_u, u_{n-1} / s_u, dload / s_l]),
+    guess = u_ext + s_out * net([u_n / s_u, u_{n-1} / s_u, c / s_c]),
 
-with the last layer initialised to zero, so an untrained network reproduces
-the extrapolation.  The network's forward, backward and Adam step are the
+where the third input block c is either the load increment (the same vector
+at every point) or the residual F(u_ext) of the step's equations at the
+extrapolation (per point: what Newton's first correction would remove), and
+the last layer starts at zero, so an untrained network reproduces the
+extrapolation.  The network's forward, backward and Adam step are the
 library's own kernels (igapgpu_net_*); torch is used here only to hold device
 buffers and to pack the 9 input channels.
 """
@@ -115,36 +118,55 @@ class ConvNet:
 @dataclass
 class Scales:
     u: float = 1.0
-    load: float = 1.0
+    load: float = 1.0   # scale of the third input block (load increment or residual)
     out: float = 1.0
+    mode: str = "load"  # third input block: "load" increment or "residual" F(u_ext)
 
 
-def features(u_n, u_nm1, dload, scales: Scales):
-    """[P, 9] float32 input channels from device DOF vectors (3 per point)."""
+def features(u_n, u_nm1, third, scales: Scales):
+    """[P, 9] float32 input channels from device DOF vectors (3 per point);
+    third: the load increment (3 values) or a residual DOF vector."""
     import torch
 
     P = u_n.numel() // 3
     x = torch.empty((P, 9), dtype=torch.float32, device=u_n.device)
     x[:, 0:3] = (u_n.view(P, 3) / scales.u).float()
     x[:, 3:6] = (u_nm1.view(P, 3) / scales.u).float()
-    x[:, 6:9] = torch.as_tensor(np.asarray(dload, np.float32) / scales.load, device=u_n.device)
+    if scales.mode == "residual":
+        x[:, 6:9] = (torch.as_tensor(third, device=u_n.device).view(P, 3) / scales.load).float()
+    else:
+        x[:, 6:9] = torch.as_tensor(np.asarray(third, np.float32) / scales.load, device=u_n.device)
     return x
 
 
 class LearnedPredictor:
     """Callable (u_n, u_{n-1}, dload) -> guess for u_{n+1} (device float64)."""
 
-    def __init__(self, net: ConvNet, scales: Scales, dload_dir=(0.0, 0.0, 1.0), scaled: bool = False):
+    def __init__(self, net: ConvNet, scales: Scales, dload_dir=(0.0, 0.0, 1.0), scaled: bool = False, A=None):
         import torch
 
+        if scales.mode == "residual" and A is None:
+            raise ValueError("a residual-input predictor needs the Assembly (A=...)")
+        self.A = A
         self.scaled = scaled
         self.net = net
         self.scales = scales
         self.dir = np.asarray(dload_dir, np.float64)
         self.out = torch.empty((1, net.P, 3), dtype=torch.float32, device="cuda")
+        self.F = None
 
     def correction(self, u_n, u_nm1, dload_scalar):
-        x = features(u_n, u_nm1, self.dir * dload_scalar, self.scales)[None]
+        if self.scales.mode == "residual":
+            # residual of this step's equations (history levels and load set by
+            # the transient driver) at the extrapolation
+            if self.F is None or self.F.numel() != u_n.numel():
+                import torch
+
+                self.F = torch.zeros_like(u_n)
+            self.A.residual((u_n + (u_n - u_nm1)).contiguous(), self.F)
+            x = features(u_n, u_nm1, self.F, self.scales)[None]
+        else:
+            x = features(u_n, u_nm1, self.dir * dload_scalar, self.scales)[None]
         self.net.forward(x, self.out)
         return self.out.view(-1).double() * self.scales.out
 

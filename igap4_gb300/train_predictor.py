@@ -39,7 +39,7 @@ def generate(A, seeds, nsteps, dt, amax, opts=None):
         load = TipLoad(seed=int(s), amax=amax)
         states, recs = run_transient(A, load, nsteps, dt, opts=opts)
         loads = np.array([0.0] + [load.value((n + 1) * dt) for n in range(nsteps)])
-        trajs.append((states, loads, recs))
+        trajs.append((states, loads, recs, load))
     return trajs
 
 
@@ -47,27 +47,49 @@ def build_dataset(trajs):
     from .predictor import make_samples
 
     X, Y = [], []
-    for states, loads, _ in trajs:
+    for states, loads, _, _ in trajs:
         x, y = make_samples(states, loads, None)
         X += x
         Y += y
     return X, Y
 
 
-def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None):
+def residual_inputs(A, trajs, dt):
+    """For every sample of build_dataset (same order): the residual of the
+    step's equations at the extrapolation 2 u_n - u_{n-1}, with the history
+    levels and the load of that step (what the transient driver sees when it
+    asks the predictor)."""
+    R = []
+    for states, _, _, load in trajs:
+        for n in range(1, len(states) - 1):
+            A.set_history(1, np.ascontiguousarray(states[n]))
+            A.set_history(2, np.ascontiguousarray(states[n - 1]))
+            A.set_neumann(load.table((n + 1) * dt))
+            R.append(A.residual(np.ascontiguousarray(2.0 * states[n] - states[n - 1])).copy())
+    return R
+
+
+def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None, R=None):
+    """Adam on the samples; R (residual inputs, residual_inputs()) selects
+    the residual-input network, else the load-increment input."""
     import torch
 
     from .predictor import ConvNet, Scales, features
 
     lattice = tuple(n + 2 for n in A.nelem)
     su = max(1e-30, max(np.abs(x[0]).max() for x in X))
-    sl = max(1e-30, max(np.abs(x[2]).max() for x in X))
     so = max(1e-30, max(np.abs(y).max() for y in Y))
-    scales = Scales(u=su, load=sl, out=so)
+    if R is not None:
+        scales = Scales(u=su, load=max(1e-30, max(np.abs(r).max() for r in R)), out=so, mode="residual")
+        thirds = R
+    else:
+        scales = Scales(u=su, load=max(1e-30, max(np.abs(x[2]).max() for x in X)), out=so)
+        thirds = [x[2] for x in X]
     P = int(np.prod(lattice))
     dev = torch.device("cuda")
-    feats = torch.stack([features(torch.tensor(x[0], device=dev), torch.tensor(x[1], device=dev), x[2], scales)
-                         for x in X])
+    feats = torch.stack([features(torch.tensor(x[0], device=dev), torch.tensor(x[1], device=dev),
+                                  torch.tensor(t, device=dev) if R is not None else t, scales)
+                         for x, t in zip(X, thirds)])
     targ = torch.stack([torch.tensor(y / so, dtype=torch.float32, device=dev).view(P, 3) for y in Y])
     net = ConvNet(lattice, batch_max=batch, storage=storage, seed=seed)
     rng = np.random.default_rng(seed)
@@ -109,6 +131,8 @@ def main():
     ap.add_argument("--amax", type=float, default=1e-3)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval-nelem", default=None, help="evaluate on another mesh (default: same)")
+    ap.add_argument("--features", default="load", choices=["load", "residual", "both"],
+                    help="third input block of the network: load increment, residual at the extrapolation")
     ap.add_argument("--compare-shortened", action="store_true",
                     help="also evaluate the best of the guess and two shortened steps along its correction")
     a = ap.parse_args()
@@ -123,31 +147,41 @@ def main():
     trajs = generate(A, range(1000, 1000 + a.train), a.steps, a.dt, a.amax, opts)
     t_gen = time.perf_counter() - t0
     X, Y = build_dataset(trajs)
-    t0 = time.perf_counter()
-    net, scales, hist = train(A, X, Y, epochs=a.epochs)
-    t_train = time.perf_counter() - t0
+    modes = ["load", "residual"] if a.features == "both" else [a.features]
+    R = residual_inputs(A, trajs, a.dt) if "residual" in modes else None
+    nets, t_train = {}, {}
+    for mode in modes:
+        t0 = time.perf_counter()
+        nets[mode] = train(A, X, Y, epochs=a.epochs, R=R if mode == "residual" else None)
+        t_train[mode] = time.perf_counter() - t0
     if a.eval_nelem:
         A.close()
         A, _ = transient_problem(tuple(int(v) for v in a.eval_nelem.split(",")), a.dt)
         from .predictor import ConvNet
 
         lattice = tuple(n + 2 for n in A.nelem)
-        net = ConvNet(lattice, batch_max=1, storage="bf16", params=net.get_params())
+        nets = {m: (ConvNet(lattice, batch_max=1, storage="bf16", params=net.get_params()), sc, h)
+                for m, (net, sc, h) in nets.items()}
     seeds = range(5000, 5000 + a.test)
     plain = evaluate(A, seeds, a.steps, a.dt, a.amax, None, opts)
-    from .predictor import init_params
+    from .predictor import ConvNet, Scales, init_params
 
-    extrap_net = type(net)(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
-    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, scales, scaled=False), opts)
-    learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales), opts)
-    shortened = (evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, scaled=True), opts)
-                 if a.compare_shortened else None)
+    extrap_net = ConvNet(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
+    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, Scales(), scaled=False), opts)
     out = {"train_mesh": list(nelem), "eval_mesh": list(A.nelem), "train_trajectories": a.train,
-           "steps": a.steps, "samples": len(X), "generation_s": t_gen, "training_s": t_train,
-           "loss_first": hist[0], "loss_last": hist[-1], "plain": plain,
-           "extrapolation_only": extrap, "learned": learned, "learned_best_of_shortened": shortened,
-           "time_ratio_learned_vs_plain": learned["seconds_per_step"] / plain["seconds_per_step"],
-           "its_ratio_learned_vs_plain": learned["newton_its_per_step"] / plain["newton_its_per_step"]}
+           "steps": a.steps, "samples": len(X), "generation_s": t_gen, "plain": plain,
+           "extrapolation_only": extrap}
+    for mode, (net, scales, hist) in nets.items():
+        learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, A=A), opts)
+        key = "learned" if mode == modes[-1] else f"learned_{mode}"
+        out[key] = learned
+        out[key + "_training"] = {"inputs": mode, "seconds": t_train[mode], "loss_first": hist[0],
+                                  "loss_last": hist[-1]}
+        if a.compare_shortened:
+            out[key + "_best_of_shortened"] = evaluate(A, seeds, a.steps, a.dt, a.amax,
+                                                       LearnedPredictor(net, scales, scaled=True, A=A), opts)
+    out["time_ratio_learned_vs_plain"] = out["learned"]["seconds_per_step"] / plain["seconds_per_step"]
+    out["its_ratio_learned_vs_plain"] = out["learned"]["newton_its_per_step"] / plain["newton_its_per_step"]
     print(json.dumps(out))
 
 
