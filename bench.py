@@ -141,6 +141,7 @@ def run_reference(a):
         "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} residual+tangent assembly, CPU",
                    "law": "linear strain gradient lambda=mu=1 ell=0.1", "sample": sample},
         "cpu_baseline": {"value": value, "unit": "elements/s", "cores": cores, "kind": "port",
+                         "per_core": value / cores,
                          "sample": sample},
         "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -303,7 +304,7 @@ def main():
         # spawn-based pool before any CUDA call
         cores = os.cpu_count() or 1
         r, nel, slowest, wall = cpu_rate(a.cpu_seconds, cores)
-        cpu = {"value": r, "unit": "elements/s", "cores": cores, "kind": "port",
+        cpu = {"value": r, "unit": "elements/s", "cores": cores, "kind": "port", "per_core": r / cores,
                "sample": f"{cores} concurrent single-threaded processes x {nel} elements each "
                          f"(residual+tangent, p=2, 64 points, linear law; oracle port of the "
                          f"reference loop) on a 32x8x8 beam; {slowest:.1f} s"}
