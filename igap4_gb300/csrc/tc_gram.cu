@@ -80,10 +80,10 @@ __device__ __forceinline__ double f32_to_f64(float f)
 // colour order (the same sums, bit for bit, as a read-modify-write).
 template <typename PosT>
 __device__ __forceinline__ void gram_scatter(const float *G, const int64_t *rowp, const PosT *pos, const DevLaw &L,
-                                             double *__restrict__ vals)
+                                             double *__restrict__ vals, int first = -1, int nthreads = G_THREADS)
 {
   const float lam = (float)L.par[0], mu = (float)L.par[1];
-  for (int t = threadIdx.x; t < NE * NE; t += G_THREADS) {
+  for (int t = first < 0 ? (int)threadIdx.x : first; t < NE * NE; t += nthreads) {
     const int rr = t / NE, cc = t - NE * rr;
     const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
     float kk = lam * G[(3 * b + d) * GPAD + 3 * c + e] + mu * G[(3 * b + e) * GPAD + 3 * c + d];
@@ -729,6 +729,270 @@ __global__ void __launch_bounds__(G_THREADS, MINB) tcs_batch_kernel(BatchArgs ba
   tcs_teardown(S, st, ba.err);
 }
 
+
+// ------------------------------------------------ warp-specialised variant
+// The cached-operand tangent with its stages on separate warps, so that the
+// copies, the TF32 split, the MMAs and the scatter of different chunks and
+// elements overlap inside one CTA (two CTAs per SM, two TMEM accumulators):
+//   warp 0 (one thread): bulk copies of the chunk stream into W_NS stages,
+//   warps 2-3: TF32 split of a staged chunk into a free operand buffer,
+//   warp 1 (one thread): the 12 MMAs of a chunk into the element's accumulator,
+//   warps 4-7: epilogue of the previous element (TMEM -> G -> K -> L2 reductions).
+// Hand-offs are mbarriers (full/empty per copy stage, opfull/opempty per
+// operand buffer, accfull/accempty per accumulator); every wait is bounded and
+// gives up early once another role has aborted.
+constexpr int W_NS = 2;
+constexpr uint32_t W_TMEM_COLS = 256;  // two accumulators of 128 columns
+
+struct TcwSmem {
+  unsigned char op[2][2][S_OP_BYTES];  // [buffer][hi, lo]
+  unsigned char val[W_NS][S_CH_BYTES]; // copy stages
+  float G[GROWS * GPAD];               // epilogue staging
+  unsigned char pos[NB * NB];
+  int64_t rowp[NE];
+  uint64_t full[W_NS], empty[W_NS], opfull[2], opempty[2], accfull[2], accempty[2];
+  uint32_t cp_n[W_NS], ope_n[2], accf_n[2];  // issue counts for the teardown
+  uint32_t taddr;
+  int abort;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(mbar)) : "memory");
+}
+
+// Bounded wait that also returns (false) once another role set the abort flag.
+__device__ __forceinline__ bool tcw_wait(uint64_t *mbar, uint32_t parity, volatile int *abort)
+{
+  const uint32_t addr = tc::smem_u32(mbar);
+  for (uint32_t it = 0; it < G_WAIT_LIMIT; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255u) == 255u && *abort) return false;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(G_THREADS, 2)
+    tcw_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
+               int *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcwSmem &S = *reinterpret_cast<TcwSmem *>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  volatile int *abort = &S.abort;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, W_TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < W_NS; i++) {
+      tc::mbar_init(&S.full[i], 1);
+      tc::mbar_init(&S.empty[i], 64);
+      S.cp_n[i] = 0;
+    }
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&S.opfull[i], 64);
+      tc::mbar_init(&S.opempty[i], 1);
+      tc::mbar_init(&S.accfull[i], 1);
+      tc::mbar_init(&S.accempty[i], 128);
+      S.ope_n[i] = S.accf_n[i] = 0;
+    }
+    S.abort = 0;
+  }
+  for (int i = tid; i < (int)(sizeof(S.op) / 4); i += G_THREADS) reinterpret_cast<float *>(&S.op[0][0][0])[i] = 0.f;
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = S.taddr;
+  const int nelem_c = ncx * ncy * ncz;
+  const int nmine = (int)blockIdx.x < nelem_c ? (nelem_c - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const uint32_t nchunk = (uint32_t)((m.npts + PW - 1) / PW);
+  const size_t ebytes = (size_t)nchunk * S_CH_BYTES;
+  auto element = [&](int j, int &ex, int &ey, int &ez) {
+    const int ei = (int)blockIdx.x + j * (int)gridDim.x;
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    ex = cx + 3 * ix;
+    ey = cy + 3 * iy;
+    ez = cz + 3 * iz;
+    return ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+  };
+  if (warp == 0) {
+    if (lane == 0) {  // producer
+      const unsigned char *cache = reinterpret_cast<const unsigned char *>(m.gop);
+      uint32_t s = 0, cpn[W_NS] = {};
+      bool ok = true;
+      for (int j = 0; j < nmine && ok; j++) {
+        int ex, ey, ez;
+        const unsigned char *src = cache + (size_t)element(j, ex, ey, ez) * ebytes;
+        for (uint32_t c = 0; c < nchunk; c++, s++) {
+          const int st = (int)(s % W_NS);
+          if (s >= (uint32_t)W_NS && !tcw_wait(&S.empty[st], ((s / W_NS) - 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&S.full[st], (uint32_t)S_CH_BYTES);
+          tc::bulk_g2s(S.val[st], src + (size_t)c * S_CH_BYTES, (uint32_t)S_CH_BYTES, &S.full[st]);
+          cpn[st]++;
+        }
+      }
+      if (!ok) S.abort = 1;
+      for (int i = 0; i < W_NS; i++) S.cp_n[i] = cpn[i];
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = tc::instr_desc(2, 128, GN);
+      const uint32_t op_base = tc::smem_u32(&S.op[0][0][0]);
+      uint32_t s = 0, open[2] = {0, 0}, accn[2] = {0, 0};
+      bool ok = true;
+      for (int j = 0; j < nmine && ok; j++) {
+        const int a = j & 1;
+        if (j >= 2 && !tcw_wait(&S.accempty[a], ((uint32_t)(j / 2) - 1) & 1, abort)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t dacc = taddr + (uint32_t)(a * 128);
+        for (uint32_t c = 0; c < nchunk; c++, s++) {
+          const int b = (int)(s & 1);
+          if (!tcw_wait(&S.opfull[b], (s / 2) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t hb = op_base + (uint32_t)(b * 2 * S_OP_BYTES), lb = hb + (uint32_t)S_OP_BYTES;
+          for (int ks = 0; ks < GKS; ks++)
+            for (int pp = 0; pp < 3; pp++) {  // hi.hi, hi.lo, lo.hi
+              const uint32_t ad = (pp == 2 ? lb : hb) + (uint32_t)(ks * S_KS_BYTES);
+              const uint32_t bd = (pp == 1 ? lb : hb) + (uint32_t)(ks * S_KS_BYTES);
+              tc::mma_tf32(dacc, tc::smem_desc(ad, 128, 256), tc::smem_desc(bd, 128, 256), idesc,
+                           (c == 0 && ks == 0 && pp == 0) ? 0u : 1u);
+            }
+          tc::mma_commit(&S.opempty[b]);
+          open[b]++;
+        }
+        if (!ok) break;
+        tc::mma_commit(&S.accfull[a]);
+        accn[a]++;
+      }
+      if (!ok) S.abort = 1;
+      for (int i = 0; i < 2; i++) {
+        S.ope_n[i] = open[i];
+        S.accf_n[i] = accn[i];
+      }
+    }
+  } else if (warp < 4) {  // TF32 split, 64 threads
+    const int t = tid - 64;
+    uint32_t s = 0;
+    bool ok = true;
+    for (int j = 0; j < nmine && ok; j++)
+      for (uint32_t c = 0; c < nchunk; c++, s++) {
+        const int st = (int)(s % W_NS), b = (int)(s & 1);
+        if (!tcw_wait(&S.full[st], (s / W_NS) & 1, abort) ||
+            (s >= 2 && !tcw_wait(&S.opempty[b], ((s / 2) - 1) & 1, abort))) {
+          ok = false;
+          break;
+        }
+        const float4 *src = reinterpret_cast<const float4 *>(S.val[st]);
+        float4 *hi = reinterpret_cast<float4 *>(S.op[b][0]);
+        float4 *lo = reinterpret_cast<float4 *>(S.op[b][1]);
+        for (int i = t; i < S_CH_BYTES / 16; i += 64) {
+          const float4 v = src[i];
+          float4 h, l;
+          h.x = tc::to_tf32(v.x);
+          h.y = tc::to_tf32(v.y);
+          h.z = tc::to_tf32(v.z);
+          h.w = tc::to_tf32(v.w);
+          l.x = tc::to_tf32(v.x - h.x);
+          l.y = tc::to_tf32(v.y - h.y);
+          l.z = tc::to_tf32(v.z - h.z);
+          l.w = tc::to_tf32(v.w - h.w);
+          hi[i] = h;
+          lo[i] = l;
+        }
+        tc::fence_proxy_async();  // the MMAs read the operands through the async proxy
+        mbar_arrive(&S.empty[st]);
+        mbar_arrive(&S.opfull[b]);
+      }
+    if (!ok) S.abort = 1;
+  } else {  // epilogue, 128 threads: warp & 3 is the TMEM lane quarter
+    const int t = tid - 128, quarter = warp & 3;
+    const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+    const int nbv[3] = {m.nbasis[0], nb1, nb2};
+    bool ok = true;
+    for (int j = 0; j < nmine && ok; j++) {
+      const int a = j & 1;
+      int ex, ey, ez;
+      element(j, ex, ey, ez);
+      if (t < NE) {
+        const int b = t / 3, dd = t % 3;
+        const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+        S.rowp[t] = __ldg(m.rowptr + 3 * cpb + dd);
+      }
+      for (int i = t; i < NB * NB; i += 128) {
+        const int b = i / NB, c = i % NB;
+        S.pos[i] = (unsigned char)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9,
+                                              ey + (c / 3) % 3, ez + c % 3, nbv);
+      }
+      // the four epilogue warps take the same decision (a named-barrier OR):
+      // a thread that gave up must not leave the others at a named barrier
+      const uint32_t got = tcw_wait(&S.accfull[a], ((uint32_t)j / 2) & 1, abort) ? 1u : 0u;
+      uint32_t any_failed;
+      asm volatile(
+          "{\n\t.reg .pred p, q;\n\t"
+          "setp.eq.u32 p, %1, 0;\n\t"
+          "bar.red.or.pred q, 1, 128, p;\n\t"
+          "selp.u32 %0, 1, 0, q;\n\t}\n"
+          : "=r"(any_failed)
+          : "r"(got)
+          : "memory");
+      if (any_failed) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const int r = quarter * 32 + lane;
+      for (int cb = 0; cb < 3; cb++) {
+        uint32_t v[32];
+        tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128 + cb * 32), v);
+        if (r < GROWS)
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++)
+            if (cb * 32 + jj < GROWS) S.G[r * GPAD + cb * 32 + jj] = __uint_as_float(v[jj]);
+      }
+      tc::fence_before_sync();
+      mbar_arrive(&S.accempty[a]);
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // G, rowp, pos of the element complete
+      gram_scatter(S.G, S.rowp, S.pos, L, vals, t, 128);
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // before the next element overwrites them
+    }
+    if (!ok) S.abort = 1;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort) {
+    if (tid == 0) {
+      for (int i = 0; i < W_NS; i++)
+        if (S.cp_n[i] > 0) tc::mbar_wait(&S.full[i], (S.cp_n[i] - 1) & 1, G_WAIT_LIMIT);
+      for (int i = 0; i < 2; i++) {
+        if (S.ope_n[i] > 0) tc::mbar_wait(&S.opempty[i], (S.ope_n[i] - 1) & 1, G_WAIT_LIMIT);
+        if (S.accf_n[i] > 0) tc::mbar_wait(&S.accfull[i], (S.accf_n[i] - 1) & 1, G_WAIT_LIMIT);
+      }
+      atomicCAS(err, 0, 2);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, W_TMEM_COLS);
+}
+
 // ------------------------------------------------------------- launches
 static size_t tcg_smem() { return sizeof(TcgSmem) + 1024; }
 template <int NS>
@@ -836,8 +1100,52 @@ static int launch_tc_gop_cfg(Context *c, double *vals)
   return IGAPGPU_OK;
 }
 
+static int launch_tc_gop_ws(Context *c, double *vals)
+{
+  const DevMesh m = c->devmesh();
+  const DevLaw L = c->devlaw();
+  const size_t smem = sizeof(TcwSmem) + 1024;
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  for (int cx = 0; cx < 3; cx++)
+    for (int cy = 0; cy < 3; cy++)
+      for (int cz = 0; cz < 3; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        const int nel = ncx * ncy * ncz;
+        if (nel <= 0) continue;
+        const int grid = nel < 2 * nsm ? nel : 2 * nsm;
+        tcw_kernel<<<grid, G_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
+        count_launch();
+        IGAP_CHECK_LAUNCH();
+        if (c->prof) {
+          c->prof_launches[1]++;
+          c->prof_elements[1] += nel;
+        }
+      }
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[1].emplace_back(e0, e1);
+  }
+  return IGAPGPU_OK;
+}
+
 static int launch_tc_gop(Context *c, double *vals)
 {
+  const char *ws = getenv("IGAPGPU_TCS_WS");
+  if (ws && ws[0] == '1') return launch_tc_gop_ws(c, vals);
   return tcs_ctas_per_sm() == 3 ? launch_tc_gop_cfg<2, 3>(c, vals) : launch_tc_gop_cfg<4, 2>(c, vals);
 }
 
