@@ -401,8 +401,9 @@ def main():
                  "tangent_rel_err_vs_fp64": err, "dtype": "tf32x3/f32-acc tangent, f64 residual",
                  "tc_kernel_ms_per_step": tc_ms / a.steps, "fp64_residual_kernel_ms_per_step": res_ms / a.steps,
                  "roofline": {"bound": "tensor",
-                              "kernel": ("tcs_kernel (cached sqrt(w)-weighted Gram operands, one bulk copy per "
-                                         "chunk; tcgen05.mma kind::tf32, TF32x3)") if cached else
+                              "kernel": ("tcw_kernel (cached sqrt(w)-weighted Gram operands, one bulk copy per "
+                                         "chunk, warp-specialised copy/split/MMA/scatter; tcgen05.mma kind::tf32, "
+                                         "TF32x3)") if cached else
                                         "tcg_kernel (tcgen05.mma kind::tf32, TF32x3, Gram form)",
                               "achieved": tc_ach, "peak": bf16_peak, "unit": "TFLOP/s",
                               "frac": tc_ach / bf16_peak,

@@ -109,6 +109,7 @@ def test_warp_specialised_tangent_bit_identical(monkeypatch):
     A = ig.Assembly((9, 4, 5), knots, w, X, law=ig.LAW_LINGRAD, par=(1.1, 0.9, 0.08), bc_type=bct, neumann=neu)
     A.set_precision(ig.PREC_SPLIT)
     U = np.random.default_rng(8).uniform(-1e-2, 1e-2, A.ndof)
+    monkeypatch.setenv("IGAPGPU_TCS_WS", "0")
     K1 = A.tangent(U.copy())
     monkeypatch.setenv("IGAPGPU_TCS_WS", "1")
     K2 = A.tangent(U.copy())
