@@ -1057,16 +1057,20 @@ int ensure_gram_operands(Context *c)
   return IGAPGPU_OK;
 }
 
-template <int NS, int MINB>
-static int launch_tc_gop_cfg(Context *c, double *vals)
+// One persistent launch per colour of a Gram-form tangent kernel: `kern`
+// with `smem` dynamic shared memory and `ctas` CTAs per SM (fewer when the
+// colour has fewer elements), timed as one tensor-core kernel group when
+// profiling is on.  `attr_set` (one per kernel, owned by the caller) records
+// that the kernel's shared-memory limit was raised, once, before any graph
+// capture can reach this call.
+template <typename Kern>
+static int launch_colours(Context *c, Kern kern, size_t smem, int ctas, double *vals, bool &attr_set)
 {
   const DevMesh m = c->devmesh();
   const DevLaw L = c->devlaw();
-  auto kern = tcs_kernel<NS, MINB>;
-  static bool attr = false;
-  if (!attr) {
-    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcs_smem<NS>()));
-    attr = true;
+  if (!attr_set) {
+    IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
   }
   int dev = 0, nsm = 0;
   IGAP_CUDA(cudaGetDevice(&dev));
@@ -1084,8 +1088,8 @@ static int launch_tc_gop_cfg(Context *c, double *vals)
                   ncz = (c->nelem[2] - cz + 2) / 3;
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
-        const int grid = nel < MINB * nsm ? nel : MINB * nsm;  // MINB persistent CTAs per SM
-        kern<<<grid, G_THREADS, tcs_smem<NS>(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
+        const int grid = nel < ctas * nsm ? nel : ctas * nsm;
+        kern<<<grid, G_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
         count_launch();
         IGAP_CHECK_LAUNCH();
         if (c->prof) {
@@ -1100,46 +1104,17 @@ static int launch_tc_gop_cfg(Context *c, double *vals)
   return IGAPGPU_OK;
 }
 
+template <int NS, int MINB>
+static int launch_tc_gop_cfg(Context *c, double *vals)
+{
+  static bool attr = false;
+  return launch_colours(c, tcs_kernel<NS, MINB>, tcs_smem<NS>(), MINB, vals, attr);
+}
+
 static int launch_tc_gop_ws(Context *c, double *vals)
 {
-  const DevMesh m = c->devmesh();
-  const DevLaw L = c->devlaw();
-  const size_t smem = sizeof(TcwSmem) + 1024;
   static bool attr = false;
-  if (!attr) {
-    IGAP_CUDA(cudaFuncSetAttribute(tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
-  int dev = 0, nsm = 0;
-  IGAP_CUDA(cudaGetDevice(&dev));
-  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (c->prof) {
-    IGAP_CUDA(cudaEventCreate(&e0));
-    IGAP_CUDA(cudaEventCreate(&e1));
-    IGAP_CUDA(cudaEventRecord(e0, c->stream));
-  }
-  for (int cx = 0; cx < 3; cx++)
-    for (int cy = 0; cy < 3; cy++)
-      for (int cz = 0; cz < 3; cz++) {
-        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
-                  ncz = (c->nelem[2] - cz + 2) / 3;
-        const int nel = ncx * ncy * ncz;
-        if (nel <= 0) continue;
-        const int grid = nel < 2 * nsm ? nel : 2 * nsm;
-        tcw_kernel<<<grid, G_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
-        count_launch();
-        IGAP_CHECK_LAUNCH();
-        if (c->prof) {
-          c->prof_launches[1]++;
-          c->prof_elements[1] += nel;
-        }
-      }
-  if (c->prof) {
-    IGAP_CUDA(cudaEventRecord(e1, c->stream));
-    c->prof_ev[1].emplace_back(e0, e1);
-  }
-  return IGAPGPU_OK;
+  return launch_colours(c, tcw_kernel, sizeof(TcwSmem) + 1024, 2, vals, attr);
 }
 
 // The warp-specialised kernel by default (6.3 ms per tangent at 128x32x32
@@ -1155,43 +1130,8 @@ static int launch_tc_gop(Context *c, double *vals)
 int launch_tc_gram(Context *c, double *vals)
 {
   if (c->d_gop) return launch_tc_gop(c, vals);
-  const DevMesh m = c->devmesh();
-  const DevLaw L = c->devlaw();
   static bool attr = false;
-  if (!attr) {
-    IGAP_CUDA(cudaFuncSetAttribute(tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg_smem()));
-    attr = true;
-  }
-  int dev = 0, nsm = 0;
-  IGAP_CUDA(cudaGetDevice(&dev));
-  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (c->prof) {
-    IGAP_CUDA(cudaEventCreate(&e0));
-    IGAP_CUDA(cudaEventCreate(&e1));
-    IGAP_CUDA(cudaEventRecord(e0, c->stream));
-  }
-  for (int cx = 0; cx < 3; cx++)
-    for (int cy = 0; cy < 3; cy++)
-      for (int cz = 0; cz < 3; cz++) {
-        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
-                  ncz = (c->nelem[2] - cz + 2) / 3;
-        const int nel = ncx * ncy * ncz;
-        if (nel <= 0) continue;
-        const int grid = nel < 2 * nsm ? nel : 2 * nsm;  // two CTAs per SM
-        tcg_kernel<<<grid, G_THREADS, tcg_smem(), c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err);
-        count_launch();
-        IGAP_CHECK_LAUNCH();
-        if (c->prof) {
-          c->prof_launches[1]++;
-          c->prof_elements[1] += nel;
-        }
-      }
-  if (c->prof) {
-    IGAP_CUDA(cudaEventRecord(e1, c->stream));
-    c->prof_ev[1].emplace_back(e0, e1);
-  }
-  return IGAPGPU_OK;
+  return launch_colours(c, tcg_kernel, tcg_smem(), 2, vals, attr);  // two CTAs per SM
 }
 
 int launch_tc_gram_batch(Context *c, const BatchArgs &a, int nsm, double *vals, bool cached)
