@@ -82,6 +82,7 @@ def lib():
         L.igapgpu_dirichlet.argtypes = [vp, vp, vp, vp]
         L.igapgpu_density.argtypes = [vp, vp, vp]
         L.igapgpu_sample_field.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
+        L.igapgpu_debug_slot_counts.argtypes = [vp, vp]
         L.igapgpu_save_solution.argtypes = [vp, ctypes.c_char_p]
         L.igapgpu_load_solution.argtypes = [vp, ctypes.c_char_p]
         L.igapgpu_impose_dirichlet.argtypes = [vp, vp]
@@ -281,6 +282,13 @@ class Assembly:
         X = np.zeros(shape + (3,))
         _check(lib().igapgpu_sample_field(self.h, int(nppe), _ptr(F), _ptr(xq), _ptr(X), None, None))
         return F, xq, X
+
+    def debug_slot_counts(self):
+        """Per CSR slot, the element contributions a plain read-modify-write
+        scatter (colour by colour) lands in it: the race check of the colouring."""
+        out = np.zeros(self.nnz)
+        _check(lib().igapgpu_debug_slot_counts(self.h, _ptr(out)))
+        return out
 
     def save_solution(self, fname):
         """Write the reference's solution file (IGAPSolvSaveSolution layout)."""

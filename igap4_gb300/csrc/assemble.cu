@@ -952,6 +952,68 @@ int launch_dirichlet_matrix(Context *c, double *vals)
 
 }  // namespace igap
 
+// --------------------------------------------------- scatter race check
+// Every element adds 1 to each of its 81 x 81 CSR slots with a plain
+// read-modify-write, colour by colour, as the element kernels scatter.  Two
+// elements of one colour sharing a slot would lose updates and leave the slot
+// below the number of elements whose support holds both of its control points.
+namespace igap {
+__global__ void slot_count_kernel(DevMesh m, int cx, int cy, int cz, int ncy, int ncz, double *counts)
+{
+  const int b = blockIdx.x;
+  const int iz = b % ncz, iy = (b / ncz) % ncy, ix = b / (ncz * ncy);
+  const int ex = cx + 3 * ix, ey = cy + 3 * iy, ez = cz + 3 * iz;
+  const int nbv[3] = {m.nbasis[0], m.nbasis[1], m.nbasis[2]};
+  for (int t = threadIdx.x; t < NE * NE; t += blockDim.x) {
+    const int rr = t / NE, cc = t % NE;
+    const int pb = rr / 3, d = rr % 3, pc = cc / 3, e = cc % 3;
+    const int rx = ex + pb / 9, ry = ey + (pb / 3) % 3, rz = ez + pb % 3;
+    const int sx = ex + pc / 9, sy = ey + (pc / 3) % 3, sz = ez + pc % 3;
+    const int64_t cpb = ((int64_t)rx * nbv[1] + ry) * nbv[2] + rz;
+    double *slot = counts + m.rowptr[3 * cpb + d] + 3 * stencil_pos(rx, ry, rz, sx, sy, sz, nbv) + e;
+    *slot = *slot + 1.0;
+  }
+}
+}  // namespace igap
+
+extern "C" int igapgpu_debug_slot_counts(igapgpu_t c, double *counts)
+{
+  using namespace igap;
+  if (!c || !counts) return IGAPGPU_ERR_ARG;
+  if (c->batch) {
+    set_error("debug_slot_counts: not available on a batch context");
+    return IGAPGPU_ERR_ARG;
+  }
+  const bool host = !is_device_ptr(counts);
+  double *d = counts;
+  if (host && cudaMalloc(&d, sizeof(double) * (size_t)c->nnz) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("debug_slot_counts: allocation failed");
+    return IGAPGPU_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(double) * (size_t)c->nnz, c->stream);
+  const DevMesh m = c->devmesh();
+  for (int cx = 0; cx < 3 && e == cudaSuccess; cx++)
+    for (int cy = 0; cy < 3 && e == cudaSuccess; cy++)
+      for (int cz = 0; cz < 3 && e == cudaSuccess; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        if (ncx * ncy * ncz <= 0) continue;
+        slot_count_kernel<<<ncx * ncy * ncz, 256, 0, c->stream>>>(m, cx, cy, cz, ncy, ncz, d);
+        count_launch();
+        e = cudaGetLastError();
+      }
+  if (e == cudaSuccess && host)
+    e = cudaMemcpyAsync(counts, d, sizeof(double) * (size_t)c->nnz, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (host) cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error("debug_slot_counts: CUDA error %s", cudaGetErrorString(e));
+    return IGAPGPU_ERR_CUDA;
+  }
+  return IGAPGPU_OK;
+}
+
 // ------------------------------------------------------- FP64 peak probe
 namespace igap {
 __global__ void fp64_peak_kernel(double *out, int iters)

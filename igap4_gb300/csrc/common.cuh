@@ -9,9 +9,20 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "igapgpu.h"
 
 namespace igap {
+
+// NVTX range over an entry point (visible in Nsight timelines; no cost
+// without a tool attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 constexpr int P = 2;                    // B-spline degree handled on the device
 constexpr int P1 = P + 1;               // basis functions per direction per element

@@ -708,19 +708,23 @@ static int assemble_common(igapgpu_t c, const double *U, double *RR, double *val
 
 int igapgpu_residual(igapgpu_t c, const double *U, double *RR)
 {
+  NvtxRange range("igapgpu_residual");
   return assemble_common(c, U, RR, nullptr, true, false);
 }
 int igapgpu_tangent(igapgpu_t c, const double *U, double *vals)
 {
+  NvtxRange range("igapgpu_tangent");
   return assemble_common(c, U, nullptr, vals, false, true);
 }
 int igapgpu_assemble(igapgpu_t c, const double *U, double *RR, double *vals)
 {
+  NvtxRange range("igapgpu_assemble");
   return assemble_common(c, U, RR, vals, true, true);
 }
 
 int igapgpu_matmult(igapgpu_t c, const double *x, double *y)
 {
+  NvtxRange range("igapgpu_matmult");
   if (!c || !x || !y) return IGAPGPU_ERR_ARG;
   if (!c->matrix_valid) {
     set_error("matmult before the tangent was assembled into the context matrix");

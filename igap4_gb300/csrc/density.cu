@@ -397,6 +397,7 @@ using namespace igap;
 
 extern "C" int igapgpu_density(igapgpu_t c, double *HH, int *ndensity)
 {
+  NvtxRange range("igapgpu_density");
   if (!c || !HH) {
     set_error("density: null argument");
     return IGAPGPU_ERR_ARG;
@@ -437,6 +438,7 @@ extern "C" int igapgpu_density(igapgpu_t c, double *HH, int *ndensity)
 extern "C" int igapgpu_sample_field(igapgpu_t c, int nppe, double *field, double *xq, double *X, int *nfield,
                                     int64_t *npoints)
 {
+  NvtxRange range("igapgpu_sample_field");
   if (!c) {
     set_error("sample_field: null context");
     return IGAPGPU_ERR_ARG;

@@ -429,6 +429,7 @@ int igapgpu_get_diagonal(igapgpu_t c, double *diag)
 int igapgpu_ksp_solve(igapgpu_t c, const double *b, double *x, const igapgpu_solver_opts *opts,
                       int *its, double *rnorm)
 {
+  NvtxRange range("igapgpu_ksp_solve");
   if (!c || !b || !x) return IGAPGPU_ERR_ARG;
   if (!c->matrix_valid) {
     set_error("ksp_solve before the tangent was assembled");
@@ -458,6 +459,7 @@ int igapgpu_ksp_solve(igapgpu_t c, const double *b, double *x, const igapgpu_sol
 // Newton with backtracking on 1/2|F|^2 (SNESNEWTONLS + BT, src/interface.c:217-224).
 int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapgpu_solve_stats *st)
 {
+  NvtxRange range("igapgpu_solve");
   if (!c || !U) return IGAPGPU_ERR_ARG;
   igapgpu_solver_opts o;
   if (opts) o = *opts; else igapgpu_default_solver_opts(&o);

@@ -145,6 +145,13 @@ int igapgpu_density(igapgpu_t ctx, double *HH, int *ndensity);
 int igapgpu_sample_field(igapgpu_t ctx, int nppe, double *field, double *xq, double *X, int *nfield,
                          int64_t *npoints);
 
+/* Race check of the colour-partitioned scatter (a debug aid): counts[nnz]
+ * receives, per CSR slot, how many element contributions landed in it when
+ * every element adds 1 to each of its slots with a plain read-modify-write,
+ * colour by colour.  Without lost updates that is the number of elements
+ * whose support holds both control points of the slot.  Host or device. */
+int igapgpu_debug_slot_counts(igapgpu_t ctx, double *counts);
+
 /* IGAPSolvSaveSolution / IGAPSolvLoadSolution (src/interface.c:271-300): the
  * reference's solution file (write_solution / read_solution, src/ioutil.c:
  * 90-159), raw FP64 levels in DOF order; static laws level 0, the transient

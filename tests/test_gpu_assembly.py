@@ -473,3 +473,16 @@ def test_field_sampling_vs_oracle_device_buffers(law):
     np.testing.assert_array_equal(dX.cpu().numpy(), X)
     with pytest.raises(ig.IgapGpuError):
         A.sample_field(0)
+
+
+def test_colour_scatter_has_no_lost_updates():
+    """Race check of the colour-partitioned scatter on the GPU: with a plain
+    read-modify-write per slot, colour by colour, every CSR slot ends at the
+    number of elements whose support holds both of its control points."""
+    from slot_counts import explicit_counts
+
+    for nelem in ((5, 4, 3), (7, 3, 4)):
+        A = gpu_case(po.Problem(nelem=nelem, law=po.LAW_LINGRAD, perturb=True))
+        rowptr, cols = A.pattern()
+        np.testing.assert_array_equal(A.debug_slot_counts(), explicit_counts(nelem, rowptr, cols))
+        A.close()

@@ -311,3 +311,17 @@ def test_field_sampling_linear_state_known_answer():
     k0, k1 = 0.75, 1.0  # last knot span in x
     assert xq[0, 0, 0, 0] == 1e-15
     assert xq[-1, 0, 0, 0] == k0 + 1e-15 + (k1 - k0) * 2 / 2 - 2 * 1e-15 * 1 and xq[-1, 0, 0, 0] < 1.0
+
+
+def test_slot_multiplicity_formula():
+    """The expected CSR slot multiplicities of the scatter race check: the
+    closed form equals an explicit element loop over the oracle's pattern, and
+    every slot of the full-stencil pattern is touched by at least one element."""
+    from slot_counts import explicit_counts, formula_counts
+
+    for nelem in ((3, 2, 2), (5, 4, 3), (1, 1, 2)):
+        case = po.OracleCase(po.Problem(nelem=nelem, law=po.LAW_LINGRAD))
+        rowptr, cols = case.pattern()
+        ex = explicit_counts(nelem, rowptr, cols)
+        np.testing.assert_array_equal(ex, formula_counts(nelem, rowptr, cols))
+        assert ex.min() >= 1 and ex.max() == np.prod([min(3, n) for n in nelem])
