@@ -17,6 +17,11 @@
  * Errors: every entry point returns IGAPGPU_OK (0) or a negative code; the
  * text of the last error is available from igapgpu_last_error().  There is no
  * CPU fallback: without a usable GPU, igapgpu_assm_init fails.
+ *
+ * Threads: a context is used by one host thread at a time (as IGAP4 drives
+ * its Core from one thread per rank); distinct contexts on distinct streams
+ * may run concurrently, but the first call of each kernel kind sets its
+ * shared-memory limit once, so make one call per kind before going parallel.
  */
 #ifndef IGAPGPU_H
 #define IGAPGPU_H
