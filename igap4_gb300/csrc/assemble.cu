@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "laws.cuh"
 #include "element.cuh"
+#include "law_thread.cuh"
 
 namespace igap {
 
@@ -604,17 +605,115 @@ __global__ void __launch_bounds__(PW * 32, 1)
   __syncthreads();
   const int q0 = ch * PW;
   const int nv = m.npts - q0 < PW ? m.npts - q0 : PW;
-  const int64_t p0 = e * m.npts + q0;
+  // point-minor layout: [element][entry][point]
   if (RES)
-    for (int i = tid; i < nv * 30; i += PW * 32) preR[p0 * 30 + i] = S.rr[i / 30][i % 30];
+    for (int i = tid; i < nv * 30; i += PW * 32)
+      preR[(e * 30 + i % 30) * m.npts + q0 + i / 30] = S.rr[i / 30][i % 30];
   if (TAN)
-    for (int i = tid; i < nv * 900; i += PW * 32) preD[p0 * 900 + i] = S.D[i / 900][i % 900];
+    for (int i = tid; i < nv * 900; i += PW * 32)
+      preD[(e * 900 + i % 900) * m.npts + q0 + i / 900] = S.D[i / 900][i % 900];
+}
+
+// ------------------------------------- law at every point, a thread per point
+// Needs the geometry cache.  Phase 1 (a warp per point, 32 points per warp):
+// the point's physical basis comes from the cache, the lanes of the 30 slots
+// interpolate every history level (src/assmcore_iga.c:209-229, same order as
+// point_setup) and store the law's inputs column-wise in shared memory.
+// Phase 2: each thread evaluates its point's law (gradelast_point) and writes
+// the weighted outputs in the point-minor layout [element][entry][point], so
+// that a warp's stores are contiguous.
+constexpr int LT_NT = 128;
+struct LawThreadSmem {
+  double sm[30 * LT_NT];
+  double sd[30 * LT_NT];
+  double wt[LT_NT];
+  double R[LT_NT / 32][GEO_STRIDE];
+  double U[LT_NT / 32][3 * NE];
+};
+
+template <int LAWK, bool RES, bool TAN>
+__global__ void __launch_bounds__(LT_NT)
+    law_thread_kernel(DevMesh m, DevLaw L, const double *__restrict__ Uhist, double *__restrict__ preR,
+                      double *__restrict__ preD, int64_t npt_total)
+{
+  constexpr bool TR = LAWK == 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LawThreadSmem &S = *reinterpret_cast<LawThreadSmem *>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t p0 = (int64_t)blockIdx.x * LT_NT;
+  const int nh = L.nhist;
+  const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+  const double rho_m = L.par[5], damp = L.par[6], dt = L.par[7];
+  int64_t cur_e = -1;
+  for (int j = 0; j < 32; j++) {
+    const int t = warp * 32 + j;
+    const int64_t p = p0 + t;
+    if (p >= npt_total) break;  // uniform over the warp
+    const int64_t e = p / m.npts;
+    if (e != cur_e) {
+      __syncwarp();
+      const int ez = (int)(e % m.nelem[2]), ey = (int)((e / m.nelem[2]) % m.nelem[1]),
+                ex = (int)(e / ((int64_t)m.nelem[1] * m.nelem[2]));
+      for (int i = lane; i < nh * NE; i += 32) {
+        const int h = i / NE, r = i % NE, b = r / 3, d = r % 3;
+        const int64_t cp = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+        S.U[warp][i] = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
+      }
+      cur_e = e;
+    }
+    const double *g = m.geo + p * GEO_STRIDE;
+    for (int i = lane; i < GEO_STRIDE; i += 32) S.R[warp][i] = __ldg(g + i);
+    __syncwarp();
+    if (lane < 30) {
+      const int d = lane / NDD, k = lane % NDD;
+      double s[3] = {0.0, 0.0, 0.0};
+      for (int h = 0; h < nh; h++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
+        s[h] = acc;
+      }
+      if (!TR) {
+        S.sm[lane * LT_NT + t] = s[0];
+      } else if (k == 0) {
+        S.sm[lane * LT_NT + t] = damp * (s[0] - s[2]) / (2.0 * dt) + rho_m * (s[0] + s[2] - 2.0 * s[1]) / (dt * dt);
+      } else {
+        S.sm[lane * LT_NT + t] = 0.5 * (s[1] + s[2]);
+        S.sd[lane * LT_NT + t] = 0.5 * (s[0] - s[2]);
+      }
+    }
+    if (lane == 0) S.wt[t] = S.R[warp][NB * NDD];
+    __syncwarp();
+  }
+  __syncthreads();
+  const int64_t p = p0 + tid;
+  if (p < npt_total) {
+    const int64_t e = p / m.npts;
+    const int q = (int)(p % m.npts);
+    gradelast_point<TR ? 4 : 1, RES, TAN>(S.sm + tid, S.sd + tid, LT_NT, L.par, S.wt[tid],
+                                          preR + e * 30 * m.npts + q, preD + e * 900 * m.npts + q, m.npts);
+  }
 }
 
 template <int LAWK, bool RES, bool TAN>
 static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
+  if (m.geo) {
+    const size_t smem = sizeof(LawThreadSmem);
+    auto kern = law_thread_kernel<LAWK, RES, TAN>;
+    static bool attr_set = false;
+    if (!attr_set) {
+      IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr_set = true;
+    }
+    const int64_t npt = c->nelem_total * m.npts;
+    const int64_t nblk = (npt + LT_NT - 1) / LT_NT;
+    kern<<<(unsigned)nblk, LT_NT, smem, c->stream>>>(m, L, c->d_Uhist, c->d_preR, c->d_preD, npt);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+    return IGAPGPU_OK;
+  }
   const size_t smem = sizeof(LawPtSmem) + sizeof(LawSmem<LAWK>);
   auto kern = law_points_kernel<LAWK, RES, TAN>;
   static bool attr_set = false;

@@ -83,8 +83,9 @@ struct DevLaw {
   const int *sl;           // [nnz]
   const float *sval;       // [nnz]
   int dnnz;
-  // weighted law outputs per point, [nelem][npts][30] and [nelem][npts][900],
-  // when computed for all points before the colour launches (else null)
+  // weighted law outputs per point, [nelem][30][npts] and [nelem][900][npts]
+  // (point-minor), when computed for all points before the colour launches
+  // (else null)
   const double *preR;
   const double *preD;
 };

@@ -244,11 +244,12 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
   if (lane == 0) P.wt = wt;
   if constexpr (LAWK != 0) {
     if (L.preR) {  // law outputs of every point computed beforehand (law_points_kernel)
-      const int64_t pq = (((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez) * m.npts + q;
+      // point-minor layout [element][entry][point]
+      const int64_t e = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
       if (RES)
-        for (int i = lane; i < 30; i += 32) rr[i] = __ldg(L.preR + pq * 30 + i);
+        for (int i = lane; i < 30; i += 32) rr[i] = __ldg(L.preR + (e * 30 + i) * m.npts + q);
       if (TAN && fill_D)
-        for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preD + pq * 900 + i);
+        for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preD + (e * 900 + i) * m.npts + q);
       __syncwarp();
       return;
     }

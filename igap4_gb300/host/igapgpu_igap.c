@@ -149,12 +149,48 @@ int IGAPGPUFinalize(Core core)
   return rc;
 }
 
+/* PETSc's error classes (petscerror.h); the stand-in header used by the
+ * tests defines the same values. */
+#ifndef PETSC_ERR_MEM
+#define PETSC_ERR_MEM 55
+#endif
+#ifndef PETSC_ERR_ARG_WRONG
+#define PETSC_ERR_ARG_WRONG 62
+#endif
+#ifndef PETSC_ERR_ARG_WRONGSTATE
+#define PETSC_ERR_ARG_WRONGSTATE 73
+#endif
+#ifndef PETSC_ERR_LIB
+#define PETSC_ERR_LIB 76
+#endif
+
+PetscErrorCode IGAPGPUPetscError(int rc)
+{
+  switch (rc) {
+  case IGAPGPU_OK: return 0;
+  case IGAPGPU_ERR_NOMEM: return PETSC_ERR_MEM;
+  case IGAPGPU_ERR_ARG:
+  case IGAPGPU_ERR_LAW: return PETSC_ERR_ARG_WRONG;
+  case IGAPGPU_ERR_STATE: return PETSC_ERR_ARG_WRONGSTATE;
+  default: return PETSC_ERR_LIB;
+  }
+}
+
+/* report a library failure once, in PETSc's terms */
+static PetscErrorCode fail(const char *where, int rc)
+{
+  if (!rc) return 0;
+  const char *msg = igapgpu_last_error();
+  fprintf(stderr, "%s: igapgpu error %d: %s\n", where, rc, msg ? msg : "");
+  return IGAPGPUPetscError(rc);
+}
+
 PetscErrorCode Residual_gpu(SNES snes, Vec U, Vec F, void *core_)
 {
   (void)snes;
   Core core = (Core)core_;
   igapgpu_t ctx = IGAPGPUContext(core);
-  if (!ctx) return IGAPGPU_ERR_STATE;
+  if (!ctx) return fail("Residual_gpu", IGAPGPU_ERR_STATE);
   const int n = core->comm[0]->nselfIdx;
   const PetscScalar *u;
   PetscScalar *f;
@@ -165,7 +201,7 @@ PetscErrorCode Residual_gpu(SNES snes, Vec U, Vec F, void *core_)
   if (!rc) rc = igapgpu_residual(ctx, u, f);
   VecRestoreArray(F, &f);
   VecRestoreArrayRead(U, &u);
-  return rc;
+  return fail("Residual_gpu", rc);
 }
 
 PetscErrorCode Tangent_gpu(SNES snes, Vec U, Mat A, Mat P, void *core_)
@@ -173,7 +209,7 @@ PetscErrorCode Tangent_gpu(SNES snes, Vec U, Mat A, Mat P, void *core_)
   (void)snes;
   Core core = (Core)core_;
   int s = slot_of(core);
-  if (s < 0) return IGAPGPU_ERR_STATE;
+  if (s < 0) return fail("Tangent_gpu", IGAPGPU_ERR_STATE);
   igapgpu_t ctx = g_core[s].ctx;
   const int n = core->comm[0]->nselfIdx;
   const PetscScalar *u;
@@ -182,14 +218,17 @@ PetscErrorCode Tangent_gpu(SNES snes, Vec U, Mat A, Mat P, void *core_)
   int rc = upload_history(core, ctx);
   if (!rc) rc = igapgpu_tangent(ctx, u, NULL);
   VecRestoreArrayRead(U, &u);
-  if (rc) return rc;
+  if (rc) return fail("Tangent_gpu", rc);
   if (g_core[s].host_matrix) {
     int64_t ndof, nnz;
     igapgpu_sizes(ctx, &ndof, &nnz, NULL, NULL);
     int64_t *rowptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ndof + 1));
     int32_t *cols = (int32_t *)malloc(sizeof(int32_t) * (size_t)nnz);
     double *vals = (double *)malloc(sizeof(double) * (size_t)nnz);
-    if (!rowptr || !cols || !vals) { free(rowptr); free(cols); free(vals); return IGAPGPU_ERR_NOMEM; }
+    if (!rowptr || !cols || !vals) {
+      free(rowptr); free(cols); free(vals);
+      return fail("Tangent_gpu", IGAPGPU_ERR_NOMEM);
+    }
     rc = igapgpu_pattern(ctx, rowptr, cols);
     if (!rc) rc = igapgpu_tangent(ctx, NULL, vals);
     if (!rc) {
@@ -209,13 +248,20 @@ PetscErrorCode Tangent_gpu(SNES snes, Vec U, Mat A, Mat P, void *core_)
     MatAssemblyBegin(A, MAT_FINAL_ASSEMBLY);
     MatAssemblyEnd(A, MAT_FINAL_ASSEMBLY);
   }
-  return rc;
+  return fail("Tangent_gpu", rc);
 }
 
-PetscErrorCode MatMult_gpu(void *core_, Vec x, Vec y)
+static igapgpu_t shell_context(Mat A)
 {
-  igapgpu_t ctx = IGAPGPUContext((Core)core_);
-  if (!ctx) return IGAPGPU_ERR_STATE;
+  void *core = NULL;
+  if (MatShellGetContext(A, &core)) return NULL;
+  return IGAPGPUContext((Core)core);
+}
+
+PetscErrorCode MatMult_gpu(Mat A, Vec x, Vec y)
+{
+  igapgpu_t ctx = shell_context(A);
+  if (!ctx) return fail("MatMult_gpu", IGAPGPU_ERR_STATE);
   const PetscScalar *xa;
   PetscScalar *ya;
   VecGetArrayRead(x, &xa);
@@ -223,16 +269,28 @@ PetscErrorCode MatMult_gpu(void *core_, Vec x, Vec y)
   int rc = igapgpu_matmult(ctx, xa, ya);
   VecRestoreArray(y, &ya);
   VecRestoreArrayRead(x, &xa);
-  return rc;
+  return fail("MatMult_gpu", rc);
 }
 
-PetscErrorCode MatGetDiagonal_gpu(void *core_, Vec d)
+PetscErrorCode MatGetDiagonal_gpu(Mat A, Vec d)
 {
-  igapgpu_t ctx = IGAPGPUContext((Core)core_);
-  if (!ctx) return IGAPGPU_ERR_STATE;
+  igapgpu_t ctx = shell_context(A);
+  if (!ctx) return fail("MatGetDiagonal_gpu", IGAPGPU_ERR_STATE);
   PetscScalar *da;
   VecGetArray(d, &da);
   int rc = igapgpu_get_diagonal(ctx, da);
   VecRestoreArray(d, &da);
-  return rc;
+  return fail("MatGetDiagonal_gpu", rc);
+}
+
+PetscErrorCode IGAPGPUCreateMatShell(Core core, Mat *A)
+{
+  igapgpu_t ctx = IGAPGPUContext(core);
+  if (!ctx || !A) return fail("IGAPGPUCreateMatShell", IGAPGPU_ERR_STATE);
+  const PetscInt n = (PetscInt)core->comm[0]->nselfIdx;
+  PetscErrorCode ierr = MatCreateShell(PETSC_COMM_WORLD, n, n, n, n, (void *)core, A);
+  if (ierr) return ierr;
+  ierr = MatShellSetOperation(*A, MATOP_MULT, (void (*)(void))MatMult_gpu);
+  if (ierr) return ierr;
+  return MatShellSetOperation(*A, MATOP_GET_DIAGONAL, (void (*)(void))MatGetDiagonal_gpu);
 }

@@ -10,7 +10,14 @@
  *
  * plus the set-up IGAPGPUAssmInit(core), which reads the partitioned mesh,
  * the law and the boundary data from IGAP4's own structs (one rank), and the
- * MATSHELL operations MatMult / MatGetDiagonal of the device matrix.
+ * MATSHELL that stands in for the AIJ tangent IGAPAssmInit creates
+ * (src/interface.c:191) and SNES receives (src/interface.c:219): its
+ * MATOP_MULT and MATOP_GET_DIAGONAL operations run on the device matrix.
+ *
+ * Errors: every PetscErrorCode returned here is 0 or a positive PETSc error
+ * class (PETSC_ERR_MEM, PETSC_ERR_ARG_WRONG, PETSC_ERR_ARG_WRONGSTATE,
+ * PETSC_ERR_LIB), so SNES/KSP propagate them like their own; the library's
+ * message goes to stderr and stays readable through igapgpu_last_error().
  *
  * Compile inside IGAP4 (after petscsnes.h and IGAP4's headers) or stand-alone
  * with igap_types.h.  The glue never computes residual or tangent values on
@@ -43,11 +50,20 @@ int IGAPGPUFinalize(Core core);
 /* The device context of a Core (NULL if none). */
 igapgpu_t IGAPGPUContext(Core core);
 
+/* PETSc error class of an IGAPGPU_ERR_* code (0 stays 0). */
+PetscErrorCode IGAPGPUPetscError(int rc);
+
 PetscErrorCode Residual_gpu(SNES snes, Vec U, Vec F, void *core);
 PetscErrorCode Tangent_gpu(SNES snes, Vec U, Mat A, Mat P, void *core);
-/* MATSHELL operations (ctx = Core): MATOP_MULT, MATOP_GET_DIAGONAL. */
-PetscErrorCode MatMult_gpu(void *core, Vec x, Vec y);
-PetscErrorCode MatGetDiagonal_gpu(void *core, Vec d);
+/* A MATSHELL of the Core's device matrix (local and global size = the DOF
+ * count of the one rank, shell context = core) with MATOP_MULT =
+ * MatMult_gpu and MATOP_GET_DIAGONAL = MatGetDiagonal_gpu; pass it to
+ * SNESSetJacobian as A and P in place of the AIJ matrix. */
+PetscErrorCode IGAPGPUCreateMatShell(Core core, Mat *A);
+/* MATSHELL operations, PETSc's MATOP_MULT / MATOP_GET_DIAGONAL signatures;
+ * the Core comes from MatShellGetContext. */
+PetscErrorCode MatMult_gpu(Mat A, Vec x, Vec y);
+PetscErrorCode MatGetDiagonal_gpu(Mat A, Vec d);
 
 #ifdef __cplusplus
 }

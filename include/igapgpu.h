@@ -48,7 +48,8 @@ extern "C" {
 
 /* Precision of the element contraction (the rest is always FP64). */
 #define IGAPGPU_PREC_FP64 0  /* FP64 everywhere */
-#define IGAPGPU_PREC_SPLIT 1 /* tensor-core split-BF16 products, FP32 accumulate */
+#define IGAPGPU_PREC_SPLIT 1 /* tangent on the tensor cores: TF32x3 products (hi*hi + hi*lo + lo*hi),
+                                FP32 accumulate; relative error <= 1e-5 (measured ~2e-6) */
 
 typedef struct igapgpu_ctx *igapgpu_t;
 

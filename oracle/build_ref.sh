@@ -3,10 +3,11 @@
 # against the project's single-rank MPI/PETSc stand-ins, into
 # oracle/_ref/libigapref.so (git-ignored).  Test infrastructure only.
 #
-# Needs the reference tree (default /root/reference, override with IGAP4_REF).
-# Where it is absent (e.g. on a machine without the reference) this script
-# exits 0 without building and the oracle falls back to the project's own C
-# restatement (oracle/libigaporacle.so).
+# Reads the reference tree at IGAP4_REF (default /root/reference, where the
+# tree is mounted in the build container).  Where it is absent (e.g. on a
+# machine without the reference) this script exits 0 without building, and the
+# tests use the golden fixtures and the project's own C restatement
+# (oracle/liborc.so, built by build_oracle.sh).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${IGAP4_REF:-/root/reference}"

@@ -8,8 +8,15 @@
  * (src/interface.c:191, setnz_iga src/assmcore_iga.c:1054-1087); entries are
  * created on first MatSetValues (zeros included, as PETSc does), so after one
  * assembly the stored pattern equals the one PETSc would hold.
- * SNES/KSP/PC calls made by IGAPSolvInit (src/interface.c:207-250) are
- * recorded but no solver is run: Krylov/Newton parity is pinned elsewhere.
+ * A Mat may also be a MATSHELL (MatCreateShell / MatShellSetOperation /
+ * MatShellGetContext), whose MatMult and MatGetDiagonal call the registered
+ * operations.  SNES/KSP/PC keep what IGAPSolvInit (src/interface.c:207-250)
+ * sets, and SNESSolve runs a plain Newton method with a backtracking line
+ * search over right-preconditioned GMRES(restart, modified Gram-Schmidt),
+ * Jacobi from MatGetDiagonal of the preconditioning matrix (PCASM is taken
+ * as Jacobi, with a warning), calling the registered residual and Jacobian
+ * callbacks and MatMult of the operator: enough to drive the SNES callbacks
+ * and a MATSHELL the way PETSc does, not a model of PETSc's arithmetic.
  */
 #ifndef IGAP_ORACLE_STUB_PETSCSNES_H
 #define IGAP_ORACLE_STUB_PETSCSNES_H
@@ -27,6 +34,13 @@ typedef double PetscReal;
 typedef enum { PETSC_FALSE = 0, PETSC_TRUE = 1 } PetscBool;
 
 #define PETSC_NULL 0
+#define PETSC_COMM_WORLD MPI_COMM_WORLD
+#define PETSC_COMM_SELF MPI_COMM_WORLD
+/* error classes (petscerror.h values) */
+#define PETSC_ERR_MEM 55
+#define PETSC_ERR_ARG_WRONG 62
+#define PETSC_ERR_ARG_WRONGSTATE 73
+#define PETSC_ERR_LIB 76
 #define PETSC_DEFAULT -2
 #define PETSC_DECIDE -1
 
@@ -47,6 +61,8 @@ typedef enum {
   MAT_SYMMETRY_ETERNAL
 } MatOption;
 
+typedef enum { MATOP_MULT = 3, MATOP_GET_DIAGONAL = 17 } MatOperation;
+
 typedef const char *SNESType;
 typedef const char *KSPType;
 typedef const char *PCType;
@@ -58,6 +74,7 @@ typedef const char *SNESLineSearchType;
 #define KSPCG "cg"
 #define PCASM "asm"
 #define PCJACOBI "jacobi"
+#define PCNONE "none"
 typedef enum { SNES_LINESEARCH_ORDER_LINEAR = 1, SNES_LINESEARCH_ORDER_QUADRATIC = 2,
                SNES_LINESEARCH_ORDER_CUBIC = 3 } SNESLineSearchOrder;
 typedef enum { PC_LEFT, PC_RIGHT, PC_SYMMETRIC } PCSide;
@@ -116,8 +133,17 @@ PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType t);
 PetscErrorCode MatZeroRowsColumns(Mat A, PetscInt n, const PetscInt rows[], PetscScalar diag,
                                   Vec x, Vec b);
 PetscErrorCode MatDestroy(Mat *A);
+PetscErrorCode MatGetSize(Mat A, PetscInt *m, PetscInt *n);
+PetscErrorCode MatMult(Mat A, Vec x, Vec y);
+PetscErrorCode MatGetDiagonal(Mat A, Vec d);
 
-/* SNES / KSP / PC: recorded only (no solve in the oracle) */
+/* MATSHELL */
+PetscErrorCode MatCreateShell(MPI_Comm comm, PetscInt m, PetscInt n, PetscInt M, PetscInt N,
+                              void *ctx, Mat *A);
+PetscErrorCode MatShellSetOperation(Mat A, MatOperation op, void (*fn)(void));
+PetscErrorCode MatShellGetContext(Mat A, void *ctx);
+
+/* SNES / KSP / PC */
 PetscErrorCode SNESCreate(MPI_Comm comm, SNES *s);
 PetscErrorCode SNESSetFunction(SNES s, Vec r, SNESFunctionFn f, void *ctx);
 PetscErrorCode SNESSetJacobian(SNES s, Mat A, Mat P, SNESJacobianFn f, void *ctx);
@@ -132,6 +158,7 @@ PetscErrorCode SNESSetFromOptions(SNES s);
 PetscErrorCode SNESSolve(SNES s, Vec b, Vec x);
 PetscErrorCode SNESGetConvergedReason(SNES s, SNESConvergedReason *r);
 PetscErrorCode SNESGetFunctionNorm(SNES s, PetscReal *fnorm);
+PetscErrorCode SNESGetIterationNumber(SNES s, PetscInt *its);
 PetscErrorCode SNESDestroy(SNES *s);
 PetscErrorCode KSPGetPC(KSP k, PC *pc);
 PetscErrorCode KSPSetInitialGuessNonzero(KSP k, PetscBool flg);

@@ -4,6 +4,7 @@
  * it exists so that the reference's unmodified sources can be compiled and run
  * as the CPU oracle.  Nothing in the product links it.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -114,8 +115,14 @@ int MPI_Wait(MPI_Request *req, MPI_Status *st)
 
 /* ---------------------------------------------------------------- PETSc -- */
 struct _p_Vec { int n; double *a; };
+typedef PetscErrorCode (*MultFn)(Mat, Vec, Vec);
+typedef PetscErrorCode (*DiagFn)(Mat, Vec);
 struct _p_Mat {
   int n;
+  int shell;   /* MATSHELL: ctx + operations, no storage */
+  void *ctx;
+  MultFn mult;
+  DiagFn diag;
   int *cap;    /* preallocated capacity per row */
   int *len;    /* entries used per row */
   int *start;  /* offset of each row in cols/vals */
@@ -123,10 +130,27 @@ struct _p_Mat {
   double *vals;
   long nnz_cap;
 };
-struct _p_SNES { int dummy; };
-struct _p_KSP { int dummy; };
-struct _p_PC { int dummy; };
-struct _p_SNESLineSearch { int dummy; };
+struct _p_PC { int jacobi; };
+struct _p_KSP {
+  struct _p_PC pc;
+  double rtol, abstol, dtol;
+  int maxits, restart, its;
+};
+struct _p_SNESLineSearch { int order; };
+struct _p_SNES {
+  struct _p_KSP ksp;
+  struct _p_SNESLineSearch ls;
+  SNESFunctionFn f;
+  void *fctx;
+  Vec r;
+  SNESJacobianFn J;
+  void *jctx;
+  Mat A, P;
+  double abstol, rtol, stol;
+  int maxit, its;
+  double fnorm;
+  SNESConvergedReason reason;
+};
 
 static const char *const g_reasons_storage[] = {
   "DIVERGED_LOCAL_MIN", "DIVERGED_INNER", "DIVERGED_LINE_SEARCH", "DIVERGED_MAX_IT",
@@ -243,6 +267,62 @@ PetscErrorCode MatZeroRowsColumns(Mat A, PetscInt n, const PetscInt rows[], Pets
   free(flag);
   return 0;
 }
+PetscErrorCode MatGetSize(Mat A, PetscInt *m, PetscInt *n)
+{
+  if (m) *m = A->n;
+  if (n) *n = A->n;
+  return 0;
+}
+PetscErrorCode MatMult(Mat A, Vec x, Vec y)
+{
+  if (A->shell) {
+    if (!A->mult) { fprintf(stderr, "stub Mat: MATSHELL without MATOP_MULT\n"); return PETSC_ERR_ARG_WRONGSTATE; }
+    return A->mult(A, x, y);
+  }
+  for (int r = 0; r < A->n; r++) {
+    double acc = 0.0;
+    for (int k = 0; k < A->len[r]; k++) acc += A->vals[A->start[r] + k] * x->a[A->cols[A->start[r] + k]];
+    y->a[r] = acc;
+  }
+  return 0;
+}
+PetscErrorCode MatGetDiagonal(Mat A, Vec d)
+{
+  if (A->shell) {
+    if (!A->diag) { fprintf(stderr, "stub Mat: MATSHELL without MATOP_GET_DIAGONAL\n"); return PETSC_ERR_ARG_WRONGSTATE; }
+    return A->diag(A, d);
+  }
+  for (int r = 0; r < A->n; r++) {
+    d->a[r] = 0.0;
+    for (int k = 0; k < A->len[r]; k++)
+      if (A->cols[A->start[r] + k] == r) d->a[r] = A->vals[A->start[r] + k];
+  }
+  return 0;
+}
+PetscErrorCode MatCreateShell(MPI_Comm c, PetscInt m, PetscInt n, PetscInt M, PetscInt N, void *ctx, Mat *A)
+{
+  (void)c; (void)n; (void)M; (void)N;
+  Mat a = (Mat)calloc(1, sizeof(*a));
+  a->n = m;
+  a->shell = 1;
+  a->ctx = ctx;
+  *A = a;
+  return 0;
+}
+PetscErrorCode MatShellSetOperation(Mat A, MatOperation op, void (*fn)(void))
+{
+  if (!A->shell) return PETSC_ERR_ARG_WRONG;
+  if (op == MATOP_MULT) A->mult = (MultFn)fn;
+  else if (op == MATOP_GET_DIAGONAL) A->diag = (DiagFn)fn;
+  else return PETSC_ERR_ARG_WRONG;
+  return 0;
+}
+PetscErrorCode MatShellGetContext(Mat A, void *ctx)
+{
+  if (!A || !A->shell) return PETSC_ERR_ARG_WRONG;
+  *(void **)ctx = A->ctx;
+  return 0;
+}
 PetscErrorCode MatDestroy(Mat *A)
 {
   if (*A) {
@@ -274,36 +354,217 @@ void oracle_stub_mat_csr(Mat A, long *rowptr, int *cols, double *vals)
   }
 }
 
-static struct _p_SNES g_snes; static struct _p_KSP g_ksp; static struct _p_PC g_pc;
-static struct _p_SNESLineSearch g_ls;
-PetscErrorCode SNESCreate(MPI_Comm c, SNES *s) { (void)c; *s = &g_snes; return 0; }
-PetscErrorCode SNESSetFunction(SNES s, Vec r, SNESFunctionFn f, void *ctx) { (void)s; (void)r; (void)f; (void)ctx; return 0; }
-PetscErrorCode SNESSetJacobian(SNES s, Mat A, Mat P, SNESJacobianFn f, void *ctx) { (void)s; (void)A; (void)P; (void)f; (void)ctx; return 0; }
-PetscErrorCode SNESSetTolerances(SNES s, PetscReal a, PetscReal r, PetscReal st, PetscInt mi, PetscInt mf) { (void)s; (void)a; (void)r; (void)st; (void)mi; (void)mf; return 0; }
-PetscErrorCode SNESSetType(SNES s, SNESType t) { (void)s; (void)t; return 0; }
-PetscErrorCode SNESGetLineSearch(SNES s, SNESLineSearch *ls) { (void)s; *ls = &g_ls; return 0; }
-PetscErrorCode SNESLineSearchSetType(SNESLineSearch ls, SNESLineSearchType t) { (void)ls; (void)t; return 0; }
-PetscErrorCode SNESLineSearchSetOrder(SNESLineSearch ls, SNESLineSearchOrder o) { (void)ls; (void)o; return 0; }
-PetscErrorCode SNESGetKSP(SNES s, KSP *k) { (void)s; *k = &g_ksp; return 0; }
-PetscErrorCode SNESSetFromOptions(SNES s) { (void)s; return 0; }
-PetscErrorCode SNESSolve(SNES s, Vec b, Vec x)
+/* SNES / KSP / PC: settings as IGAPSolvInit leaves them; SNESSolve is a
+ * plain Newton / GMRES driver that calls the registered callbacks. */
+PetscErrorCode SNESCreate(MPI_Comm c, SNES *s)
 {
-  (void)s; (void)b; (void)x;
-  fprintf(stderr, "oracle stub: SNESSolve is not available\n");
-  abort();
+  (void)c;
+  SNES n = (SNES)calloc(1, sizeof(*n));
+  n->abstol = 1e-50; n->rtol = 1e-8; n->stol = 1e-8; n->maxit = 50;
+  n->ksp.rtol = 1e-5; n->ksp.abstol = 1e-50; n->ksp.dtol = 1e5; n->ksp.maxits = 10000; n->ksp.restart = 30;
+  n->ksp.pc.jacobi = 1;
+  *s = n;
+  return 0;
 }
-PetscErrorCode SNESGetConvergedReason(SNES s, SNESConvergedReason *r) { (void)s; *r = SNES_DIVERGED_INNER; return 0; }
-PetscErrorCode SNESGetFunctionNorm(SNES s, PetscReal *f) { (void)s; *f = 0; return 0; }
-PetscErrorCode SNESDestroy(SNES *s) { *s = 0; return 0; }
-PetscErrorCode KSPGetPC(KSP k, PC *pc) { (void)k; *pc = &g_pc; return 0; }
+PetscErrorCode SNESSetFunction(SNES s, Vec r, SNESFunctionFn f, void *ctx) { s->r = r; s->f = f; s->fctx = ctx; return 0; }
+PetscErrorCode SNESSetJacobian(SNES s, Mat A, Mat P, SNESJacobianFn f, void *ctx)
+{
+  s->A = A; s->P = P; s->J = f; s->jctx = ctx;
+  return 0;
+}
+PetscErrorCode SNESSetTolerances(SNES s, PetscReal a, PetscReal r, PetscReal st, PetscInt mi, PetscInt mf)
+{
+  (void)mf;
+  if (a != PETSC_DEFAULT) s->abstol = a;
+  if (r != PETSC_DEFAULT) s->rtol = r;
+  if (st != PETSC_DEFAULT) s->stol = st;
+  if (mi != PETSC_DEFAULT) s->maxit = mi;
+  return 0;
+}
+PetscErrorCode SNESSetType(SNES s, SNESType t) { (void)s; return strcmp(t, SNESNEWTONLS) ? PETSC_ERR_ARG_WRONG : 0; }
+PetscErrorCode SNESGetLineSearch(SNES s, SNESLineSearch *ls) { *ls = &s->ls; return 0; }
+PetscErrorCode SNESLineSearchSetType(SNESLineSearch ls, SNESLineSearchType t) { (void)ls; (void)t; return 0; }
+PetscErrorCode SNESLineSearchSetOrder(SNESLineSearch ls, SNESLineSearchOrder o) { ls->order = (int)o; return 0; }
+PetscErrorCode SNESGetKSP(SNES s, KSP *k) { *k = &s->ksp; return 0; }
+PetscErrorCode SNESSetFromOptions(SNES s) { (void)s; return 0; }
+PetscErrorCode SNESGetConvergedReason(SNES s, SNESConvergedReason *r) { *r = s->reason; return 0; }
+PetscErrorCode SNESGetFunctionNorm(SNES s, PetscReal *f) { *f = s->fnorm; return 0; }
+PetscErrorCode SNESGetIterationNumber(SNES s, PetscInt *i) { *i = s->its; return 0; }
+PetscErrorCode SNESDestroy(SNES *s) { if (*s) free(*s); *s = 0; return 0; }
+PetscErrorCode KSPGetPC(KSP k, PC *pc) { *pc = &k->pc; return 0; }
 PetscErrorCode KSPSetInitialGuessNonzero(KSP k, PetscBool f) { (void)k; (void)f; return 0; }
-PetscErrorCode KSPSetTolerances(KSP k, PetscReal r, PetscReal a, PetscReal d, PetscInt m) { (void)k; (void)r; (void)a; (void)d; (void)m; return 0; }
-PetscErrorCode KSPSetType(KSP k, KSPType t) { (void)k; (void)t; return 0; }
-PetscErrorCode KSPGMRESSetRestart(KSP k, PetscInt r) { (void)k; (void)r; return 0; }
+PetscErrorCode KSPSetTolerances(KSP k, PetscReal r, PetscReal a, PetscReal d, PetscInt m)
+{
+  if (r != PETSC_DEFAULT) k->rtol = r;
+  if (a != PETSC_DEFAULT) k->abstol = a;
+  if (d != PETSC_DEFAULT) k->dtol = d;
+  if (m != PETSC_DEFAULT) k->maxits = m;
+  return 0;
+}
+PetscErrorCode KSPSetType(KSP k, KSPType t) { (void)k; return strcmp(t, KSPGMRES) ? PETSC_ERR_ARG_WRONG : 0; }
+PetscErrorCode KSPGMRESSetRestart(KSP k, PetscInt r) { k->restart = r; return 0; }
 PetscErrorCode KSPGMRESSetOrthogonalization(KSP k, PetscErrorCode (*fn)(KSP, PetscInt)) { (void)k; (void)fn; return 0; }
-PetscErrorCode KSPSetPCSide(KSP k, PCSide s) { (void)k; (void)s; return 0; }
-PetscErrorCode KSPGetIterationNumber(KSP k, PetscInt *i) { (void)k; *i = 0; return 0; }
+PetscErrorCode KSPSetPCSide(KSP k, PCSide s) { (void)k; return s == PC_RIGHT ? 0 : PETSC_ERR_ARG_WRONG; }
+PetscErrorCode KSPGetIterationNumber(KSP k, PetscInt *i) { *i = k->its; return 0; }
 PetscErrorCode KSPCGSetType(KSP k, KSPCGType t) { (void)k; (void)t; return 0; }
-PetscErrorCode PCSetType(PC pc, PCType t) { (void)pc; (void)t; return 0; }
+PetscErrorCode PCSetType(PC pc, PCType t)
+{
+  if (!strcmp(t, PCJACOBI)) pc->jacobi = 1;
+  else if (!strcmp(t, PCNONE)) pc->jacobi = 0;
+  else if (!strcmp(t, PCASM)) {
+    fprintf(stderr, "stub PC: PCASM taken as Jacobi\n");
+    pc->jacobi = 1;
+  } else return PETSC_ERR_ARG_WRONG;
+  return 0;
+}
 PetscErrorCode PCASMSetType(PC pc, PCASMType t) { (void)pc; (void)t; return 0; }
 PetscErrorCode PCJacobiSetUseAbs(PC pc, PetscBool f) { (void)pc; (void)f; return 0; }
+
+static double vnorm(int n, const double *a)
+{
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s += a[i] * a[i];
+  return sqrt(s);
+}
+
+/* Right-preconditioned GMRES(m) with modified Gram-Schmidt on A x = b from
+ * x = 0; z = M^-1 v with M = diag(P) (or the identity). */
+static PetscErrorCode ksp_gmres(KSP k, Mat A, Mat P, Vec b, Vec x)
+{
+  const int n = b->n, m = k->restart > 0 ? (k->restart < 200 ? k->restart : 200) : 30;
+  PetscErrorCode ierr = 0;
+  double *dinv = (double *)malloc(sizeof(double) * (size_t)n);
+  double *V = (double *)malloc(sizeof(double) * (size_t)n * (m + 1));
+  double *Z = (double *)malloc(sizeof(double) * (size_t)n * m);
+  double *H = (double *)calloc((size_t)(m + 1) * m, sizeof(double));
+  double *cs = (double *)malloc(sizeof(double) * m), *sn = (double *)malloc(sizeof(double) * m);
+  double *g = (double *)malloc(sizeof(double) * (m + 1)), *yv = (double *)malloc(sizeof(double) * m);
+  Vec vin, vout;
+  VecDuplicate(b, &vin);
+  VecDuplicate(b, &vout);
+  if (k->pc.jacobi) {
+    Vec d;
+    VecDuplicate(b, &d);
+    ierr = MatGetDiagonal(P, d);
+    for (int i = 0; i < n && !ierr; i++) dinv[i] = d->a[i] != 0.0 ? 1.0 / d->a[i] : 1.0;
+    VecDestroy(&d);
+  } else {
+    for (int i = 0; i < n; i++) dinv[i] = 1.0;
+  }
+  memset(x->a, 0, sizeof(double) * (size_t)n);
+  const double bnorm = vnorm(n, b->a);
+  const double tol = fmax(k->rtol * bnorm, k->abstol);
+  k->its = 0;
+  double rnorm = bnorm;
+  while (!ierr && rnorm > tol && k->its < k->maxits) {
+    /* r = b - A x */
+    memcpy(vin->a, x->a, sizeof(double) * (size_t)n);
+    if ((ierr = MatMult(A, vin, vout))) break;
+    for (int i = 0; i < n; i++) V[i] = b->a[i] - vout->a[i];
+    double beta = vnorm(n, V);
+    if (beta == 0.0) { rnorm = 0.0; break; }
+    for (int i = 0; i < n; i++) V[i] /= beta;
+    for (int i = 0; i <= m; i++) g[i] = 0.0;
+    g[0] = beta;
+    int j = 0;
+    for (; j < m && k->its < k->maxits; j++) {
+      double *zj = Z + (size_t)n * j, *w = V + (size_t)n * (j + 1);
+      for (int i = 0; i < n; i++) zj[i] = dinv[i] * V[(size_t)n * j + i];
+      memcpy(vin->a, zj, sizeof(double) * (size_t)n);
+      if ((ierr = MatMult(A, vin, vout))) break;
+      memcpy(w, vout->a, sizeof(double) * (size_t)n);
+      for (int q = 0; q <= j; q++) {
+        const double *vq = V + (size_t)n * q;
+        double h = 0.0;
+        for (int i = 0; i < n; i++) h += w[i] * vq[i];
+        H[q * m + j] = h;
+        for (int i = 0; i < n; i++) w[i] -= h * vq[i];
+      }
+      double hn = vnorm(n, w);
+      H[(j + 1) * m + j] = hn;
+      if (hn != 0.0)
+        for (int i = 0; i < n; i++) w[i] /= hn;
+      for (int q = 0; q < j; q++) {
+        double a = H[q * m + j], c = H[(q + 1) * m + j];
+        H[q * m + j] = cs[q] * a + sn[q] * c;
+        H[(q + 1) * m + j] = -sn[q] * a + cs[q] * c;
+      }
+      double a = H[j * m + j], c = H[(j + 1) * m + j], r = hypot(a, c);
+      cs[j] = r != 0.0 ? a / r : 1.0;
+      sn[j] = r != 0.0 ? c / r : 0.0;
+      H[j * m + j] = r;
+      H[(j + 1) * m + j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      k->its++;
+      rnorm = fabs(g[j + 1]);
+      if (rnorm <= tol || hn == 0.0) { j++; break; }
+    }
+    if (ierr) break;
+    for (int q = j - 1; q >= 0; q--) {
+      double s = g[q];
+      for (int t = q + 1; t < j; t++) s -= H[q * m + t] * yv[t];
+      yv[q] = s / H[q * m + q];
+    }
+    for (int q = 0; q < j; q++)
+      for (int i = 0; i < n; i++) x->a[i] += yv[q] * Z[(size_t)n * q + i];
+    if (rnorm > k->dtol * bnorm) break;
+  }
+  VecDestroy(&vin);
+  VecDestroy(&vout);
+  free(dinv); free(V); free(Z); free(H); free(cs); free(sn); free(g); free(yv);
+  return ierr;
+}
+
+/* Newton with a backtracking line search on 1/2 |F|^2 (full step first,
+ * then quadratic backtracking, step kept in [0.1, 0.5] of the previous). */
+PetscErrorCode SNESSolve(SNES s, Vec b, Vec x)
+{
+  (void)b;
+  if (!s->f || !s->J || !s->A) return PETSC_ERR_ARG_WRONGSTATE;
+  PetscErrorCode ierr;
+  const int n = x->n;
+  Vec F = s->r, Y, Xb;
+  int ownF = 0;
+  if (!F) { VecDuplicate(x, &F); ownF = 1; }
+  VecDuplicate(x, &Y);
+  VecDuplicate(x, &Xb);
+  s->its = 0;
+  s->reason = SNES_CONVERGED_ITERATING;
+  if ((ierr = s->f(s, x, F, s->fctx))) goto done;
+  double fnorm = vnorm(n, F->a);
+  const double fnorm0 = fnorm;
+  for (;;) {
+    if (!isfinite(fnorm)) { s->reason = SNES_DIVERGED_FNORM_NAN; break; }
+    if (fnorm <= s->abstol) { s->reason = SNES_CONVERGED_FNORM_ABS; break; }
+    if (s->its > 0 && fnorm <= s->rtol * fnorm0) { s->reason = SNES_CONVERGED_FNORM_RELATIVE; break; }
+    if (s->its >= s->maxit) { s->reason = SNES_DIVERGED_MAX_IT; break; }
+    if ((ierr = s->J(s, x, s->A, s->P ? s->P : s->A, s->jctx))) break;
+    /* J Y = F, x <- x - lam Y */
+    if ((ierr = ksp_gmres(&s->ksp, s->A, s->P ? s->P : s->A, F, Y))) break;
+    memcpy(Xb->a, x->a, sizeof(double) * (size_t)n);
+    const double f0 = 0.5 * fnorm * fnorm, slope = -fnorm * fnorm;
+    double lam = 1.0, fn = fnorm;
+    int ok = 0;
+    for (int ls = 0; ls < 30; ls++) {
+      for (int i = 0; i < n; i++) x->a[i] = Xb->a[i] - lam * Y->a[i];
+      if ((ierr = s->f(s, x, F, s->fctx))) break;
+      fn = vnorm(n, F->a);
+      const double fl = 0.5 * fn * fn;
+      if (isfinite(fl) && fl <= f0 + 1e-4 * lam * slope) { ok = 1; break; }
+      double lnew = isfinite(fl) ? -slope * lam * lam / (2.0 * (fl - f0 - lam * slope)) : 0.5 * lam;
+      lam = fmin(fmax(lnew, 0.1 * lam), 0.5 * lam);
+    }
+    if (ierr) break;
+    s->its++;
+    fnorm = fn;
+    if (!ok) { s->reason = SNES_DIVERGED_LINE_SEARCH; break; }
+    if (lam * vnorm(n, Y->a) <= s->stol * vnorm(n, x->a)) { s->reason = SNES_CONVERGED_SNORM_RELATIVE; break; }
+  }
+  s->fnorm = fnorm;
+done:
+  VecDestroy(&Y);
+  VecDestroy(&Xb);
+  if (ownF) VecDestroy(&F);
+  return ierr;
+}
