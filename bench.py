@@ -73,6 +73,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=256,
                     help="instances of the batched workload (0 skips it)")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--transient-steps", type=int, default=40,
+                    help="time steps of the transient workload per arm (0 skips it)")
+    ap.add_argument("--transient-nelem", default="64,16,16")
     return ap.parse_args()
 
 
@@ -289,6 +292,64 @@ def bench_batched(ig, torch, dev, n, steps, warmup, flush, peaks):
     return out
 
 
+PREDICTOR_FILE = os.path.join(ROOT, "igap4_gb300", "data", "predictor_gradelasttime.npz")
+
+
+def bench_transient(ig, torch, nelem, steps, seed=9001):
+    """Time to |F| <= 1e-8 per transient step, plain Newton from u_n against
+    the learned predictor's guess (kept only when it lowers |F|): the
+    reference's three-level law (gradelasttime, density 1, dt 1e-2) on a
+    quadratic beam clamped at x = 0 under a seeded tip-load history (sum of 4
+    sinusoids, amplitudes in [0, 1e-3], frequencies in [0.5, 5]) that the
+    predictor never saw.  Newton: FP64 residual, tangent on the tensor cores,
+    GMRES(100) with Jacobi and two-pass classical Gram-Schmidt, replayed from
+    CUDA graphs.  Each arm runs the same steps from rest; the step time is the
+    wall time of the whole step (predictor, acceptance test, Newton)."""
+    from igap4_gb300.train_predictor import load_network, transient_problem
+    from igap4_gb300.transient import TipLoad, run_transient
+    from igap4_gb300.predictor import LearnedPredictor
+
+    dt = 1e-2
+    A, _ = transient_problem(nelem, dt, prec="split")
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30,
+                use_graphs=1, pc=1, orth=1)
+    load = TipLoad(seed=seed)
+    run_transient(A, load, 3, dt, opts=opts, record_states=False)  # warm-up: graphs captured
+
+    def summary(recs):
+        ms = np.array([1e3 * r.seconds for r in recs])
+        return {"ms_per_step": float(ms.mean()), "ms_median": float(np.median(ms)),
+                "newton_its_per_step": float(np.mean([r.newton_its for r in recs])),
+                "gmres_its_per_step": float(np.mean([r.ksp_its for r in recs])),
+                "converged_all": bool(all(r.converged for r in recs)),
+                "max_final_fnorm": float(max(r.fnorm for r in recs)),
+                "prediction_used_fraction": float(np.mean([r.used_prediction for r in recs]))}
+
+    t0 = time.perf_counter()
+    _, plain = run_transient(A, load, steps, dt, opts=opts, record_states=False)
+    out = {"workload": f"transient gradelasttime beam {nelem[0]}x{nelem[1]}x{nelem[2]} ({A.ndof} DOF), "
+                       f"{steps} steps of dt=1e-2 from rest, unseen seeded tip-load history (seed {seed})",
+           "tolerance": "Newton |F| <= 1e-8 (FP64 residual)", "plain": summary(plain),
+           "plain_wall_s": time.perf_counter() - t0}
+    if os.path.exists(PREDICTOR_FILE):
+        net, sc = load_network(PREDICTOR_FILE, tuple(n + 2 for n in nelem))
+        pred = LearnedPredictor(net, sc, A=A)
+        _, learned = run_transient(A, load, steps, dt, predictor=pred, opts=opts, record_states=False)
+        out["learned"] = summary(learned)
+        out["time_ratio_learned_vs_plain"] = out["learned"]["ms_per_step"] / out["plain"]["ms_per_step"]
+        out["its_ratio_learned_vs_plain"] = (out["learned"]["newton_its_per_step"] /
+                                             out["plain"]["newton_its_per_step"])
+        z = np.load(PREDICTOR_FILE)
+        out["predictor"] = {"file": os.path.relpath(PREDICTOR_FILE, ROOT), "training": json.loads(str(z["meta"])),
+                            "inputs": str(z["mode"])}
+        net.close()
+    else:
+        out["learned"] = None
+        out["note"] = "no trained predictor file"
+    A.close()
+    return out
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -456,6 +517,10 @@ def main():
         sampler.start()
         batched = bench_batched(ig, torch, dev, a.batch, a.batch_steps, max(3, a.warmup), flush, peaks)
         sampler.stop()
+    transient = None
+    if a.transient_steps > 0 and world == 1:
+        transient = bench_transient(ig, torch, tuple(int(v) for v in a.transient_nelem.split(",")),
+                                    a.transient_steps)
     elem_kernel_ms = elem_ms / max(elem_launches, 1)
     flop_per_launch = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) * elem_count / max(elem_launches, 1)
     achieved = flop_per_launch / (elem_kernel_ms * 1e-3) / 1e12
@@ -508,6 +573,7 @@ def main():
             "cpu_baseline": cpu,
             "split": split,
             "batched": batched,
+            "transient": transient,
             "clocks": sampler.summary(local),
             "step_ms": step_ms,
             "wall_s": t_wall,

@@ -53,7 +53,7 @@ class SolverOpts(ctypes.Structure):
                 ("linesearch", ctypes.c_int), ("ksp_restart", ctypes.c_int),
                 ("ksp_rtol", ctypes.c_double), ("ksp_abstol", ctypes.c_double),
                 ("ksp_dtol", ctypes.c_double), ("ksp_max_it", ctypes.c_int), ("pc", ctypes.c_int),
-                ("use_graphs", ctypes.c_int)]
+                ("use_graphs", ctypes.c_int), ("orth", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):

@@ -131,11 +131,62 @@ __global__ void gm_cycle_init(GmState *st, const double *beta_in, double *g, int
   for (int i = 0; i <= m; i++) g[i] = 0.0;
   g[0] = beta;
 }
-// Givens update of Hessenberg column j (column-major, leading dim m+1)
-__global__ void gm_givens(double *H, double *cs, double *sn, double *g, int j, int m, GmState *st)
+// Classical Gram-Schmidt pass over basis vectors 0..cnt-1 (blockIdx.y):
+// per row block the partial dot products with w, then per vector a fixed-order
+// sum (deterministic), then w -= V h.
+constexpr int MD_BLOCKS = 64;
+__global__ void __launch_bounds__(256) gm_mdot_partial(const double *__restrict__ V, const double *__restrict__ w,
+                                                       int64_t n, double *partial, const GmState *st)
+{
+  if (st->done) return;
+  __shared__ double sh[8];
+  const double *v = V + (size_t)blockIdx.y * n;
+  double s = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    s = fma(v[r], w[r], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < 8 ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = s;
+  }
+}
+// one warp per vector: h[i] = sum of its MD_BLOCKS partials
+__global__ void gm_mdot_final(const double *partial, int cnt, double *h, const GmState *st)
+{
+  if (st->done) return;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= cnt) return;
+  double s = 0.0;
+  for (int k = lane; k < MD_BLOCKS; k += 32) s += partial[i * MD_BLOCKS + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) h[i] = s;
+}
+__global__ void __launch_bounds__(256) gm_vupdate(double *__restrict__ w, const double *__restrict__ V,
+                                                  const double *__restrict__ h, int cnt, int64_t n,
+                                                  const GmState *st)
+{
+  if (st->done) return;
+  __shared__ double hs[1024];
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = h[i];
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = w[r];
+    for (int i = 0; i < cnt; i++) s = fma(-hs[i], V[(size_t)i * n + r], s);
+    w[r] = s;
+  }
+}
+// Givens update of Hessenberg column j (column-major, leading dim m+1); with
+// corr (the second Gram-Schmidt pass) h[0..j] += corr[0..j] first.
+__global__ void gm_givens(double *H, double *cs, double *sn, double *g, int j, int m, GmState *st,
+                          const double *corr = nullptr)
 {
   if (st->done) return;
   double *h = H + (size_t)j * (m + 1);
+  if (corr)
+    for (int i = 0; i <= j; i++) h[i] += corr[i];
   for (int i = 0; i < j; i++) {
     const double t = cs[i] * h[i] + sn[i] * h[i + 1];
     h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
@@ -190,7 +241,7 @@ __global__ void get_diag_kernel_g(const int64_t *rowptr, const int32_t *cols, co
 
 // Graph workspace held by the context.
 struct GraphWork {
-  int m = 0, pc = -1;
+  int m = 0, pc = -1, orth = -1;
   cudaGraphExec_t exec = nullptr;
   int64_t nodes = 0;
   double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *V = nullptr, *Z = nullptr;
@@ -231,7 +282,7 @@ static cudaStream_t capture_stream(const Context *c)
   return (c->stream == nullptr || c->stream == cudaStreamLegacy) ? c->own_stream : c->stream;
 }
 
-static int build_gmres_graph(Context *c, int m, int pc)
+static int build_gmres_graph(Context *c, int m, int pc, int orth)
 {
   free_graph(c->gmres_graph);
   c->gmres_graph = nullptr;
@@ -241,7 +292,8 @@ static int build_gmres_graph(Context *c, int m, int pc)
   if (alloc(&gw->b, n) || alloc(&gw->x, n) || alloc(&gw->r, n) || alloc(&gw->w, n) ||
       alloc(&gw->V, (size_t)(m + 1) * n) || alloc(&gw->Z, (size_t)m * n) ||
       alloc(&gw->H, (size_t)(m + 1) * m) || alloc(&gw->cs, m) || alloc(&gw->sn, m) ||
-      alloc(&gw->g, m + 1) || alloc(&gw->y, m) || alloc(&gw->scal, m + 2) || alloc(&gw->partial, RB) ||
+      alloc(&gw->g, m + 1) || alloc(&gw->y, m) || alloc(&gw->scal, m + 2) ||
+      alloc(&gw->partial, (size_t)(RB > MD_BLOCKS * (m + 1) ? RB : MD_BLOCKS * (m + 1))) ||
       alloc(&gw->diag, pc == 3 ? (size_t)cell_count(cell_geom(c)) * CBS * CBS : (size_t)3 * n) ||
       cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
       cudaMallocHost(&gw->h_st, sizeof(GmState)) != cudaSuccess) {
@@ -252,6 +304,7 @@ static int build_gmres_graph(Context *c, int m, int pc)
   }
   gw->m = m;
   gw->pc = pc;
+  gw->orth = orth;
   const unsigned vb = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
   const unsigned sb = (unsigned)((n * SPMV_G + 255) / 256);
   cudaStream_t s = capture_stream(c);
@@ -274,16 +327,28 @@ static int build_gmres_graph(Context *c, int m, int pc)
     gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st, nb0, c->nbasis[1],
                                c->nbasis[2]);
     nodes += 2;
-    for (int i = 0; i <= j; i++) {
-      gm_dot_partial<<<RB, RT, 0, s>>>(gw->w, gw->V + (size_t)i * n, n, gw->partial, gw->st);
-      gm_dot_final<<<1, 1024, 0, s>>>(gw->partial, RB, hcol + i, 0, gw->st);
-      gm_axpy_neg<<<vb, 256, 0, s>>>(gw->w, gw->V + (size_t)i * n, hcol + i, n, gw->st);
-      nodes += 3;
+    if (orth == 1) {  // CGS2: two block passes h = V^T w, w -= V h
+      const dim3 gp(MD_BLOCKS, (unsigned)(j + 1));
+      const unsigned fb = (unsigned)((j + 1 + 7) / 8);
+      gm_mdot_partial<<<gp, 256, 0, s>>>(gw->V, gw->w, n, gw->partial, gw->st);
+      gm_mdot_final<<<fb, 256, 0, s>>>(gw->partial, j + 1, hcol, gw->st);
+      gm_vupdate<<<vb, 256, 0, s>>>(gw->w, gw->V, hcol, j + 1, n, gw->st);
+      gm_mdot_partial<<<gp, 256, 0, s>>>(gw->V, gw->w, n, gw->partial, gw->st);
+      gm_mdot_final<<<fb, 256, 0, s>>>(gw->partial, j + 1, gw->y, gw->st);
+      gm_vupdate<<<vb, 256, 0, s>>>(gw->w, gw->V, gw->y, j + 1, n, gw->st);
+      nodes += 6;
+    } else {
+      for (int i = 0; i <= j; i++) {
+        gm_dot_partial<<<RB, RT, 0, s>>>(gw->w, gw->V + (size_t)i * n, n, gw->partial, gw->st);
+        gm_dot_final<<<1, 1024, 0, s>>>(gw->partial, RB, hcol + i, 0, gw->st);
+        gm_axpy_neg<<<vb, 256, 0, s>>>(gw->w, gw->V + (size_t)i * n, hcol + i, n, gw->st);
+        nodes += 3;
+      }
     }
     gm_dot_partial<<<RB, RT, 0, s>>>(gw->w, gw->w, n, gw->partial, gw->st);
     gm_dot_final<<<1, 1024, 0, s>>>(gw->partial, RB, hcol + j + 1, 1, gw->st);
     gm_scale_div<<<vb, 256, 0, s>>>(vn, gw->w, hcol + j + 1, n, gw->st);
-    gm_givens<<<1, 1, 0, s>>>(gw->H, gw->cs, gw->sn, gw->g, j, m, gw->st);
+    gm_givens<<<1, 1, 0, s>>>(gw->H, gw->cs, gw->sn, gw->g, j, m, gw->st, orth == 1 ? gw->y : nullptr);
     nodes += 4;
   }
   gm_backsolve<<<1, 1, 0, s>>>(gw->H, gw->g, gw->y, m, gw->st);
@@ -314,12 +379,17 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
 {
   const int m = o->ksp_restart > 0 ? o->ksp_restart : 30;
   const int pc = (o->pc >= 1 && o->pc <= 3) ? o->pc : 0;
+  const int orth = o->orth == 1 ? 1 : 0;
+  if (m > 1000) {
+    set_error("graph GMRES: restart %d above 1000", m);
+    return IGAPGPU_ERR_ARG;
+  }
   if (pc == 3 && c->batch) {
     set_error("cell-block Jacobi (pc = 3) needs a single lattice; a batch takes pc 0, 1 or 2");
     return IGAPGPU_ERR_ARG;
   }
-  if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc) {
-    int r = build_gmres_graph(c, m, pc);
+  if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc || c->gmres_graph->orth != orth) {
+    int r = build_gmres_graph(c, m, pc, orth);
     if (r) return r;
   }
   GraphWork *gw = c->gmres_graph;

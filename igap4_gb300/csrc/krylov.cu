@@ -386,6 +386,7 @@ void igapgpu_default_solver_opts(igapgpu_solver_opts *o)
   o->ksp_max_it = 10000;
   o->pc = 1;
   o->use_graphs = 1;
+  o->orth = 0;
 }
 
 int igapgpu_norm2(igapgpu_t c, const double *x, double *out)

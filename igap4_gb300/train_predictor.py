@@ -20,7 +20,11 @@ import time
 import numpy as np
 
 
-def transient_problem(nelem, dt=1e-2, rho=1.0):
+def transient_problem(nelem, dt=1e-2, rho=1.0, prec="fp64"):
+    """The transient beam of the learned-predictor workload: the reference's
+    three-level law (gradelasttime, default material, density rho, time step
+    dt), clamped at x = 0; prec "split" puts the Newton tangent on the tensor
+    cores (the residual stays FP64, so the converged states do not change)."""
     import igap4_gb300 as ig
 
     par = np.array(ig.LAW_DEFAULT_PAR[ig.LAW_GRADELASTTIME], dtype=float)
@@ -28,6 +32,7 @@ def transient_problem(nelem, dt=1e-2, rho=1.0):
     bct, _ = ig.clamp_bc((0,))
     knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0))
     A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_GRADELASTTIME, par=par, bc_type=bct)
+    A.set_precision(ig.PREC_SPLIT if prec == "split" else ig.PREC_FP64)
     return A, par
 
 
@@ -121,6 +126,22 @@ def evaluate(A, seeds, nsteps, dt, amax, predictor=None, opts=None):
             "prediction_used_fraction": float(np.mean(used)) if predictor else 0.0}
 
 
+def save_network(path, net, scales, meta=None):
+    """Trained parameters (FP32 master copy) and input/output scales."""
+    np.savez(path, params=net.get_params(), scale_u=scales.u, scale_load=scales.load, scale_out=scales.out,
+             mode=scales.mode, meta=json.dumps(meta or {}))
+
+
+def load_network(path, lattice, batch_max=1, storage="bf16"):
+    """(ConvNet on `lattice`, Scales) from a file written by save_network;
+    the network is convolutional, so any lattice size takes the weights."""
+    from .predictor import ConvNet, Scales
+
+    z = np.load(path, allow_pickle=False)
+    sc = Scales(u=float(z["scale_u"]), load=float(z["scale_load"]), out=float(z["scale_out"]), mode=str(z["mode"]))
+    return ConvNet(lattice, batch_max=batch_max, storage=storage, params=z["params"]), sc
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nelem", default="16,4,4")
@@ -135,6 +156,8 @@ def main():
                     help="third input block of the network: load increment, residual at the extrapolation")
     ap.add_argument("--compare-shortened", action="store_true",
                     help="also evaluate the best of the guess and two shortened steps along its correction")
+    ap.add_argument("--prec", default="fp64", choices=["fp64", "split"], help="Newton tangent precision")
+    ap.add_argument("--save", default=None, help="write the trained network (params, scales) to this .npz")
     a = ap.parse_args()
     import torch  # noqa: F401
 
@@ -142,7 +165,7 @@ def main():
 
     nelem = tuple(int(v) for v in a.nelem.split(","))
     opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30, use_graphs=1)
-    A, _ = transient_problem(nelem, a.dt)
+    A, _ = transient_problem(nelem, a.dt, prec=a.prec)
     t0 = time.perf_counter()
     trajs = generate(A, range(1000, 1000 + a.train), a.steps, a.dt, a.amax, opts)
     t_gen = time.perf_counter() - t0
@@ -156,12 +179,17 @@ def main():
         t_train[mode] = time.perf_counter() - t0
     if a.eval_nelem:
         A.close()
-        A, _ = transient_problem(tuple(int(v) for v in a.eval_nelem.split(",")), a.dt)
+        A, _ = transient_problem(tuple(int(v) for v in a.eval_nelem.split(",")), a.dt, prec=a.prec)
         from .predictor import ConvNet
 
         lattice = tuple(n + 2 for n in A.nelem)
         nets = {m: (ConvNet(lattice, batch_max=1, storage="bf16", params=net.get_params()), sc, h)
                 for m, (net, sc, h) in nets.items()}
+    if a.save:
+        net, sc, hist = nets[modes[-1]]
+        save_network(a.save, net, sc, meta={"train_mesh": list(nelem), "train_trajectories": a.train,
+                                            "steps": a.steps, "epochs": a.epochs, "dt": a.dt, "amax": a.amax,
+                                            "loss_first": hist[0], "loss_last": hist[-1]})
     seeds = range(5000, 5000 + a.test)
     plain = evaluate(A, seeds, a.steps, a.dt, a.amax, None, opts)
     from .predictor import ConvNet, Scales, init_params

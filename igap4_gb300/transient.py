@@ -58,13 +58,14 @@ class StepRecord:
 
 
 def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts=None,
-                  record_states: bool = True, device=None):
+                  record_states: bool = True, device=None, log=None):
     """Advance `nsteps` steps of size dt (dt must equal the law's par[7]).
 
     A: igap4_gb300.Assembly with the transient law.  predictor: optional
     callable (u_n, u_nm1, dload) -> guess for u_{n+1}, or an object whose
     candidates(u_n, u_nm1, dload) lists guesses; a guess is kept only if it
     lowers the residual norm below that of u_n (plain Newton fallback).
+    log: optional callable, given each StepRecord as it is made.
     Returns (states [nsteps+1, ndof] or None, list of StepRecord)."""
     import torch
 
@@ -113,6 +114,8 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         dtm = time.perf_counter() - t0
         recs.append(StepRecord(t, st["newton_its"], st["ksp_its_total"], st["fnorm0"], st["fnorm"],
                                st["converged"], dtm, used))
+        if log:
+            log(recs[-1])
         # history shift: u_{n-1} <- u_n, u_n <- u_{n+1}
         A.set_history(0, U)
         A.shift_history()
@@ -121,3 +124,71 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         if record_states:
             states.append(U.cpu().numpy())
     return (np.array(states) if record_states else None), recs
+
+
+def main():
+    """Config-3 style run: the transient beam under a seeded tip-load history,
+    plain Newton from u_n (or a saved predictor), per-step records as JSON.
+
+        python -m igap4_gb300.transient --nelem 64,16,16 --steps 400 --seed 0 --prec split
+    """
+    import argparse
+    import json
+
+    import numpy as np  # noqa: F811
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nelem", default="64,16,16")
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--dt", type=float, default=1e-2)
+    ap.add_argument("--amax", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--prec", default="split", choices=["fp64", "split"])
+    ap.add_argument("--pc", type=int, default=1)
+    ap.add_argument("--predictor", default=None, help=".npz written by train_predictor --save")
+    ap.add_argument("--states", default=None, help="write the trajectory (FP64 states) to this .npy")
+    ap.add_argument("--orth", type=int, default=1, help="GMRES orthogonalisation: 0 MGS, 1 CGS2")
+    a = ap.parse_args()
+    import sys
+    import torch  # noqa: F401
+
+    from .train_predictor import load_network, transient_problem
+
+    nelem = tuple(int(v) for v in a.nelem.split(","))
+    A, _ = transient_problem(nelem, a.dt, prec=a.prec)
+    pred = None
+    if a.predictor:
+        from .predictor import LearnedPredictor
+
+        net, sc = load_network(a.predictor, tuple(n + 2 for n in nelem))
+        pred = LearnedPredictor(net, sc, A=A)
+    load = TipLoad(seed=a.seed, amax=a.amax)
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30,
+                use_graphs=1, pc=a.pc, orth=a.orth)
+
+    def log(r):  # one line per step on stderr, as it happens
+        print(f"t {r.t:.4f} newton {r.newton_its} ksp {r.ksp_its} |F| {r.fnorm0:.3e} -> {r.fnorm:.3e} "
+              f"conv {r.converged} {1e3 * r.seconds:.1f} ms pred {int(r.used_prediction)}", file=sys.stderr,
+              flush=True)
+
+    t0 = time.perf_counter()
+    states, recs = run_transient(A, load, a.steps, a.dt, predictor=pred, opts=opts,
+                                 record_states=a.states is not None, log=log)
+    wall = time.perf_counter() - t0
+    if a.states:
+        np.save(a.states, states)
+    its = np.array([r.newton_its for r in recs])
+    kits = np.array([r.ksp_its for r in recs])
+    ms = np.array([1e3 * r.seconds for r in recs])
+    out = {"nelem": list(nelem), "ndof": A.ndof, "steps": a.steps, "dt": a.dt, "seed": a.seed,
+           "load": {"amp": load.amp.tolist(), "freq": load.freq.tolist()}, "prec": a.prec, "pc": a.pc,
+           "predictor": a.predictor, "wall_s": wall, "converged_all": bool(all(r.converged for r in recs)),
+           "newton_its_per_step": float(its.mean()), "ksp_its_per_step": float(kits.mean()),
+           "ms_per_step": float(ms.mean()), "max_fnorm": float(max(r.fnorm for r in recs)),
+           "records": [{"t": r.t, "newton": r.newton_its, "ksp": r.ksp_its, "f0": r.fnorm0, "f": r.fnorm,
+                        "ms": 1e3 * r.seconds, "pred": r.used_prediction} for r in recs]}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -94,6 +94,11 @@ typedef struct {
   int pc;              /* 0 = none, 1 = Jacobi, 2 = point-block Jacobi (3 x 3 blocks of each control point),
                           3 = cell-block Jacobi (blocks of 2 x 2 x 2 control points, up to 24 x 24; single lattice) */
   int use_graphs;      /* 1: assembly and GMRES cycles replayed as CUDA graphs */
+  int orth;            /* GMRES orthogonalisation: 0 = modified Gram-Schmidt (the reference's
+                          KSPGMRESModifiedGramSchmidtOrthogonalization, src/interface.c:234);
+                          1 = classical Gram-Schmidt applied twice (CGS2: two block passes per
+                          Arnoldi step instead of one dot and one update per basis vector;
+                          graph GMRES only, the host-driven GMRES always uses MGS) */
 } igapgpu_solver_opts;
 
 typedef struct {

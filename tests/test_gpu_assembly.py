@@ -199,6 +199,33 @@ def test_gmres_jacobi_solves():
     assert rel(x, xs) <= 1e-6
 
 
+@pytest.mark.parametrize("law", [po.LAW_LINGRAD, po.LAW_GRADELASTTIME])
+def test_newton_cgs2_matches_mgs(law):
+    """Graph GMRES with classical Gram-Schmidt applied twice (two block passes
+    per Arnoldi step) converges like the reference's modified Gram-Schmidt:
+    the same Newton solution to the tolerance, and GMRES iteration counts
+    within a few of each other."""
+    bct, neu = po.clamp_bc((0,), 1, (0, 0, -1e-3))
+    prob = po.Problem(nelem=(12, 3, 3), L=(4.0, 1.0, 1.0), law=law, bc_type=bct, neumann=neu)
+    if law == po.LAW_GRADELASTTIME:
+        par = prob.params()
+        par[5], par[7] = 1.0, 1e-2
+        prob.par = par
+    out = {}
+    for orth in (0, 1):
+        A = gpu_case(prob)
+        if prob.torder:
+            A.set_state(np.zeros((3, A.ndof)))
+        U = np.zeros(A.ndof)
+        st = A.solve(U, snes_abstol=1e-10, ksp_rtol=1e-8, ksp_restart=60, ksp_max_it=20000, orth=orth)
+        assert st["converged"] == 1, st
+        out[orth] = (U, st)
+        A.close()
+    assert rel(out[1][0], out[0][0]) <= 1e-7
+    k0, k1 = out[0][1]["ksp_its_total"], out[1][1]["ksp_its_total"]
+    assert abs(k1 - k0) <= max(3, 0.05 * k0), (k0, k1)
+
+
 def test_newton_linear_beam_matches_direct_solve():
     """Config-1 style: clamped beam, tip traction, linear law; Newton-GMRES on
     the device converges and agrees with a direct CPU solve."""

@@ -103,9 +103,13 @@ def test_snes_drives_gpu_callbacks_linear():
     assert nits >= 1 and kits >= 1
     orc = po.OracleCase(prob)
     r2, c2 = orc.pattern()
-    K = sp.csr_matrix((orc.tangent(U0[None]), c2, r2), shape=(prob.ndof, prob.ndof))
-    Ustar = U0 - spla.spsolve(K.tocsc(), orc.residual(U0[None]))
-    assert np.linalg.norm(U - Ustar) <= 1e-8 * np.linalg.norm(Ustar)
+    K = sp.csr_matrix((orc.tangent(U0[None]), c2, r2), shape=(prob.ndof, prob.ndof)).tocsc()
+    # the tangent has the Dirichlet rows and columns eliminated: the first
+    # exact step puts the Dirichlet values in place, the second is then exact
+    U1 = U0 - spla.spsolve(K, orc.residual(U0[None]))
+    Ustar = U1 - spla.spsolve(K, orc.residual(U1[None]))
+    # |F| <= 1e-10 leaves the state within the conditioning of the system
+    assert np.linalg.norm(U - Ustar) <= 1e-6 * np.linalg.norm(Ustar)
     assert np.linalg.norm(orc.residual(U[None])) <= 1e-9
 
 

@@ -114,3 +114,46 @@ def test_warp_specialised_tangent_bit_identical(monkeypatch):
     monkeypatch.setenv("IGAPGPU_TCS_WS", "1")
     K2 = A.tangent(U.copy())
     np.testing.assert_array_equal(K1, K2)
+
+
+def slab_rows(prob, ix):
+    """CSR rows of the control points of x-layer ix (every DOF), and the
+    element range whose contributions complete them: the slabs ix-2..ix."""
+    nb = prob.nbasis
+    per_layer = 3 * nb[1] * nb[2]
+    rows = np.arange(ix * per_layer, (ix + 1) * per_layer)
+    per_slab = prob.nelem[1] * prob.nelem[2]
+    return rows, (ix - 2) * per_slab, (ix + 1) * per_slab
+
+
+def rows_of(vals, rowptr, rows):
+    return np.concatenate([vals[rowptr[r]:rowptr[r + 1]] for r in rows])
+
+
+@pytest.mark.parametrize("law,nelem", [(po.LAW_LINGRAD, (32, 8, 8)), (po.LAW_LINGRAD, (16, 4, 4)),
+                                       (po.LAW_GRADELAST, (16, 4, 4)), (po.LAW_GRADELASTTIME, (16, 4, 4))])
+def test_split_and_fp64_vs_cpu_oracle(law, nelem):
+    """Both precisions against the FP64 CPU oracle directly, at the sizes of the
+    assembly sweep and of the static workload: the full residual, and the
+    tangent on the rows of one control-point layer in the middle of the beam
+    (the oracle assembles the three element slabs that complete them).  FP64:
+    1e-12 relative; split: the stated 1e-5 bound."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=nelem, L=(4.0, 1.0, 1.0), law=law, bc_type=bct, neumann=neu)
+    U = po.random_state(prob, 31)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=law, par=prob.params(), bc_type=bct, neumann=neu)
+    A.set_state(U)
+    R64, K64 = A.residual(), A.tangent()
+    A.set_precision(ig.PREC_SPLIT)
+    Ks = A.tangent()
+    orc = po.OracleCase(prob)
+    rowptr, _ = orc.pattern()
+    assert rel(R64, orc.residual(U)) <= 1e-12
+    ix = nelem[0] // 2 + 1
+    rows, e0, e1 = slab_rows(prob, ix)
+    Ko = rows_of(orc.tangent_elements(U, e0, e1), rowptr, rows)
+    e64, es = rel(rows_of(K64, rowptr, rows), Ko), rel(rows_of(Ks, rowptr, rows), Ko)
+    print(f"law {law} {nelem}: FP64 {e64:.2e}, split {es:.2e} vs the CPU oracle")
+    assert e64 <= 1e-12
+    assert es <= SPLIT_TOL
