@@ -295,46 +295,54 @@ def bench_batched(ig, torch, dev, n, steps, warmup, flush, peaks):
 PREDICTOR_FILE = os.path.join(ROOT, "igap4_gb300", "data", "predictor_gradelasttime.npz")
 
 
-def bench_transient(ig, torch, nelem, steps, seed=9001):
+def bench_transient(ig, torch, nelem, steps, start_steps=200, seed=9001, dt=5e-4):
     """Time to |F| <= 1e-8 per transient step, plain Newton from u_n against
     the learned predictor's guess (kept only when it lowers |F|): the
-    reference's three-level law (gradelasttime, density 1, dt 1e-2) on a
-    quadratic beam clamped at x = 0 under a seeded tip-load history (sum of 4
-    sinusoids, amplitudes in [0, 1e-3], frequencies in [0.5, 5]) that the
-    predictor never saw.  Newton: FP64 residual, tangent on the tensor cores,
+    reference's three-level law (gradelasttime, its default material, density
+    1, its default time step 5e-4) on a quadratic beam clamped at x = 0 under a
+    seeded tip-load history (sum of 4 sinusoids, amplitudes in [0, 1e-3],
+    frequencies in [0.5, 5]) that the predictor never saw.  The first
+    start_steps steps (plain Newton, not timed) carry the beam from rest into
+    the regime where the default material transforms (the residual at u_n
+    grows from 1e-6 to order 1); both arms then run the same `steps` steps
+    from that state.  Newton: FP64 residual, tangent on the tensor cores,
     GMRES(100) with Jacobi and two-pass classical Gram-Schmidt, replayed from
-    CUDA graphs.  Each arm runs the same steps from rest; the step time is the
-    wall time of the whole step (predictor, acceptance test, Newton)."""
+    CUDA graphs.  The step time is the wall time of the whole step
+    (predictor, acceptance test, Newton)."""
     from igap4_gb300.train_predictor import load_network, transient_problem
     from igap4_gb300.transient import TipLoad, run_transient
     from igap4_gb300.predictor import LearnedPredictor
 
-    dt = 1e-2
     A, _ = transient_problem(nelem, dt, prec="split")
     opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30,
                 use_graphs=1, pc=1, orth=1)
     load = TipLoad(seed=seed)
-    run_transient(A, load, 3, dt, opts=opts, record_states=False)  # warm-up: graphs captured
+    t0 = time.perf_counter()
+    _, warm = run_transient(A, load, start_steps, dt, opts=opts, record_states=False)
+    start = run_transient.last
+    t_warm = time.perf_counter() - t0
 
     def summary(recs):
         ms = np.array([1e3 * r.seconds for r in recs])
         return {"ms_per_step": float(ms.mean()), "ms_median": float(np.median(ms)),
                 "newton_its_per_step": float(np.mean([r.newton_its for r in recs])),
                 "gmres_its_per_step": float(np.mean([r.ksp_its for r in recs])),
+                "fnorm_at_start_median": float(np.median([r.fnorm0 for r in recs])),
                 "converged_all": bool(all(r.converged for r in recs)),
                 "max_final_fnorm": float(max(r.fnorm for r in recs)),
                 "prediction_used_fraction": float(np.mean([r.used_prediction for r in recs]))}
 
-    t0 = time.perf_counter()
-    _, plain = run_transient(A, load, steps, dt, opts=opts, record_states=False)
-    out = {"workload": f"transient gradelasttime beam {nelem[0]}x{nelem[1]}x{nelem[2]} ({A.ndof} DOF), "
-                       f"{steps} steps of dt=1e-2 from rest, unseen seeded tip-load history (seed {seed})",
+    _, plain = run_transient(A, load, steps, dt, opts=opts, record_states=False, start=start)
+    out = {"workload": f"transient gradelasttime beam {nelem[0]}x{nelem[1]}x{nelem[2]} ({A.ndof} DOF), dt={dt}, "
+                       f"steps {start_steps}..{start_steps + steps} of an unseen seeded tip-load history "
+                       f"(seed {seed})",
            "tolerance": "Newton |F| <= 1e-8 (FP64 residual)", "plain": summary(plain),
-           "plain_wall_s": time.perf_counter() - t0}
+           "warm_steps": {"steps": start_steps, "seconds": t_warm,
+                          "all_converged": bool(all(r.converged for r in warm))}}
     if os.path.exists(PREDICTOR_FILE):
         net, sc = load_network(PREDICTOR_FILE, tuple(n + 2 for n in nelem))
         pred = LearnedPredictor(net, sc, A=A)
-        _, learned = run_transient(A, load, steps, dt, predictor=pred, opts=opts, record_states=False)
+        _, learned = run_transient(A, load, steps, dt, predictor=pred, opts=opts, record_states=False, start=start)
         out["learned"] = summary(learned)
         out["time_ratio_learned_vs_plain"] = out["learned"]["ms_per_step"] / out["plain"]["ms_per_step"]
         out["its_ratio_learned_vs_plain"] = (out["learned"]["newton_its_per_step"] /

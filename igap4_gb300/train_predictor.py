@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
 
 import numpy as np
@@ -45,6 +46,8 @@ def generate(A, seeds, nsteps, dt, amax, opts=None):
         states, recs = run_transient(A, load, nsteps, dt, opts=opts)
         loads = np.array([0.0] + [load.value((n + 1) * dt) for n in range(nsteps)])
         trajs.append((states, loads, recs, load))
+        print(f"trajectory {s}: {nsteps} steps, {np.mean([r.newton_its for r in recs]):.2f} Newton its/step, "
+              f"all converged {all(r.converged for r in recs)}", file=sys.stderr, flush=True)
     return trajs
 
 
@@ -112,13 +115,29 @@ def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None
     return net, scales, hist
 
 
-def evaluate(A, seeds, nsteps, dt, amax, predictor=None, opts=None):
+def eval_starts(A, seeds, n0, dt, amax, opts=None):
+    """Per seed, the state after n0 plain steps from rest: (u_n, u_{n-1}, n0),
+    so that the arms of an evaluation are timed on the same later window."""
+    from .transient import TipLoad, run_transient
+
+    out = {}
+    for s in seeds:
+        if n0 <= 0:
+            out[int(s)] = None
+            continue
+        run_transient(A, TipLoad(seed=int(s), amax=amax), n0, dt, opts=opts, record_states=False)
+        out[int(s)] = run_transient.last
+    return out
+
+
+def evaluate(A, seeds, nsteps, dt, amax, predictor=None, opts=None, starts=None):
     from .transient import TipLoad, run_transient
 
     its, times, used = [], [], []
     for s in seeds:
         load = TipLoad(seed=int(s), amax=amax)
-        _, recs = run_transient(A, load, nsteps, dt, predictor=predictor, opts=opts, record_states=False)
+        _, recs = run_transient(A, load, nsteps, dt, predictor=predictor, opts=opts, record_states=False,
+                                start=(starts or {}).get(int(s)))
         its += [r.newton_its for r in recs]
         times += [r.seconds for r in recs]
         used += [r.used_prediction for r in recs]
@@ -158,13 +177,17 @@ def main():
                     help="also evaluate the best of the guess and two shortened steps along its correction")
     ap.add_argument("--prec", default="fp64", choices=["fp64", "split"], help="Newton tangent precision")
     ap.add_argument("--save", default=None, help="write the trained network (params, scales) to this .npz")
+    ap.add_argument("--eval-start", type=int, default=0,
+                    help="plain steps from rest before the evaluated window (not timed)")
+    ap.add_argument("--eval-steps", type=int, default=None, help="evaluated steps (default --steps)")
     a = ap.parse_args()
     import torch  # noqa: F401
 
     from .predictor import LearnedPredictor
 
     nelem = tuple(int(v) for v in a.nelem.split(","))
-    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=60, ksp_max_it=3000, snes_max_it=30, use_graphs=1)
+    opts = dict(snes_abstol=1e-8, ksp_rtol=1e-5, ksp_restart=100, ksp_max_it=5000, snes_max_it=30, use_graphs=1,
+                orth=1)
     A, _ = transient_problem(nelem, a.dt, prec=a.prec)
     t0 = time.perf_counter()
     trajs = generate(A, range(1000, 1000 + a.train), a.steps, a.dt, a.amax, opts)
@@ -175,7 +198,8 @@ def main():
     nets, t_train = {}, {}
     for mode in modes:
         t0 = time.perf_counter()
-        nets[mode] = train(A, X, Y, epochs=a.epochs, R=R if mode == "residual" else None)
+        nets[mode] = train(A, X, Y, epochs=a.epochs, R=R if mode == "residual" else None,
+                           log=lambda msg: print(msg, file=sys.stderr, flush=True))
         t_train[mode] = time.perf_counter() - t0
     if a.eval_nelem:
         A.close()
@@ -191,23 +215,26 @@ def main():
                                             "steps": a.steps, "epochs": a.epochs, "dt": a.dt, "amax": a.amax,
                                             "loss_first": hist[0], "loss_last": hist[-1]})
     seeds = range(5000, 5000 + a.test)
-    plain = evaluate(A, seeds, a.steps, a.dt, a.amax, None, opts)
+    ev_steps = a.eval_steps or a.steps
+    starts = eval_starts(A, seeds, a.eval_start, a.dt, a.amax, opts)
+    plain = evaluate(A, seeds, ev_steps, a.dt, a.amax, None, opts, starts)
     from .predictor import ConvNet, Scales, init_params
 
     extrap_net = ConvNet(tuple(n + 2 for n in A.nelem), batch_max=1, storage="bf16", params=init_params(0))
-    extrap = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(extrap_net, Scales(), scaled=False), opts)
+    extrap = evaluate(A, seeds, ev_steps, a.dt, a.amax, LearnedPredictor(extrap_net, Scales(), scaled=False), opts,
+                      starts)
     out = {"train_mesh": list(nelem), "eval_mesh": list(A.nelem), "train_trajectories": a.train,
-           "steps": a.steps, "samples": len(X), "generation_s": t_gen, "plain": plain,
-           "extrapolation_only": extrap}
+           "steps": a.steps, "dt": a.dt, "eval_window": [a.eval_start, a.eval_start + ev_steps],
+           "samples": len(X), "generation_s": t_gen, "plain": plain, "extrapolation_only": extrap}
     for mode, (net, scales, hist) in nets.items():
-        learned = evaluate(A, seeds, a.steps, a.dt, a.amax, LearnedPredictor(net, scales, A=A), opts)
+        learned = evaluate(A, seeds, ev_steps, a.dt, a.amax, LearnedPredictor(net, scales, A=A), opts, starts)
         key = "learned" if mode == modes[-1] else f"learned_{mode}"
         out[key] = learned
         out[key + "_training"] = {"inputs": mode, "seconds": t_train[mode], "loss_first": hist[0],
                                   "loss_last": hist[-1]}
         if a.compare_shortened:
-            out[key + "_best_of_shortened"] = evaluate(A, seeds, a.steps, a.dt, a.amax,
-                                                       LearnedPredictor(net, scales, scaled=True, A=A), opts)
+            out[key + "_best_of_shortened"] = evaluate(A, seeds, ev_steps, a.dt, a.amax,
+                                                       LearnedPredictor(net, scales, scaled=True, A=A), opts, starts)
     out["time_ratio_learned_vs_plain"] = out["learned"]["seconds_per_step"] / plain["seconds_per_step"]
     out["its_ratio_learned_vs_plain"] = out["learned"]["newton_its_per_step"] / plain["newton_its_per_step"]
     print(json.dumps(out))

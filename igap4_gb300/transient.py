@@ -58,7 +58,7 @@ class StepRecord:
 
 
 def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts=None,
-                  record_states: bool = True, device=None, log=None):
+                  record_states: bool = True, device=None, log=None, start=None):
     """Advance `nsteps` steps of size dt (dt must equal the law's par[7]).
 
     A: igap4_gb300.Assembly with the transient law.  predictor: optional
@@ -66,7 +66,11 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     candidates(u_n, u_nm1, dload) lists guesses; a guess is kept only if it
     lowers the residual norm below that of u_n (plain Newton fallback).
     log: optional callable, given each StepRecord as it is made.
-    Returns (states [nsteps+1, ndof] or None, list of StepRecord)."""
+    start: optional (u_n, u_{n-1}, n0): continue a trajectory after step n0
+    (device FP64 vectors) instead of starting from rest.
+    Returns (states [nsteps+1, ndof] or None, list of StepRecord); the
+    state where the run ended is left in run_transient.last as
+    (u_n, u_{n-1}, n), a `start` for the next run."""
     import torch
 
     dev = device or torch.device("cuda")
@@ -77,15 +81,18 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     if opts:
         o.update(opts)
     zero = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
-    A.set_history(1, zero)
-    A.set_history(2, zero)
-    states = [np.zeros(A.ndof)] if record_states else None
-    recs = []
+    n0 = 0
     u_n = zero.clone()
     u_nm1 = zero.clone()
+    if start is not None:
+        u_n, u_nm1, n0 = start[0].clone(), start[1].clone(), int(start[2])
+    A.set_history(1, u_n)
+    A.set_history(2, u_nm1)
+    states = [u_n.cpu().numpy()] if record_states else None
+    recs = []
     F = torch.zeros_like(zero)
-    prev_load = 0.0
-    for n in range(nsteps):
+    prev_load = load.value(n0 * dt) if n0 > 0 else 0.0
+    for n in range(n0, n0 + nsteps):
         t = (n + 1) * dt
         A.set_neumann(load.table(t))
         t0 = time.perf_counter()
@@ -123,6 +130,7 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         prev_load = load.value(t)
         if record_states:
             states.append(U.cpu().numpy())
+    run_transient.last = (u_n, u_nm1, n0 + nsteps)
     return (np.array(states) if record_states else None), recs
 
 
