@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libigapgpu.so")
 
 LAW_GRADELAST, LAW_GRADELASTTIME, LAW_LINGRAD = 0, 1, 2
-PREC_FP64, PREC_SPLIT = 0, 1
+PREC_FP64, PREC_SPLIT, PREC_OZAKI = 0, 1, 2
+REASON_REJECTED = -9  # igapgpu_solve: initial |F| above snes_f0_max
 LAW_TORDER = {LAW_GRADELAST: 0, LAW_GRADELASTTIME: 2, LAW_LINGRAD: 0}
 # default parameters of the reference plugins (phys/physgradelast.c:21,
 # phys/physgradelasttime.c:21) and of the linear law
@@ -53,7 +54,7 @@ class SolverOpts(ctypes.Structure):
                 ("linesearch", ctypes.c_int), ("ksp_restart", ctypes.c_int),
                 ("ksp_rtol", ctypes.c_double), ("ksp_abstol", ctypes.c_double),
                 ("ksp_dtol", ctypes.c_double), ("ksp_max_it", ctypes.c_int), ("pc", ctypes.c_int),
-                ("use_graphs", ctypes.c_int), ("orth", ctypes.c_int)]
+                ("use_graphs", ctypes.c_int), ("orth", ctypes.c_int), ("snes_f0_max", ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):

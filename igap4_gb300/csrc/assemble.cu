@@ -895,8 +895,11 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   if (do_res && do_tan) rc = run_colours<LK, true, true>(c, L, RR, vals);   \
   else if (do_res) rc = run_colours<LK, true, false>(c, L, RR, vals);       \
   else rc = run_colours<LK, false, true>(c, L, RR, vals);
-  // split precision: the residual stays FP64, the tangent goes to the tensor cores
-  const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT;
+  // split precision: the residual stays FP64, the tangent goes to the tensor
+  // cores (TF32x3); FP64-quality tensor-core precision: the linear law's
+  // tangent from BF16 slices when they were built, else the FP64 kernel
+  const bool oz_tan = do_tan && c->prec == IGAPGPU_PREC_OZAKI && c->d_oz;
+  const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT && !oz_tan;
   // nonlinear laws: every point's law outputs in one launch, so that the
   // colour launches do not evaluate the law colour after colour
   DevLaw L = c->devlaw();
@@ -920,7 +923,7 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   if (rc) return rc;
   if (do_tan && !fp64_tan) {
     IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
-    rc = launch_tc_tangent(c, vals, L);
+    rc = oz_tan ? launch_tc_ozaki(c, vals) : launch_tc_tangent(c, vals, L);
     if (rc) return rc;
     if (!c->capturing) {  // a graph replay checks the error word itself
       int herr = 0;

@@ -144,6 +144,9 @@ struct Context {
   float *d_geof = nullptr;     // FP32 copy for the split-precision tangent
   float *d_gop = nullptr;      // linear law: sqrt(w)-weighted Gram operands in MMA layout (split tangent)
   int gop_state = -1;          // -1 not decided, 0 off, 1 on
+  void *d_oz = nullptr;        // linear law: BF16 slices of the Gram operands (FP64-quality tensor-core tangent)
+  void *d_ozexp = nullptr;     // their per-row power-of-two exponents (int8, 88 per element)
+  int oz_state = -1;           // -1 not decided, 0 off, 1 on
   double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
   double *d_preD = nullptr;
   int pre_state = -1;          // -1 not decided, 0 off, 1 on
@@ -174,8 +177,8 @@ struct Context {
   cudaStream_t stream = nullptr;
   // CUDA graphs (graph.cu)
   GraphWork *gmres_graph = nullptr;
-  cudaGraphExec_t asm_graph[8] = {};
-  int64_t asm_graph_nodes[8] = {};
+  cudaGraphExec_t asm_graph[12] = {};  // key: residual + 2 tangent + 4 precision mode
+  int64_t asm_graph_nodes[12] = {};
   bool capturing = false;
   // batched instances (batch.cu): this context is then their block-diagonal union
   Batch *batch = nullptr;
@@ -261,6 +264,9 @@ int launch_tc_tangent(Context *c, double *vals, const DevLaw &L);
 int launch_tc_gram(Context *c, double *vals);
 // cached: every instance has its Gram operands (d_gop); persistent CTAs per SM of nsm
 int launch_tc_gram_batch(Context *c, const BatchArgs &a, int nsm, double *vals, bool cached);
+// tc_ozaki.cu (linear law, BF16 slices, FP64-quality)
+int ensure_ozaki_operands(Context *c);
+int launch_tc_ozaki(Context *c, double *vals);
 // builds d_gop once (linear law, FP64 geometry cache present, memory allows)
 int ensure_gram_operands(Context *c);
 // krylov.cu

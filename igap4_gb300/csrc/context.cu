@@ -164,7 +164,7 @@ static int free_ctx(Context *c)
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
-                  c->d_diag, c->d_bdiag, c->d_cinv, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_gop, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
+                  c->d_diag, c->d_bdiag, c->d_cinv, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_gop, c->d_oz, c->d_ozexp, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int d = 0; d < 3; d++) {
@@ -755,12 +755,17 @@ int igapgpu_set_neumann(igapgpu_t c, const double *table)
 int igapgpu_set_precision(igapgpu_t c, int mode)
 {
   if (!c) return IGAPGPU_ERR_ARG;
-  if (mode != IGAPGPU_PREC_FP64 && mode != IGAPGPU_PREC_SPLIT) {
+  if (mode != IGAPGPU_PREC_FP64 && mode != IGAPGPU_PREC_SPLIT && mode != IGAPGPU_PREC_OZAKI) {
     set_error("unknown precision mode %d", mode);
+    return IGAPGPU_ERR_ARG;
+  }
+  if (mode == IGAPGPU_PREC_OZAKI && c->batch) {
+    set_error("IGAPGPU_PREC_OZAKI is for single lattices; a batch takes FP64 or split precision");
     return IGAPGPU_ERR_ARG;
   }
   c->prec = mode;
   if (mode == IGAPGPU_PREC_SPLIT) return c->batch ? batch_prepare_split(c) : ensure_gram_operands(c);
+  if (mode == IGAPGPU_PREC_OZAKI) return ensure_ozaki_operands(c);
   return IGAPGPU_OK;
 }
 

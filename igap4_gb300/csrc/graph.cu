@@ -267,7 +267,7 @@ void graph_release(Context *c)
 {
   free_graph(c->gmres_graph);
   c->gmres_graph = nullptr;
-  for (int i = 0; i < 8; i++) {
+  for (int i = 0; i < 12; i++) {
     if (c->asm_graph[i]) cudaGraphExecDestroy(c->asm_graph[i]);
     c->asm_graph[i] = nullptr;
   }
@@ -451,7 +451,7 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
 // captured once per (res, tan, precision) and replayed.
 int assembly_graph(Context *c, bool do_res, bool do_tan)
 {
-  const int key = (do_res ? 1 : 0) + (do_tan ? 2 : 0) + (c->prec == IGAPGPU_PREC_SPLIT ? 4 : 0);
+  const int key = (do_res ? 1 : 0) + (do_tan ? 2 : 0) + 4 * c->prec;
   if (!c->asm_graph[key]) {
     // first use: run it directly (one-time set-up such as kernel attributes
     // and constant tables happens outside the capture), then capture it
@@ -489,7 +489,7 @@ int assembly_graph(Context *c, bool do_res, bool do_tan)
   }
   // the error word is cleared inside the graph; it is read after the replay
   // when a kernel of the graph has bounded waits
-  const bool waits = c->batch || (c->prec == IGAPGPU_PREC_SPLIT && do_tan);
+  const bool waits = c->batch || (c->prec != IGAPGPU_PREC_FP64 && do_tan);
   if (waits) IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
   IGAP_CUDA(cudaGraphLaunch(c->asm_graph[key], c->stream));
   count_launch((int)c->asm_graph_nodes[key]);

@@ -387,6 +387,7 @@ void igapgpu_default_solver_opts(igapgpu_solver_opts *o)
   o->pc = 1;
   o->use_graphs = 1;
   o->orth = 0;
+  o->snes_f0_max = 0.0;
 }
 
 int igapgpu_norm2(igapgpu_t c, const double *x, double *out)
@@ -481,6 +482,14 @@ int igapgpu_solve(igapgpu_t c, double *U, const igapgpu_solver_opts *opts, igapg
   if ((r = dev_norm2(c, F, &fnorm))) return r;
   S.fnorm0 = fnorm;
   S.reason = 0;
+  if (o.snes_f0_max > 0.0 && !(fnorm <= o.snes_f0_max)) {  // rejected initial iterate: U unchanged
+    S.reason = IGAPGPU_REASON_REJECTED;
+    S.fnorm = fnorm;
+    if (uh) IGAP_CUDA(cudaMemcpyAsync(U, Ud, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    IGAP_CUDA(cudaStreamSynchronize(c->stream));
+    if (st) *st = S;
+    return IGAPGPU_OK;
+  }
   for (int it = 0; it < o.snes_max_it; it++) {
     if (!isfinite(fnorm)) { S.reason = -4; break; }
     if (fnorm <= o.snes_abstol) { S.reason = 2; break; }

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "element.cuh"
 #include "tcgen05.cuh"
+#include "gram_common.cuh"
 
 namespace igap {
 
@@ -41,11 +42,6 @@ constexpr uint32_t G_WAIT_LIMIT = 1u << 26;
 constexpr uint32_t G_TMEM_COLS = 128;
 constexpr int GPAD = 84;                     // row stride of the staged Gram matrix
 
-__device__ __forceinline__ int hess_slot(int i, int m)
-{
-  const int a = i < m ? i : m, b = i < m ? m : i;
-  return a == 0 ? b : (a == 1 ? 2 + b : 5);  // (0,0)0 (0,1)1 (0,2)2 (1,1)3 (1,2)4 (2,2)5
-}
 
 __device__ __forceinline__ bool tc_wait_ge(const int *p, int target)
 {
@@ -58,19 +54,6 @@ __device__ __forceinline__ bool tc_wait_ge(const int *p, int target)
   return false;
 }
 }  // namespace
-
-// float -> double on the integer pipe (bit-exact with the conversion for
-// normal numbers and zeros; subnormals, infinities and NaN take the
-// conversion instruction): FP64 work is scarce on this GPU.
-__device__ __forceinline__ double f32_to_f64(float f)
-{
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu)
-    return (b & 0x7fffffffu) == 0u ? __hiloint2double((int)(b & 0x80000000u), 0) : (double)f;
-  const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hi, (int)(b << 29));
-}
 
 // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc
 // for every (b,d), (c,e) (6,561 slots, each once per element), added into the

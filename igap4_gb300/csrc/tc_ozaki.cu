@@ -1,0 +1,494 @@
+// FP64-quality tangent of the linear isotropic strain-gradient law on the
+// tensor cores: the Gram form of tc_gram.cu with the sqrt(w)-weighted
+// operand S split error-free into BF16 slices (the Ozaki scheme: Ozaki,
+// Ogita, Oishi, Rump, Numer. Algorithms 59 (2012); GEMM on tensor cores:
+// Mukunoki, Ozaki, Ogita, Imamura, ICCS 2020).
+//
+// Per element, row r = (b, i) of S (81 rows, K = 64 points x (1 + 3) = 256
+// columns) is scaled by its own power of two 2^(8 - E_r) (max |S_r| < 2^E_r)
+// and cut into four 8-bit integer slices,
+//   S_r = 2^(E_r - 8) (D1 + D2 2^-8 + D3 2^-16 + D4 2^-24),  |D_j| <= 256,
+// each stored exactly in BF16 as D_j' = D_j 2^(-8(j-1)).  The Gram matrix
+// G = S S^T is then
+//   G_rc = 2^(E_r + E_c - 16) sum_{i,j} D_i'[r] . D_j'[c],
+// and the tensor cores form the products with FP32 accumulation in four
+// accumulators: acc0 = D1 D1^T holds integers below 2^24 (256 x 255^2) and
+// acc1 = X = D1 D2'^T multiples of 2^-8 below 2^16, so both are exact however
+// the tensor core rounds its sums; acc2 = the products with i + j = 4 and
+// acc3 those with i + j = 5, 6, each rounded at its own scale (2^-16 and
+// 2^-24 of the leading term).  Products with i + j >= 7 are left out.  The
+// epilogue stages X and forms G = (acc0 + t) + (e + acc2 + acc3) in FP64,
+// t + e = X + X^T exactly (FP32 two-sum), the power of two applied on the
+// integer pipe.  A model of the scheme on random operands with this row
+// scaling gives 2e-10 relative Frobenius error whether the tensor core
+// rounds its sums to nearest or towards zero (one accumulator for i + j >= 4
+// and an FP32 X + X^T: 1e-9 towards zero; stopping at i + j = 5: 1e-8).
+// K = lam G + mu (G^T + tr G I) per 3 x 3 block in FP64
+// and adds it into the FP64 CSR values with L2 reductions (colour order, as
+// every other tangent kernel here).  Relative error of the tangent: about
+// 2^-32 of the entries' natural scale (~1e-10), against the 2e-6 of TF32x3.
+//
+// One persistent CTA per SM (four accumulators of 96 columns fill the tensor
+// memory, so they are single buffered and drained into shared memory right
+// after the last MMA):
+//   warp 0 (one thread): bulk copies of the element's chunks (4 slices x
+//     2 K-steps x 11 row groups x 256 B = 22,528 B) into OZ_NS stages,
+//   warp 1 (one thread): 24 MMAs (M128 N96 K16, kind::f16 BF16) per chunk
+//     into four accumulators
+//     straight from the stage (the slices are built once, already in the
+//     operand layout; the same tile is A and B),
+//   warps 4-7: drain TMEM -> G (FP64, shared memory), free the accumulators,
+//     form K and scatter it.
+// Every mbarrier wait is bounded; a CTA that gives up waits (bounded) for
+// its copies and MMAs in flight and frees its tensor memory.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <limits.h>
+#include <stdlib.h>
+
+#include "common.cuh"
+#include "element.cuh"
+#include "gram_common.cuh"
+#include "tcgen05.cuh"
+
+namespace igap {
+
+namespace {
+constexpr int OZ_THREADS = 256;
+constexpr int OZ_ROWS = 81;
+constexpr int OZ_RG = 11;                               // row groups holding rows 0..87
+constexpr int OZ_KS_BYTES = OZ_RG * 256;                // 2816: one K-step of 16 BF16 values
+constexpr int OZ_SLICE_BYTES = 2 * OZ_KS_BYTES;         // 5632: a chunk of 8 points (K = 32)
+constexpr int OZ_CH_BYTES = 4 * OZ_SLICE_BYTES;         // 22528: the four slices of a chunk
+constexpr int OZ_STAGE = OZ_CH_BYTES + 5 * 256;         // an M = 128 read of the last K-step stays inside
+constexpr int OZ_NS = 5;                                // copy stages
+constexpr int OZ_GP = 82;                               // row stride (doubles) of the staged G
+constexpr int OZ_XP = 84;                               // row stride (floats) of the staged X
+constexpr int OZ_EXP = 88;                              // exponent bytes per element
+constexpr uint32_t OZ_TMEM_COLS = 512;
+constexpr uint32_t OZ_WAIT_LIMIT = 1u << 26;
+static_assert(OZ_STAGE % 16 == 0 && OZ_CH_BYTES % 16 == 0, "bulk copies and descriptors need 16-byte alignment");
+
+struct OzSmem {
+  unsigned char stage[OZ_NS][OZ_STAGE];
+  double G[OZ_ROWS * OZ_GP];
+  float X[OZ_ROWS * OZ_XP];
+  unsigned char pos[NB * NB];
+  int64_t rowp[NE];
+  int ex[OZ_EXP];
+  uint64_t full[OZ_NS], empty[OZ_NS], accfull, accempty;
+  uint32_t cp_n[OZ_NS], mm_n[OZ_NS], accf_n;
+  uint32_t taddr;
+  int abort;
+};
+
+__device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(mbar)) : "memory");
+}
+
+__device__ __forceinline__ bool oz_wait(uint64_t *mbar, uint32_t parity, volatile int *abort)
+{
+  const uint32_t addr = tc::smem_u32(mbar);
+  for (uint32_t it = 0; it < OZ_WAIT_LIMIT; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255u) == 255u && *abort) return false;
+  }
+  return false;
+}
+
+// Column kk (0..31) of a chunk of 8 points: kk < 8 the gradient slot of
+// point kk, else the Hessian slot (i, m) of point (kk - 8) / 3, times ell.
+__device__ __forceinline__ double oz_value(const double *__restrict__ geo, int64_t e, int npts, int ch, int r,
+                                           int kk, double ell, int *bad)
+{
+  if (r >= OZ_ROWS) return 0.0;
+  const int b = r / 3, i = r % 3;
+  int p, slot;
+  bool hess;
+  if (kk < PW) {
+    p = kk;
+    slot = 1 + i;
+    hess = false;
+  } else {
+    p = (kk - PW) / 3;
+    slot = 4 + hess_slot(i, (kk - PW) % 3);
+    hess = true;
+  }
+  const int q = ch * PW + p;
+  if (q >= npts) return 0.0;
+  const double *g = geo + (e * npts + q) * GEO_STRIDE;
+  const double w = g[NB * NDD];
+  if (!(w > 0.0)) {
+    atomicExch(bad, 1);
+    return 0.0;
+  }
+  return sqrt(w) * (hess ? ell : 1.0) * g[NDD * b + slot];
+}
+}  // namespace
+
+// Slices of every element, once per context (state independent): one CTA per
+// element (grid-stride).  Pass 1: per row the exponent E_r with
+// max |S_r| < 2^E_r; pass 2: the four slices in the MMA operand layout,
+// out[e][chunk][slice][K-step][row group][K half][row][8 BF16], and E_r.
+__global__ void __launch_bounds__(256) ozaki_operand_kernel(const double *__restrict__ geo, int npts, int nchunk,
+                                                            int64_t nelem, double ell,
+                                                            __nv_bfloat16 *__restrict__ out,
+                                                            signed char *__restrict__ expo, int *__restrict__ bad)
+{
+  __shared__ int rexp[OZ_EXP];
+  const int K = nchunk * 32;
+  for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x) {
+    for (int r = threadIdx.x; r < OZ_EXP; r += blockDim.x) rexp[r] = INT_MIN;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < OZ_ROWS * K; idx += blockDim.x) {
+      const int r = idx / K, k = idx % K;
+      const double v = oz_value(geo, e, npts, k / 32, r, k % 32, ell, bad);
+      if (v != 0.0) {
+        int ex;
+        frexp(v, &ex);
+        atomicMax(&rexp[r], ex);
+      }
+    }
+    __syncthreads();
+    const int per_chunk = OZ_CH_BYTES / 2;  // BF16 values
+    __nv_bfloat16 *oe = out + (size_t)e * nchunk * per_chunk;
+    for (int idx = threadIdx.x; idx < nchunk * 32 * OZ_RG * 8; idx += blockDim.x) {
+      // idx = ((ch * 32 + kk) * 88 + r)
+      const int r = idx % (OZ_RG * 8), kk = (idx / (OZ_RG * 8)) % 32, ch = idx / (OZ_RG * 8 * 32);
+      const int E = rexp[r] == INT_MIN ? 0 : rexp[r];
+      double x = ldexp(oz_value(geo, e, npts, ch, r, kk, ell, bad), 8 - E);  // |x| < 256
+      const int ks = kk / 16, half = (kk / 8) % 2, f = kk % 8, rg = r / 8, r8 = r % 8;
+      const size_t off = (size_t)ch * per_chunk + (size_t)ks * (OZ_KS_BYTES / 2) + rg * 128 + half * 64 + r8 * 8 + f;
+      for (int j = 0; j < 4; j++) {
+        const double d = j < 3 ? trunc(x) : rint(x);  // |d| <= 256: exact in BF16
+        x = (x - d) * 256.0;                         // exact
+        oe[off + (size_t)j * (OZ_SLICE_BYTES / 2)] = __float2bfloat16_rn(ldexpf((float)d, -8 * j));
+      }
+    }
+    for (int r = threadIdx.x; r < OZ_EXP; r += blockDim.x)
+      expo[e * OZ_EXP + r] = (signed char)(r < OZ_ROWS && rexp[r] != INT_MIN ? rexp[r] : 0);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    tco_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz, double *__restrict__ vals,
+               int *err, const unsigned char *__restrict__ ops, const signed char *__restrict__ expo)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  OzSmem &S = *reinterpret_cast<OzSmem *>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  volatile int *abort = &S.abort;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, OZ_TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < OZ_NS; i++) {
+      tc::mbar_init(&S.full[i], 1);
+      tc::mbar_init(&S.empty[i], 1);
+      S.cp_n[i] = S.mm_n[i] = 0;
+    }
+    tc::mbar_init(&S.accfull, 1);
+    tc::mbar_init(&S.accempty, 128);
+    S.accf_n = 0;
+    S.abort = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = S.taddr;
+  const int nelem_c = ncx * ncy * ncz;
+  const int nmine = (int)blockIdx.x < nelem_c ? (nelem_c - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const uint32_t nchunk = (uint32_t)((m.npts + PW - 1) / PW);
+  auto element = [&](int j, int &ex, int &ey, int &ez) {
+    const int ei = (int)blockIdx.x + j * (int)gridDim.x;
+    const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
+    ex = cx + 3 * ix;
+    ey = cy + 3 * iy;
+    ez = cz + 3 * iz;
+    return ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+  };
+  if (warp == 0) {
+    if (lane == 0) {  // producer
+      uint32_t s = 0, cpn[OZ_NS] = {};
+      bool ok = true;
+      for (int j = 0; j < nmine && ok; j++) {
+        int ex, ey, ez;
+        const unsigned char *src = ops + (size_t)element(j, ex, ey, ez) * nchunk * OZ_CH_BYTES;
+        for (uint32_t c = 0; c < nchunk; c++, s++) {
+          const int st = (int)(s % OZ_NS);
+          if (s >= (uint32_t)OZ_NS && !oz_wait(&S.empty[st], ((s / OZ_NS) - 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&S.full[st], (uint32_t)OZ_CH_BYTES);
+          tc::bulk_g2s(S.stage[st], src + (size_t)c * OZ_CH_BYTES, (uint32_t)OZ_CH_BYTES, &S.full[st]);
+          cpn[st]++;
+        }
+      }
+      if (!ok) S.abort = 1;
+      for (int i = 0; i < OZ_NS; i++) S.cp_n[i] = cpn[i];
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = tc::instr_desc(1, 128, 96);  // BF16 x BF16 -> FP32, M128 N96
+      const uint32_t acc0 = taddr, acc1 = taddr + 128u, acc2 = taddr + 256u, acc3 = taddr + 384u;
+      uint32_t s = 0, mmn[OZ_NS] = {}, accn = 0;
+      bool ok = true;
+      for (int j = 0; j < nmine && ok; j++) {
+        if (j >= 1 && !oz_wait(&S.accempty, ((uint32_t)j - 1) & 1, abort)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        for (uint32_t c = 0; c < nchunk; c++, s++) {
+          const int st = (int)(s % OZ_NS);
+          if (!oz_wait(&S.full[st], (s / OZ_NS) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t base = tc::smem_u32(S.stage[st]);
+          for (int ks = 0; ks < 2; ks++) {
+            uint64_t d[4];
+            for (int q = 0; q < 4; q++)
+              d[q] = tc::smem_desc(base + (uint32_t)(q * OZ_SLICE_BYTES + ks * OZ_KS_BYTES), 128, 256);
+            const uint32_t first = (c == 0 && ks == 0) ? 0u : 1u;
+            tc::mma_bf16(acc0, d[0], d[0], idesc, first);       // i + j = 2
+            tc::mma_bf16(acc1, d[0], d[1], idesc, first);       // i + j = 3: X (its transpose in the epilogue)
+            tc::mma_bf16(acc2, d[0], d[2], idesc, first);       // i + j = 4
+            tc::mma_bf16(acc2, d[2], d[0], idesc, 1u);
+            tc::mma_bf16(acc2, d[1], d[1], idesc, 1u);
+            tc::mma_bf16(acc3, d[0], d[3], idesc, first);       // i + j = 5
+            tc::mma_bf16(acc3, d[3], d[0], idesc, 1u);
+            tc::mma_bf16(acc3, d[1], d[2], idesc, 1u);
+            tc::mma_bf16(acc3, d[2], d[1], idesc, 1u);
+            tc::mma_bf16(acc3, d[1], d[3], idesc, 1u);          // i + j = 6
+            tc::mma_bf16(acc3, d[3], d[1], idesc, 1u);
+            tc::mma_bf16(acc3, d[2], d[2], idesc, 1u);
+          }
+          tc::mma_commit(&S.empty[st]);
+          mmn[st]++;
+        }
+        if (!ok) break;
+        tc::mma_commit(&S.accfull);
+        accn++;
+      }
+      if (!ok) S.abort = 1;
+      for (int i = 0; i < OZ_NS; i++) S.mm_n[i] = mmn[i];
+      S.accf_n = accn;
+    }
+  } else if (warp >= 4) {  // epilogue, 128 threads: warp & 3 is the TMEM lane quarter
+    const int t = tid - 128, quarter = warp & 3;
+    const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+    const int nbv[3] = {m.nbasis[0], nb1, nb2};
+    const double lam = L.par[0], mu = L.par[1];
+    bool ok = true;
+    for (int j = 0; j < nmine && ok; j++) {
+      int ex, ey, ez;
+      const int64_t eg = element(j, ex, ey, ez);
+      if (t < NE) {
+        const int b = t / 3, dd = t % 3;
+        const int64_t cpb = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+        S.rowp[t] = __ldg(m.rowptr + 3 * cpb + dd);
+      }
+      if (t < OZ_EXP) S.ex[t] = (int)__ldg(expo + eg * OZ_EXP + t);
+      for (int i = t; i < NB * NB; i += 128) {
+        const int b = i / NB, c = i % NB;
+        S.pos[i] = (unsigned char)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9,
+                                              ey + (c / 3) % 3, ez + c % 3, nbv);
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // exponents in place
+      // the four epilogue warps take the same decision (a named-barrier OR)
+      const uint32_t got = oz_wait(&S.accfull, (uint32_t)j & 1, abort) ? 1u : 0u;
+      uint32_t any_failed;
+      asm volatile(
+          "{\n\t.reg .pred p, q;\n\t"
+          "setp.eq.u32 p, %1, 0;\n\t"
+          "bar.red.or.pred q, 1, 128, p;\n\t"
+          "selp.u32 %0, 1, 0, q;\n\t}\n"
+          : "=r"(any_failed)
+          : "r"(got)
+          : "memory");
+      if (any_failed) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const int r = quarter * 32 + lane;
+      const uint32_t rowb = (uint32_t)(quarter * 32) << 16;
+      for (int cb = 0; cb < 3; cb++) {  // X = acc1 to shared memory (its transpose is needed)
+        uint32_t v1[32];
+        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(128 + cb * 32), v1);
+        if (r < OZ_ROWS)
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++)
+            if (cb * 32 + jj < OZ_ROWS) S.X[r * OZ_XP + cb * 32 + jj] = __uint_as_float(v1[jj]);
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // X complete
+      for (int cb = 0; cb < 3; cb++) {
+        uint32_t v0[32], v2[32], v3[32];
+        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(cb * 32), v0);
+        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(256 + cb * 32), v2);
+        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(384 + cb * 32), v3);
+        if (r < OZ_ROWS) {
+          const int er = S.ex[r] - 16;
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++) {
+            const int c = cb * 32 + jj;
+            if (c < OZ_ROWS) {
+              const int sh = er + S.ex[c];
+              const float xa = S.X[r * OZ_XP + c], xb = S.X[c * OZ_XP + r];
+              const float t = xa + xb, bv = t - xa;                     // two-sum: t + e = xa + xb
+              const float e = (xa - (t - bv)) + (xb - bv);
+              const float lo = e + (__uint_as_float(v2[jj]) + __uint_as_float(v3[jj]));
+              S.G[r * OZ_GP + c] = (f32_to_f64_scaled(__uint_as_float(v0[jj]), sh) + f32_to_f64_scaled(t, sh)) +
+                                   f32_to_f64_scaled(lo, sh);
+            }
+          }
+        }
+      }
+      tc::fence_before_sync();
+      mbar_arrive1(&S.accempty);  // the next element's MMAs may overwrite the accumulators
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // G, rowp, pos of the element complete
+      // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc
+      for (int u = t; u < NE * NE; u += 128) {
+        const int rr = u / NE, cc = u - NE * rr;
+        const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
+        double kk = fma(lam, S.G[(3 * b + d) * OZ_GP + 3 * c + e], mu * S.G[(3 * b + e) * OZ_GP + 3 * c + d]);
+        if (d == e)
+          kk = fma(mu, S.G[(3 * b) * OZ_GP + 3 * c] + S.G[(3 * b + 1) * OZ_GP + 3 * c + 1] +
+                           S.G[(3 * b + 2) * OZ_GP + 3 * c + 2], kk);
+        double *dst = vals + S.rowp[rr] + 3 * (int)S.pos[NB * b + c] + e;
+        asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(kk) : "memory");
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // before the next element overwrites them
+    }
+    if (!ok) S.abort = 1;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (S.abort) {
+    if (tid == 0) {
+      for (int i = 0; i < OZ_NS; i++) {
+        if (S.cp_n[i] > 0) tc::mbar_wait(&S.full[i], (S.cp_n[i] - 1) & 1, OZ_WAIT_LIMIT);
+        if (S.mm_n[i] > 0) tc::mbar_wait(&S.empty[i], (S.mm_n[i] - 1) & 1, OZ_WAIT_LIMIT);
+      }
+      if (S.accf_n > 0) tc::mbar_wait(&S.accfull, (S.accf_n - 1) & 1, OZ_WAIT_LIMIT);
+      atomicCAS(err, 0, 2);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, OZ_TMEM_COLS);
+}
+
+// Builds the slices once (linear law, FP64 geometry cache present, memory
+// allows); leaves c->d_oz null otherwise (the FP64 element kernel then
+// assembles the tangent of this precision mode).
+int ensure_ozaki_operands(Context *c)
+{
+  if (c->oz_state >= 0 || c->law != IGAPGPU_LAW_LINGRAD || !c->d_geo) return IGAPGPU_OK;
+  c->oz_state = 0;
+  const int npts = c->nquad * c->nquad * c->nquad, nchunk = (npts + PW - 1) / PW;
+  const size_t bytes = (size_t)c->nelem_total * nchunk * OZ_CH_BYTES;
+  const size_t ebytes = (size_t)c->nelem_total * OZ_EXP;
+  size_t freeb = 0, totb = 0;
+  IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
+  if (bytes + ebytes + ((size_t)4 << 30) > freeb) return IGAPGPU_OK;
+  int *d_bad = nullptr;
+  if (cudaMalloc(&c->d_oz, bytes) != cudaSuccess || cudaMalloc(&c->d_ozexp, ebytes) != cudaSuccess ||
+      cudaMalloc(&d_bad, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    if (c->d_oz) cudaFree(c->d_oz);
+    if (c->d_ozexp) cudaFree(c->d_ozexp);
+    if (d_bad) cudaFree(d_bad);
+    c->d_oz = nullptr;
+    c->d_ozexp = nullptr;
+    return IGAPGPU_OK;
+  }
+  int bad = 0, dev = 0, nsm = 0;
+  cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    const int64_t grid = c->nelem_total < (int64_t)nsm * 8 ? c->nelem_total : (int64_t)nsm * 8;
+    ozaki_operand_kernel<<<(unsigned)grid, 256, 0, c->stream>>>(c->d_geo, npts, nchunk, c->nelem_total,
+                                                                 c->par[2], (__nv_bfloat16 *)c->d_oz,
+                                                                 (signed char *)c->d_ozexp, d_bad);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_bad);
+  if (e != cudaSuccess || bad) {
+    cudaFree(c->d_oz);
+    cudaFree(c->d_ozexp);
+    c->d_oz = nullptr;
+    c->d_ozexp = nullptr;
+    if (e != cudaSuccess) {
+      set_error("ozaki operands: CUDA error %s", cudaGetErrorString(e));
+      return IGAPGPU_ERR_CUDA;
+    }
+    return IGAPGPU_OK;  // a non-positive point weight: the FP64 kernel stays in use
+  }
+  c->oz_state = 1;
+  return IGAPGPU_OK;
+}
+
+// One persistent launch per colour, one CTA per SM.
+int launch_tc_ozaki(Context *c, double *vals)
+{
+  const DevMesh m = c->devmesh();
+  const DevLaw L = c->devlaw();
+  const size_t smem = sizeof(OzSmem) + 1024;
+  static bool attr_set = false;
+  if (!attr_set) {
+    IGAP_CUDA(cudaFuncSetAttribute(tco_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  for (int cx = 0; cx < 3; cx++)
+    for (int cy = 0; cy < 3; cy++)
+      for (int cz = 0; cz < 3; cz++) {
+        const int ncx = (c->nelem[0] - cx + 2) / 3, ncy = (c->nelem[1] - cy + 2) / 3,
+                  ncz = (c->nelem[2] - cz + 2) / 3;
+        const int nel = ncx * ncy * ncz;
+        if (nel <= 0) continue;
+        const int grid = nel < nsm ? nel : nsm;
+        tco_kernel<<<grid, OZ_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err,
+                                                          (const unsigned char *)c->d_oz,
+                                                          (const signed char *)c->d_ozexp);
+        count_launch();
+        IGAP_CHECK_LAUNCH();
+        if (c->prof) {
+          c->prof_launches[1]++;
+          c->prof_elements[1] += nel;
+        }
+      }
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[1].emplace_back(e0, e1);
+  }
+  return IGAPGPU_OK;
+}
+
+}  // namespace igap

@@ -16,6 +16,7 @@
 // One persistent CTA per SM walks the elements of one colour, so the CSR
 // scatter is conflict-free as in the FP64 kernel.
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include <stdlib.h>
 
 #include "common.cuh"
@@ -68,8 +69,10 @@ struct TcSmem {
 };
 
 // ------------------------------------------------------------ self-test
-// D (128 x 32) = A (128 x 16) . B (32 x 16)^T with small integers, two K-steps;
-// variant 0: LBO = 128 / SBO = 256, variant 1: swapped.
+// D (128 x 32) = A (128 x 16) . B (32 x 16)^T with small integers;
+// variant 0: TF32, two K-steps, LBO = 128 / SBO = 256; variant 1: the same
+// with LBO and SBO swapped; variant 2: BF16 (kind::f16), one K = 16 step,
+// core matrices of 8 rows x 8 values (16 B), LBO = 128 / SBO = 256.
 __global__ void tc_selftest_kernel(int variant, float *out, int *err)
 {
   __shared__ __align__(1024) float sA[2][128 * 8];
@@ -82,13 +85,22 @@ __global__ void tc_selftest_kernel(int variant, float *out, int *err)
     tc::tmem_relinquish();
   }
   if (tid == 0) tc::mbar_init(&mbar, 1);
+  __nv_bfloat16 *hA = reinterpret_cast<__nv_bfloat16 *>(sA[0]), *hB = reinterpret_cast<__nv_bfloat16 *>(sB[0]);
   for (int i = tid; i < 128 * 16; i += blockDim.x) {
     const int r = i / 16, kk = i % 16;
-    sA[kk / 8][kmajor_off(r, kk % 8) / 4] = (float)(((r * 3 + kk * 5) % 7) - 3);
+    const float a = (float)(((r * 3 + kk * 5) % 7) - 3);
+    if (variant == 2)
+      hA[(r >> 3) * 128 + (kk >> 3) * 64 + (r & 7) * 8 + (kk & 7)] = __float2bfloat16_rn(a);
+    else
+      sA[kk / 8][kmajor_off(r, kk % 8) / 4] = a;
   }
   for (int i = tid; i < 32 * 16; i += blockDim.x) {
     const int n = i / 16, kk = i % 16;
-    sB[kk / 8][kmajor_off(n, kk % 8) / 4] = (float)(((n * 2 + kk * 3) % 5) - 2);
+    const float b = (float)(((n * 2 + kk * 3) % 5) - 2);
+    if (variant == 2)
+      hB[(n >> 3) * 128 + (kk >> 3) * 64 + (n & 7) * 8 + (kk & 7)] = __float2bfloat16_rn(b);
+    else
+      sB[kk / 8][kmajor_off(n, kk % 8) / 4] = b;
   }
   tc::fence_proxy_async();
   tc::fence_before_sync();
@@ -97,9 +109,14 @@ __global__ void tc_selftest_kernel(int variant, float *out, int *err)
   const uint32_t taddr = taddr_s;
   const uint32_t lbo = variant == 0 ? 128 : 256, sbo = variant == 0 ? 256 : 128;
   if (tid == 0) {
-    for (int kt = 0; kt < 2; kt++)
-      tc::mma_tf32(taddr, tc::smem_desc(tc::smem_u32(sA[kt]), lbo, sbo),
-                   tc::smem_desc(tc::smem_u32(sB[kt]), lbo, sbo), tc::instr_desc(2, 128, 32), kt > 0);
+    if (variant == 2) {
+      tc::mma_bf16(taddr, tc::smem_desc(tc::smem_u32(sA[0]), 128, 256), tc::smem_desc(tc::smem_u32(sB[0]), 128, 256),
+                   tc::instr_desc(1, 128, 32), 0u);
+    } else {
+      for (int kt = 0; kt < 2; kt++)
+        tc::mma_tf32(taddr, tc::smem_desc(tc::smem_u32(sA[kt]), lbo, sbo),
+                     tc::smem_desc(tc::smem_u32(sB[kt]), lbo, sbo), tc::instr_desc(2, 128, 32), kt > 0);
+    }
     tc::mma_commit(&mbar);
   }
   if (!tc::mbar_wait(&mbar, 0, WAIT_LIMIT)) atomicExch(err, 1);

@@ -14,6 +14,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+REASON_REJECTED = -9  # igapgpu_solve: initial |F| above snes_f0_max
+
 
 @dataclass
 class TipLoad:
@@ -98,25 +100,38 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
         t0 = time.perf_counter()
         U = u_n.clone()
         used = False
+        st = None
         if predictor is not None:
             # the Newton correction leaves Dirichlet DOFs where the initial
             # iterate puts them (their columns are cleared), so every guess
-            # carries the prescribed values exactly; a predictor may offer
-            # several guesses (the one with the smallest residual is taken)
+            # carries the prescribed values exactly
             dl = load.value(t) - prev_load
             cands = predictor.candidates(u_n, u_nm1, dl) if hasattr(predictor, "candidates") \
                 else [predictor(u_n, u_nm1, dl)]
             A.residual(U, F)
-            best = A.norm2(F)
-            for g in cands:
-                guess = A.impose_dirichlet(g.contiguous())
-                A.residual(guess, F)
-                f_pred = A.norm2(F)
-                if f_pred < best:
-                    best = f_pred
-                    U = guess.clone()
-                    used = True
-        st = A.solve(U, **o)
+            f_plain = A.norm2(F)
+            if len(cands) == 1:
+                # Newton from the guess, unless its residual is above that of
+                # u_n (the solve then stops before its first step and the
+                # step falls back to plain Newton from u_n)
+                guess = A.impose_dirichlet(cands[0].contiguous())
+                st = A.solve(guess, **dict(o, snes_f0_max=f_plain))
+                if st["reason"] == REASON_REJECTED:
+                    st = None
+                else:
+                    U, used = guess, True
+            else:  # several guesses: the one with the smallest residual
+                best = f_plain
+                for g in cands:
+                    guess = A.impose_dirichlet(g.contiguous())
+                    A.residual(guess, F)
+                    f_pred = A.norm2(F)
+                    if f_pred < best:
+                        best = f_pred
+                        U = guess.clone()
+                        used = True
+        if st is None:
+            st = A.solve(U, **o)
         A.synchronize()
         dtm = time.perf_counter() - t0
         recs.append(StepRecord(t, st["newton_its"], st["ksp_its_total"], st["fnorm0"], st["fnorm"],

@@ -50,6 +50,12 @@ extern "C" {
 #define IGAPGPU_PREC_FP64 0  /* FP64 everywhere */
 #define IGAPGPU_PREC_SPLIT 1 /* tangent on the tensor cores: TF32x3 products (hi*hi + hi*lo + lo*hi),
                                 FP32 accumulate; relative error <= 1e-5 (measured ~2e-6) */
+#define IGAPGPU_PREC_OZAKI 2 /* FP64-quality tangent on the tensor cores (linear law): the sqrt(w)-weighted
+                                Gram operands split error-free into four BF16 slices with a power-of-two
+                                scale per row (Ozaki scheme), exact FP32 accumulation of the leading
+                                product, FP64 recombination; relative error <= 1e-9 (measured ~1e-11);
+                                other laws, or slices that do not fit in memory: the FP64 kernel;
+                                single lattices only */
 
 typedef struct igapgpu_ctx *igapgpu_t;
 
@@ -99,7 +105,12 @@ typedef struct {
                           1 = classical Gram-Schmidt applied twice (CGS2: two block passes per
                           Arnoldi step instead of one dot and one update per basis vector;
                           graph GMRES only, the host-driven GMRES always uses MGS) */
+  double snes_f0_max;  /* > 0: an initial iterate whose |F| exceeds this is rejected before any Newton
+                          step (reason IGAPGPU_REASON_REJECTED, U unchanged): a predicted guess is
+                          tried against the residual of the plain guess without a second solve */
 } igapgpu_solver_opts;
+
+#define IGAPGPU_REASON_REJECTED (-9) /* igapgpu_solve: initial |F| above snes_f0_max */
 
 typedef struct {
   int newton_its;

@@ -157,3 +157,75 @@ def test_split_and_fp64_vs_cpu_oracle(law, nelem):
     print(f"law {law} {nelem}: FP64 {e64:.2e}, split {es:.2e} vs the CPU oracle")
     assert e64 <= 1e-12
     assert es <= SPLIT_TOL
+
+
+# ---------------------------------------------------------- FP64-quality mode
+OZAKI_TOL = 1e-9
+
+
+def test_tcgen05_selftest_bf16_exact():
+    """The BF16 (kind::f16) MMA path of the FP64-quality tangent reproduces an
+    exact integer product."""
+    D, E = ig.tc_selftest(2)
+    assert np.array_equal(D, E), f"max |D-E| = {np.abs(D - E).max()}"
+
+
+@pytest.mark.parametrize("nelem,perturb,nquad", [((8, 4, 3), False, 4), ((5, 3, 4), True, 4),
+                                                 ((6, 3, 2), True, 3)])
+def test_ozaki_tangent_vs_fp64(nelem, perturb, nquad):
+    """Tangent from error-free BF16 slices of the Gram operands (one
+    power-of-two scale per row, exact leading product): within 1e-9 of the
+    FP64 tangent; the residual is the FP64 residual, bit for bit."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0), 2, perturb)
+    A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct, neumann=neu,
+                    nquad=nquad)
+    U = np.random.default_rng(3).uniform(-1e-2, 1e-2, A.ndof)
+    K64, R64 = A.tangent(U.copy()), A.residual(U.copy())
+    n0 = ig.launch_count()
+    A.set_precision(ig.PREC_OZAKI)
+    assert ig.launch_count() - n0 == 1  # the slices are built once, in one launch
+    Ko, Ro = A.tangent(U.copy()), A.residual(U.copy())
+    e = rel(Ko, K64)
+    print(f"FP64-quality tensor-core tangent rel err {e:.3e}")
+    assert e <= OZAKI_TOL
+    np.testing.assert_array_equal(Ro, R64)
+    RR, V = np.zeros(A.ndof), np.zeros(A.nnz)
+    A.assemble(U.copy(), RR, V)
+    np.testing.assert_array_equal(RR, R64)
+    assert rel(V, K64) <= OZAKI_TOL
+    # twice in a row: the same values (the slices are state independent)
+    np.testing.assert_array_equal(A.tangent(U.copy()), Ko)
+
+
+def test_ozaki_vs_cpu_oracle_sweep_mesh():
+    """At the 32x8x8 size of the assembly sweep, against the FP64 CPU oracle on
+    the rows of one control-point layer."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=(32, 8, 8), L=(4.0, 1.0, 1.0), law=po.LAW_LINGRAD, bc_type=bct, neumann=neu)
+    U = po.random_state(prob, 31)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=prob.law, par=prob.params(), bc_type=bct, neumann=neu)
+    A.set_state(U)
+    A.set_precision(ig.PREC_OZAKI)
+    Ko = A.tangent()
+    orc = po.OracleCase(prob)
+    rowptr, _ = orc.pattern()
+    rows, e0, e1 = slab_rows(prob, 17)
+    err = rel(rows_of(Ko, rowptr, rows), rows_of(orc.tangent_elements(U, e0, e1), rowptr, rows))
+    print(f"FP64-quality tensor-core tangent vs CPU oracle: {err:.3e}")
+    assert err <= OZAKI_TOL
+
+
+@pytest.mark.parametrize("law", [po.LAW_GRADELAST, po.LAW_GRADELASTTIME])
+def test_ozaki_mode_other_laws_is_fp64(law):
+    """The reference's laws have no sliced operands: the FP64-quality mode
+    assembles their tangent with the FP64 kernel (the same values)."""
+    prob = po.Problem(nelem=(4, 3, 3), law=law)
+    U = po.random_state(prob, 6)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=law, par=prob.params())
+    A.set_state(U)
+    K64 = A.tangent()
+    A.set_precision(ig.PREC_OZAKI)
+    np.testing.assert_array_equal(A.tangent(), K64)
