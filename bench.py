@@ -2,14 +2,21 @@
 
 One step = one fused assembly of the residual Vec and the CSR tangent of the
 whole beam (131,072 elements, 64 Gauss points each) on the GPU, state already
-resident in HBM.  Metric: assembled elements/s.  Also reported:
+resident in HBM.  Metric: assembled elements/s.  The headline is the
+FP64-quality mode (FP64 residual; tangent on the tensor cores from error-free
+BF16 slices of the Gram operands, its error against the FP64 tangent measured
+in the same run); the pure FP64 and the TF32x3 split modes follow in `modes`.
+Also reported:
 
 * e2e  -- the same step through the C ABI with HOST buffers (state in from
   pinned host memory, residual back to pinned host memory; the tangent stays
   in the device matrix that MatMult uses), copies inside the timed region;
-* roofline -- the element kernel's algorithmic FLOP rate against the measured
-  peak of the pipe that bounds it;
+* roofline -- the dominant kernel of the headline mode against the measured
+  peak of the pipe or memory that bounds it;
 * spmv -- CSR SpMV (the MATSHELL multiply) GB/s over repeated multiplies;
+* batched -- 256 seeded uneven beams in persistent launches;
+* transient -- time to |F| <= 1e-8 per step of the transient law, plain
+  Newton against the learned predictor;
 * cpu_baseline -- the CPU oracle port (the reference's loop structure,
   restated in C) on the host cores, on a bounded element sample.
 
@@ -49,8 +56,15 @@ RES_FLOP_PER_ELEM = 2 * 64 * (27 * 30 + 27 * 30)                 # 207,360
 EXEC_FLOP_FP64_ELEM = 378 * 64 * 72 + 64 * 243 + 64 * 3420 + 30_000  # ~2.0 M
 # tensor-core kernel: 3 TF32 products of M128 x N96 x K256 per element
 EXEC_FLOP_TC_ELEM = 3 * 2 * 128 * 96 * 256                         # 18.9 M
+# FP64-quality tensor-core kernel: 12 BF16 products of M128 x N96 x K256 per element
+EXEC_FLOP_OZ_ELEM = 12 * 2 * 128 * 96 * 256                        # 75.5 M
+# residual-only FP64 kernel: state interpolation, law and projection per point
+EXEC_FLOP_RES_ELEM = 64 * 3420 + 64 * 243
+# FP64-quality tangent: per element the slices (8 chunks x 22,528 B), the row
+# exponents (88 B) and the read-modify-write of its 6,561 FP64 CSR slots
+ALG_BYTES_OZ_ELEM = 8 * 22528 + 88 + 2 * 8 * 6561
 # DRAM traffic per launch of the FP64 element kernel at 128x32x32, from the
-# one-pass ncu launch list (profiles/assembly_launch_list_beam128x32x32.md)
+# one-pass ncu launch list (gpu__time_duration and DRAM bytes, 128x32x32)
 TRAFFIC_FP64_LAUNCH = 1.5063e9
 # cached-operand tensor-core tangent: per element the operands (8 chunks x
 # 11,264 B) and the read-modify-write of its 6,561 FP64 CSR slots
@@ -65,8 +79,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--nelem", default="128,32,32")
-    ap.add_argument("--prec", default="both", choices=["fp64", "split", "both"],
-                    help="both: FP64 headline plus the split (tensor-core) mode")
+    ap.add_argument("--prec", default="all", choices=["fp64q", "fp64", "split", "all"],
+                    help="all: the FP64-quality tensor-core mode as the headline, then the FP64 and the "
+                         "split modes")
     ap.add_argument("--spmv", type=int, default=200, help="SpMV repetitions")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -130,16 +145,21 @@ def run_reference(a):
     for _ in range(a.warmup):
         cpu_rate(2.0, cores)
     sample = None
+    sample_s = []
     for _ in range(a.steps):
         r, nel, slowest, wall = cpu_rate(max(2.0, a.cpu_seconds / max(a.steps, 1)), cores)
         rates.append(r)
+        sample_s.append(slowest)
         sample = f"{cores} processes x {nel} elements (p=2, 64 Gauss points, linear law) of a 32x8x8 beam"
     value = statistics.median(rates)
     nelem = tuple(int(x) for x in a.nelem.split(","))
     out = {
         "impl": "reference", "metric": "assembled elements/s (tangent+residual)", "value": value,
         "unit": "elements/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": 1e3 * np.prod(nelem) / value, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * np.prod(nelem) / value,
+        "ms_per_step_note": "extrapolated: the whole beam's elements over the measured element rate of the "
+                            "sample (the per-element cost does not depend on the mesh size)",
+        "sample_seconds_per_step": sample_s, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} residual+tangent assembly, CPU",
                    "law": "linear strain gradient lambda=mu=1 ell=0.1", "sample": sample},
@@ -342,6 +362,8 @@ def bench_transient(ig, torch, nelem, steps, start_steps=200, seed=9001, dt=5e-4
     if os.path.exists(PREDICTOR_FILE):
         net, sc = load_network(PREDICTOR_FILE, tuple(n + 2 for n in nelem))
         pred = LearnedPredictor(net, sc, A=A)
+        pred(start[0], start[1], 0.0)  # first call: the network kernels' one-time set-up, not timed
+        torch.cuda.synchronize()
         _, learned = run_transient(A, load, steps, dt, predictor=pred, opts=opts, record_states=False, start=start)
         out["learned"] = summary(learned)
         out["time_ratio_learned_vs_plain"] = out["learned"]["ms_per_step"] / out["plain"]["ms_per_step"]
@@ -433,57 +455,41 @@ def main():
     sampler = ClockSampler()
     sampler.start()
     t_wall0 = time.perf_counter()
-    fp64_prec = ig.PREC_FP64
-    headline_prec = ig.PREC_SPLIT if a.prec == "split" else fp64_prec
-    ms_per_step, step_ms, kinds, launches = measure(headline_prec, a.steps, a.warmup)
-    t_wall = time.perf_counter() - t_wall0
-    value = job_rate(A.nelem_total, ms_per_step, world)
-    elem_ms, elem_launches, elem_count = kinds[0] if headline_prec == fp64_prec else kinds[1]
-    dev_ms = ms_per_step * a.steps
+    precs = {"fp64q": ig.PREC_OZAKI, "fp64": ig.PREC_FP64, "split": ig.PREC_SPLIT}
+    head = "fp64q" if a.prec == "all" else a.prec
+    prep_launches = {}
 
-    split = None
-    if a.prec == "both":
-        # split mode: same step, tangent on the tensor cores; error vs FP64 at full size.
-        # Setting split precision builds the cached Gram operands once (one launch)
-        # when they fit; the tangent kernel then is tcs_kernel, else tcg_kernel.
+    def prepare(name):
+        # a mode's one-time set-up (BF16 slices, cached Gram operands), outside the timing
         n0 = ig.launch_count()
-        A.set_precision(ig.PREC_SPLIT)
-        cached = ig.launch_count() - n0 == 1
-        sms, sstep, skinds, slaunch = measure(ig.PREC_SPLIT, a.steps, max(1, a.warmup - 1))
-        A.set_precision(ig.PREC_FP64)
-        K64 = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
-        A.tangent(U, K64)
-        A.set_precision(ig.PREC_SPLIT)
-        Ks = torch.zeros_like(K64)
-        A.tangent(U, Ks)
+        A.set_precision(precs[name])
+        prep_launches[name] = ig.launch_count() - n0
+
+    prepare(head)
+    runs = {head: measure(precs[head], a.steps, a.warmup)}
+    t_wall = time.perf_counter() - t_wall0
+    ms_per_step, step_ms, kinds, launches = runs[head]
+    value = job_rate(A.nelem_total, ms_per_step, world)
+    dev_ms = ms_per_step * a.steps
+    others = [m for m in ("fp64q", "fp64", "split") if m != head] if a.prec == "all" else []
+    for name in others:
+        prepare(name)
+        runs[name] = measure(precs[name], a.steps, max(1, a.warmup - 1))
+    # tangent error of each mode against the FP64 tangent, at full size
+    A.set_precision(ig.PREC_FP64)
+    K64 = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
+    A.tangent(U, K64)
+    errs = {"fp64": 0.0}
+    Kx = torch.zeros_like(K64)
+    for name in runs:
+        if name == "fp64":
+            continue
+        A.set_precision(precs[name])
+        A.tangent(U, Kx)
         A.synchronize()
-        err = (torch.linalg.norm(Ks - K64) / torch.linalg.norm(K64)).item()
-        del K64, Ks
-        tc_ms, tc_l, tc_e = skinds[1]
-        res_ms, res_l, res_e = skinds[0]
-        tc_flop = TAN_FLOP_PER_ELEM * tc_e / max(tc_l, 1)
-        tc_ach = tc_flop / (tc_ms / max(tc_l, 1) * 1e-3) / 1e12
-        tc_exec = tc_ach * EXEC_FLOP_TC_ELEM / TAN_FLOP_PER_ELEM
-        bf16_peak = peaks.get("bf16_tflops", 1900.0) if (peaks := _peaks()) else 1900.0
-        split = {"value": world * A.nelem_total / (sms * 1e-3), "unit": "elements/s",
-                 "ms_per_step": sms, "step_ms": sstep, "gpu_launches": slaunch,
-                 "tangent_rel_err_vs_fp64": err, "dtype": "tf32x3/f32-acc tangent, f64 residual",
-                 "tc_kernel_ms_per_step": tc_ms / a.steps, "fp64_residual_kernel_ms_per_step": res_ms / a.steps,
-                 "roofline": {"bound": "tensor",
-                              "kernel": ("tcw_kernel (cached sqrt(w)-weighted Gram operands, one bulk copy per "
-                                         "chunk, warp-specialised copy/split/MMA/scatter; tcgen05.mma kind::tf32, "
-                                         "TF32x3)") if cached else
-                                        "tcg_kernel (tcgen05.mma kind::tf32, TF32x3, Gram form)",
-                              "achieved": tc_ach, "peak": bf16_peak, "unit": "TFLOP/s",
-                              "frac": tc_ach / bf16_peak,
-                              "executed_flop_per_element": EXEC_FLOP_TC_ELEM,
-                              "executed_achieved": tc_exec, "executed_frac": tc_exec / bf16_peak,
-                              "traffic": (TRAFFIC_TCS_LAUNCH if cached else 1.1448e9) if nelem == NELEM else None,
-                              "traffic_source": "ncu launch list (per colour launch)",
-                              "hbm_algorithmic_bytes_per_element": (ALG_BYTES_TCS_ELEM if cached else None),
-                              "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense TF32 is half of it)",
-                              "algorithmic_flop_per_element": TAN_FLOP_PER_ELEM}}
-        A.set_precision(headline_prec)
+        errs[name] = (torch.linalg.norm(Kx - K64) / torch.linalg.norm(K64)).item()
+    del K64, Kx
+    A.set_precision(precs[head])
 
     # e2e through the C ABI with pinned host buffers
     Uh = torch.empty(A.ndof, dtype=torch.float64, pin_memory=True)
@@ -516,6 +522,7 @@ def main():
 
     peaks = _peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
     fp64_peak = ig.measure_fp64_peak()
     nelem_total, ndof_total, nnz_total = A.nelem_total, A.ndof, A.nnz
     A.close()  # frees the beam's matrix and geometry cache before the batched workload
@@ -529,33 +536,81 @@ def main():
     if a.transient_steps > 0 and world == 1:
         transient = bench_transient(ig, torch, tuple(int(v) for v in a.transient_nelem.split(",")),
                                     a.transient_steps)
-    elem_kernel_ms = elem_ms / max(elem_launches, 1)
-    flop_per_launch = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) * elem_count / max(elem_launches, 1)
-    achieved = flop_per_launch / (elem_kernel_ms * 1e-3) / 1e12
-    exec_ach = EXEC_FLOP_FP64_ELEM * elem_count / max(elem_launches, 1) / (elem_kernel_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak,
-                "frac_note": "achieved counts the dense R^T D R FLOPs per element; the kernel evaluates the "
-                             "same sum through Gram sums with 5.3x fewer FLOPs, so frac exceeds 1; "
-                             "executed_frac is the FP64 pipe fraction",
-                "executed_flop_per_element": EXEC_FLOP_FP64_ELEM, "executed_achieved": exec_ach,
-                "executed_frac": exec_ach / fp64_peak,
-                "traffic": TRAFFIC_FP64_LAUNCH if nelem == NELEM else None,
-                "traffic_source": "ncu launch list, dram__bytes_read.sum + dram__bytes_write.sum per launch "
-                                  "(profiles/assembly_launch_list_beam128x32x32.md); the geometry cache "
-                                  "re-read replaces FP64 recomputation",
-                "kernel": "element_kernel (fused residual+tangent, FP64)",
-                "peak_source": "measured in-run FP64 FMA throughput (MEASURED_PEAKS.json has no FP64 figure)",
-                "algorithmic_flop_per_element": TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM,
-                "elements_per_launch": elem_count / max(elem_launches, 1),
-                "avg_launch_ms": elem_kernel_ms,
-                "kernel_share_of_step": elem_ms / dev_ms if dev_ms > 0 else None}
+
+    def fp64_roofline(name, kms, kl, kc, step_total_ms):
+        """The FP64 element kernel of a mode (fused residual + tangent in the
+        FP64 mode, residual only in the tensor-core modes)."""
+        fused = name == "fp64"
+        per_launch_ms = kms / max(kl, 1)
+        alg = (TAN_FLOP_PER_ELEM + RES_FLOP_PER_ELEM) if fused else RES_FLOP_PER_ELEM
+        exe = EXEC_FLOP_FP64_ELEM if fused else EXEC_FLOP_RES_ELEM
+        ach = alg * kc / max(kl, 1) / (per_launch_ms * 1e-3) / 1e12
+        ex_ach = exe * kc / max(kl, 1) / (per_launch_ms * 1e-3) / 1e12
+        out = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+               "executed_flop_per_element": exe, "executed_achieved": ex_ach, "executed_frac": ex_ach / fp64_peak,
+               "kernel": "element_kernel (fused residual+tangent, FP64)" if fused else
+                         "element_kernel (residual, FP64)",
+               "peak_source": "measured in-run FP64 FMA throughput (MEASURED_PEAKS.json has no FP64 figure)",
+               "algorithmic_flop_per_element": alg, "elements_per_launch": kc / max(kl, 1),
+               "avg_launch_ms": per_launch_ms,
+               "kernel_share_of_step": kms / step_total_ms if step_total_ms > 0 else None,
+               "traffic": (TRAFFIC_FP64_LAUNCH if fused else None) if nelem == NELEM else None}
+        if fused:
+            out["frac_note"] = ("achieved counts the dense R^T D R FLOPs per element; the kernel evaluates the "
+                                "same sum through Gram sums with 5.3x fewer FLOPs, so frac exceeds 1; "
+                                "executed_frac is the FP64 pipe fraction")
+        return out
+
+    def tc_roofline(name, kms, kl, kc):
+        per_launch_ms = kms / max(kl, 1)
+        per_launch_el = kc / max(kl, 1)
+        if name == "split":
+            exe, kern = EXEC_FLOP_TC_ELEM, ("tcw_kernel (cached sqrt(w)-weighted Gram operands, warp-specialised "
+                                           "copy/split/MMA/scatter; tcgen05.mma kind::tf32, TF32x3)")
+            bytes_el, traffic = ALG_BYTES_TCS_ELEM, (TRAFFIC_TCS_LAUNCH if nelem == NELEM else None)
+        else:
+            exe, kern = EXEC_FLOP_OZ_ELEM, ("tco_kernel (error-free BF16 slices of the Gram operands, one bulk "
+                                           "copy per chunk, 24 tcgen05.mma kind::f16 per chunk into 4 TMEM "
+                                           "accumulators, FP64 recombination and scatter)")
+            bytes_el, traffic = ALG_BYTES_OZ_ELEM, None
+        gbs = bytes_el * per_launch_el / (per_launch_ms * 1e-3) / 1e9
+        ex_ach = exe * per_launch_el / (per_launch_ms * 1e-3) / 1e12
+        return {"bound": "hbm", "kernel": kern, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": gbs / hbm_peak, "hbm_algorithmic_bytes_per_element": bytes_el,
+                "traffic": traffic, "executed_tensor_flop_per_element": exe,
+                "executed_tensor_tflops": ex_ach, "executed_tensor_frac_of_bf16": ex_ach / bf16_peak,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy) and bf16_tflops",
+                "avg_launch_ms": per_launch_ms, "elements_per_launch": per_launch_el}
+
+    mode_desc = {"fp64q": "FP64 residual; tangent on the tensor cores from error-free BF16 slices (FP64 quality)",
+                 "fp64": "FP64 residual and tangent (FP64 pipe)",
+                 "split": "FP64 residual; TF32x3 tensor-core tangent"}
+    blocks = {}
+    for name, (mms, mstep, mkinds, mlaunch) in runs.items():
+        res_ms, res_l, res_c = mkinds[0]
+        tc_ms, tc_l, tc_c = mkinds[1]
+        tot = mms * a.steps
+        b = {"value": world * nelem_total / (mms * 1e-3), "unit": "elements/s", "ms_per_step": mms,
+             "step_ms": mstep, "gpu_launches": mlaunch, "precision": mode_desc[name],
+             "tangent_rel_err_vs_fp64": errs.get(name), "setup_launches": prep_launches.get(name),
+             "fp64_kernel_ms_per_step": res_ms / a.steps, "tc_kernel_ms_per_step": tc_ms / a.steps,
+             "fp64_kernel_roofline": fp64_roofline(name, res_ms, res_l, res_c, tot)}
+        if name != "fp64" and tc_l > 0:
+            b["tc_kernel_roofline"] = tc_roofline(name, tc_ms, tc_l, tc_c)
+        blocks[name] = b
+    hb = blocks[head]
+    # the headline's roofline: its dominant kernel
+    if head != "fp64" and "tc_kernel_roofline" in hb and hb["tc_kernel_ms_per_step"] > hb["fp64_kernel_ms_per_step"]:
+        roofline = hb["tc_kernel_roofline"]
+    else:
+        roofline = hb["fp64_kernel_roofline"]
     if rank == 0:
         out = {
             "metric": "assembled elements/s (tangent+residual)", "value": value, "unit": "elements/s",
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if a.prec != "split" else "tf32x3/f32-acc tangent, f64 residual",
+            "dtype": {"fp64q": "f64 (tangent: bf16 slices, exact f32 accumulation, f64 recombination)",
+                      "fp64": "f64", "split": "tf32x3/f32-acc tangent, f64 residual"}[head],
             "data": "synthetic",
             "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} "
                                    f"({nelem_total} elements, {ndof_total} DOF, nnz {nnz_total}) "
@@ -563,7 +618,8 @@ def main():
                        "law": "linear isotropic strain gradient lambda=1 mu=1 ell=0.1",
                        "quadrature": "4x4x4 Gauss", "bc": "clamped x=0, traction 1e-3 in -z at x=4",
                        "state": "seeded uniform [-1e-2,1e-2] per DOF",
-                       "precision": "fp64" if a.prec != "split" else "split",
+                       "precision": mode_desc[head],
+                       "tangent_rel_err_vs_fp64": errs.get(head),
                        "l2": "flushed (256 MiB write) before every timed step; the 1.25 GB CSR output also exceeds L2",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": ndof_total * 8,
@@ -579,7 +635,7 @@ def main():
                      "frac_of_fp64": 2 * nnz_total / (spmv_ms * 1e-3) / 1e12 / fp64_peak,
                      "bound": "fp64"},
             "cpu_baseline": cpu,
-            "split": split,
+            "modes": blocks,
             "batched": batched,
             "transient": transient,
             "clocks": sampler.summary(local),

@@ -169,6 +169,7 @@ struct Context {
   double *d_diag = nullptr;    // [ndof]
   double *d_bdiag = nullptr;   // [3 ndof] inverted 3 x 3 point blocks (point-block Jacobi)
   double *d_cinv = nullptr;    // [cells][24 x 24] inverted cell blocks (cell-block Jacobi, lazy)
+  float *d_asmz = nullptr;     // [cells][24 x 192] subdomain inverse rows (restricted additive Schwarz, lazy)
   double *d_red = nullptr;     // device scalars (norms, Hessenberg column) [red_cap]
   double *h_red = nullptr;     // pinned host mirror of d_red [red_cap]
   double *d_partial = nullptr; // per-block partial sums of the reductions
@@ -277,6 +278,9 @@ int dev_norm2(Context *c, const double *x, double *out);
 struct CellGeom;
 CellGeom cell_geom(const Context *c);
 int ensure_cblock(Context *c, int64_t ncell);
+// restricted additive Schwarz (pc = 4): set-up of the subdomain rows into Z
+// (cells x 24 x 192 floats) from the context matrix
+int asm_setup(Context *c, float *Z);
 // batch.cu
 int launch_batch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
 void batch_release(Context *c);

@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "spmv.cuh"
+#include "asm_pc.cuh"
 
 namespace igap {
 
@@ -109,6 +110,10 @@ __global__ void gm_precond(double *z, const double *v, const double *diag, int p
   }
   if (pc == 3) {  // cell-block Jacobi: diag holds the inverted cell blocks
     cblock_apply(z, v, diag, cg, cell_count(cg));
+    return;
+  }
+  if (pc == 4) {  // restricted additive Schwarz: diag holds the subdomain rows (FP32)
+    asm_apply(z, v, reinterpret_cast<const float *>(diag), cg, cell_count(cg));
     return;
   }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -294,7 +299,9 @@ static int build_gmres_graph(Context *c, int m, int pc, int orth)
       alloc(&gw->H, (size_t)(m + 1) * m) || alloc(&gw->cs, m) || alloc(&gw->sn, m) ||
       alloc(&gw->g, m + 1) || alloc(&gw->y, m) || alloc(&gw->scal, m + 2) ||
       alloc(&gw->partial, (size_t)(RB > MD_BLOCKS * (m + 1) ? RB : MD_BLOCKS * (m + 1))) ||
-      alloc(&gw->diag, pc == 3 ? (size_t)cell_count(cell_geom(c)) * CBS * CBS : (size_t)3 * n) ||
+      alloc(&gw->diag, pc == 3   ? (size_t)cell_count(cell_geom(c)) * CBS * CBS
+                       : pc == 4 ? (size_t)cell_count(cell_geom(c)) * AS_NC * AS_N / 2
+                                 : (size_t)3 * n) ||
       cudaMalloc(&gw->st, sizeof(GmState)) != cudaSuccess ||
       cudaMallocHost(&gw->h_st, sizeof(GmState)) != cudaSuccess) {
     cudaGetLastError();
@@ -378,14 +385,14 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
                     double *rnorm_out)
 {
   const int m = o->ksp_restart > 0 ? o->ksp_restart : 30;
-  const int pc = (o->pc >= 1 && o->pc <= 3) ? o->pc : 0;
+  const int pc = (o->pc >= 1 && o->pc <= 4) ? o->pc : 0;
   const int orth = o->orth == 1 ? 1 : 0;
   if (m > 1000) {
     set_error("graph GMRES: restart %d above 1000", m);
     return IGAPGPU_ERR_ARG;
   }
-  if (pc == 3 && c->batch) {
-    set_error("cell-block Jacobi (pc = 3) needs a single lattice; a batch takes pc 0, 1 or 2");
+  if ((pc == 3 || pc == 4) && c->batch) {
+    set_error("block preconditioners (pc = 3, 4) need a single lattice; a batch takes pc 0, 1 or 2");
     return IGAPGPU_ERR_ARG;
   }
   if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc || c->gmres_graph->orth != orth) {
@@ -413,6 +420,9 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
                                                                                               gw->diag, cg, ncell);
     count_launch();
     IGAP_CHECK_LAUNCH();
+  } else if (pc == 4) {
+    int r = asm_setup(c, reinterpret_cast<float *>(gw->diag));
+    if (r) return r;
   }
   GmState h0;
   memset(&h0, 0, sizeof h0);

@@ -12,6 +12,7 @@
 
 #include "common.cuh"
 #include "spmv.cuh"
+#include "asm_pc.cuh"
 
 namespace igap {
 
@@ -234,6 +235,31 @@ int ensure_cblock(Context *c, int64_t ncell)
   return IGAPGPU_OK;
 }
 
+static __global__ void asm_kernel(double *z, const double *v, const float *Zi, CellGeom g, int64_t ncell)
+{
+  asm_apply(z, v, Zi, g, ncell);
+}
+
+int asm_setup(Context *c, float *Z)
+{
+  if (c->batch) {
+    set_error("additive Schwarz (pc = 4) needs a single lattice; a batch takes pc 0, 1 or 2");
+    return IGAPGPU_ERR_ARG;
+  }
+  static bool attr = false;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(asm_setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)asm_smem_bytes()));
+    attr = true;
+  }
+  const CellGeom cg = cell_geom(c);
+  asm_setup_kernel<<<(unsigned)cell_count(cg), AS_THREADS, asm_smem_bytes(), c->stream>>>(c->d_rowptr, c->d_vals, Z,
+                                                                                          cg);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
 // Right-preconditioned GMRES(m) with MGS, x in/out (device), b device.
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its_out,
               double *rnorm_out)
@@ -260,6 +286,14 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
         c->d_rowptr, c->d_vals, c->d_cinv, cg, ncell);
     count_launch();
     IGAP_CHECK_LAUNCH();
+  } else if (o->pc == 4) {  // restricted additive Schwarz
+    if (!c->d_asmz && cudaMalloc(&c->d_asmz, sizeof(float) * (size_t)ncell * AS_NC * AS_N) != cudaSuccess) {
+      cudaGetLastError();
+      c->d_asmz = nullptr;
+      set_error("additive Schwarz: allocation of %lld subdomains failed", (long long)ncell);
+      return IGAPGPU_ERR_NOMEM;
+    }
+    if ((r = asm_setup(c, c->d_asmz))) return r;
   }
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   double rnorm0 = -1.0, rnorm = 0.0;
@@ -301,6 +335,9 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
         count_launch();
       } else if (o->pc == 3) {
         cblock_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_cinv, cg, ncell);
+        count_launch();
+      } else if (o->pc == 4) {
+        asm_kernel<<<vb, 256, 0, c->stream>>>(zj, vj, c->d_asmz, cg, ncell);
         count_launch();
       } else {
         IGAP_CUDA(cudaMemcpyAsync(zj, vj, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));

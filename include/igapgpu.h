@@ -98,7 +98,10 @@ typedef struct {
   double ksp_dtol;
   int ksp_max_it;
   int pc;              /* 0 = none, 1 = Jacobi, 2 = point-block Jacobi (3 x 3 blocks of each control point),
-                          3 = cell-block Jacobi (blocks of 2 x 2 x 2 control points, up to 24 x 24; single lattice) */
+                          3 = cell-block Jacobi (blocks of 2 x 2 x 2 control points, up to 24 x 24; single lattice),
+                          4 = restricted additive Schwarz: the cells of 3 extended by one control-point layer
+                              (up to 192 DOFs), FP32 subdomain solves, each DOF from its own cell (the
+                              reference's default PCASM / PC_ASM_RESTRICT, src/interface.c:240-241; single lattice) */
   int use_graphs;      /* 1: assembly and GMRES cycles replayed as CUDA graphs */
   int orth;            /* GMRES orthogonalisation: 0 = modified Gram-Schmidt (the reference's
                           KSPGMRESModifiedGramSchmidtOrthogonalization, src/interface.c:234);
