@@ -27,14 +27,18 @@ __device__ __forceinline__ double f32_to_f64(float f)
   return __hiloint2double((int)hi, (int)(b << 29));
 }
 
+static __device__ __noinline__ double f32_to_f64_scaled_rare(float f, int sh) { return ldexp((double)f, sh); }
+
 // f * 2^sh as a double, the scaling folded into the exponent on the integer
 // pipe (exact); |sh| small enough that the result stays a normal double.
+// Zeros stay on the integer pipe; subnormal, infinite and NaN inputs take an
+// out-of-line call (the FP64 pipe only there).
 __device__ __forceinline__ double f32_to_f64_scaled(float f, int sh)
 {
   const uint32_t b = __float_as_uint(f);
   const uint32_t e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu)
-    return (b & 0x7fffffffu) == 0u ? __hiloint2double((int)(b & 0x80000000u), 0) : ldexp((double)f, sh);
+  if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+  if (__builtin_expect(e == 0u || e == 0xffu, 0)) return f32_to_f64_scaled_rare(f, sh);
   const uint32_t hi = (b & 0x80000000u) | ((uint32_t)((int)e + 896 + sh) << 20) | ((b & 0x7fffffu) >> 3);
   return __hiloint2double((int)hi, (int)(b << 29));
 }

@@ -37,8 +37,8 @@
 //     into four accumulators
 //     straight from the stage (the slices are built once, already in the
 //     operand layout; the same tile is A and B),
-//   warps 4-7: drain TMEM -> G (FP64, shared memory), free the accumulators,
-//     form K and scatter it.
+//   warps 4-7: drain TMEM -> G (FP64, shared memory), free the accumulators;
+//   warps 2-7: form K and scatter it.
 // Every mbarrier wait is bounded; a CTA that gives up waits (bounded) for
 // its copies and MMAs in flight and frees its tensor memory.
 #include <cuda_runtime.h>
@@ -72,6 +72,7 @@ static_assert(OZ_STAGE % 16 == 0 && OZ_CH_BYTES % 16 == 0, "bulk copies and desc
 struct OzSmem {
   unsigned char stage[OZ_NS][OZ_STAGE];
   double G[OZ_ROWS * OZ_GP];
+  double T[NB * NB];                    // mu * trace of each 3 x 3 block of G
   float X[OZ_ROWS * OZ_XP];
   unsigned char pos[NB * NB];
   int64_t rowp[NE];
@@ -288,8 +289,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int i = 0; i < OZ_NS; i++) S.mm_n[i] = mmn[i];
       S.accf_n = accn;
     }
-  } else if (warp >= 4) {  // epilogue, 128 threads: warp & 3 is the TMEM lane quarter
-    const int t = tid - 128, quarter = warp & 3;
+  } else if (warp >= 2) {
+    // epilogue, warps 2-7 (192 threads); warps 4-7 also drain the tensor
+    // memory (warp & 3 is their lane quarter)
+    const int t = tid - 64, quarter = warp & 3;
+    const bool drain = warp >= 4;
     const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
     const int nbv[3] = {m.nbasis[0], nb1, nb2};
     const double lam = L.par[0], mu = L.par[1];
@@ -303,19 +307,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         S.rowp[t] = __ldg(m.rowptr + 3 * cpb + dd);
       }
       if (t < OZ_EXP) S.ex[t] = (int)__ldg(expo + eg * OZ_EXP + t);
-      for (int i = t; i < NB * NB; i += 128) {
+      for (int i = t; i < NB * NB; i += 192) {
         const int b = i / NB, c = i % NB;
         S.pos[i] = (unsigned char)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9,
                                               ey + (c / 3) % 3, ez + c % 3, nbv);
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // exponents in place
-      // the four epilogue warps take the same decision (a named-barrier OR)
-      const uint32_t got = oz_wait(&S.accfull, (uint32_t)j & 1, abort) ? 1u : 0u;
+      // the six warps take the same decision (a named-barrier OR): only the
+      // draining warps wait for the accumulators
+      const uint32_t got = (!drain || oz_wait(&S.accfull, (uint32_t)j & 1, abort)) ? 1u : 0u;
       uint32_t any_failed;
       asm volatile(
           "{\n\t.reg .pred p, q;\n\t"
           "setp.eq.u32 p, %1, 0;\n\t"
-          "bar.red.or.pred q, 1, 128, p;\n\t"
+          "bar.red.or.pred q, 1, 192, p;\n\t"
           "selp.u32 %0, 1, 0, q;\n\t}\n"
           : "=r"(any_failed)
           : "r"(got)
@@ -324,55 +328,61 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         ok = false;
         break;
       }
-      tc::fence_after_sync();
-      const int r = quarter * 32 + lane;
-      const uint32_t rowb = (uint32_t)(quarter * 32) << 16;
-      for (int cb = 0; cb < 3; cb++) {  // X = acc1 to shared memory (its transpose is needed)
-        uint32_t v1[32];
-        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(128 + cb * 32), v1);
-        if (r < OZ_ROWS)
+      if (drain) {
+        tc::fence_after_sync();
+        const int r = quarter * 32 + lane;
+        const uint32_t rowb = (uint32_t)(quarter * 32) << 16;
+        for (int cb = 0; cb < 3; cb++) {  // X = acc1 to shared memory (its transpose is needed)
+          uint32_t v1[32];
+          tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(128 + cb * 32), v1);
+          if (r < OZ_ROWS)
 #pragma unroll
-          for (int jj = 0; jj < 32; jj++)
-            if (cb * 32 + jj < OZ_ROWS) S.X[r * OZ_XP + cb * 32 + jj] = __uint_as_float(v1[jj]);
-      }
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // X complete
-      for (int cb = 0; cb < 3; cb++) {
-        uint32_t v0[32], v2[32], v3[32];
-        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(cb * 32), v0);
-        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(256 + cb * 32), v2);
-        tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(384 + cb * 32), v3);
-        if (r < OZ_ROWS) {
-          const int er = S.ex[r] - 16;
+            for (int jj = 0; jj < 32; jj++)
+              if (cb * 32 + jj < OZ_ROWS) S.X[r * OZ_XP + cb * 32 + jj] = __uint_as_float(v1[jj]);
+        }
+        asm volatile("bar.sync 2, 128;" ::: "memory");  // X complete
+        for (int cb = 0; cb < 3; cb++) {
+          uint32_t v0[32], v2[32], v3[32];
+          tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(cb * 32), v0);
+          tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(256 + cb * 32), v2);
+          tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(384 + cb * 32), v3);
+          if (r < OZ_ROWS) {
+            const int er = S.ex[r] - 16;
 #pragma unroll
-          for (int jj = 0; jj < 32; jj++) {
-            const int c = cb * 32 + jj;
-            if (c < OZ_ROWS) {
-              const int sh = er + S.ex[c];
-              const float xa = S.X[r * OZ_XP + c], xb = S.X[c * OZ_XP + r];
-              const float t = xa + xb, bv = t - xa;                     // two-sum: t + e = xa + xb
-              const float e = (xa - (t - bv)) + (xb - bv);
-              const float lo = e + (__uint_as_float(v2[jj]) + __uint_as_float(v3[jj]));
-              S.G[r * OZ_GP + c] = (f32_to_f64_scaled(__uint_as_float(v0[jj]), sh) + f32_to_f64_scaled(t, sh)) +
-                                   f32_to_f64_scaled(lo, sh);
+            for (int jj = 0; jj < 32; jj++) {
+              const int c = cb * 32 + jj;
+              if (c < OZ_ROWS) {
+                const int sh = er + S.ex[c];
+                const float xa = S.X[r * OZ_XP + c], xb = S.X[c * OZ_XP + r];
+                const float tt = xa + xb, bv = tt - xa;  // two-sum: tt + e = xa + xb
+                const float e = (xa - (tt - bv)) + (xb - bv);
+                const float lo = e + (__uint_as_float(v2[jj]) + __uint_as_float(v3[jj]));
+                S.G[r * OZ_GP + c] = (f32_to_f64_scaled(__uint_as_float(v0[jj]), sh) + f32_to_f64_scaled(tt, sh)) +
+                                     f32_to_f64_scaled(lo, sh);
+              }
             }
           }
         }
+        tc::fence_before_sync();
+        mbar_arrive1(&S.accempty);  // the next element's MMAs may overwrite the accumulators
       }
-      tc::fence_before_sync();
-      mbar_arrive1(&S.accempty);  // the next element's MMAs may overwrite the accumulators
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // G, rowp, pos of the element complete
+      asm volatile("bar.sync 1, 192;" ::: "memory");  // G, rowp, pos of the element complete
+      for (int u = t; u < NB * NB; u += 192) {  // mu tr G_bc
+        const int b = u / NB, c = u % NB;
+        S.T[u] = mu * ((S.G[(3 * b) * OZ_GP + 3 * c] + S.G[(3 * b + 1) * OZ_GP + 3 * c + 1]) +
+                       S.G[(3 * b + 2) * OZ_GP + 3 * c + 2]);
+      }
+      asm volatile("bar.sync 1, 192;" ::: "memory");
       // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc
-      for (int u = t; u < NE * NE; u += 128) {
+      for (int u = t; u < NE * NE; u += 192) {
         const int rr = u / NE, cc = u - NE * rr;
         const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
         double kk = fma(lam, S.G[(3 * b + d) * OZ_GP + 3 * c + e], mu * S.G[(3 * b + e) * OZ_GP + 3 * c + d]);
-        if (d == e)
-          kk = fma(mu, S.G[(3 * b) * OZ_GP + 3 * c] + S.G[(3 * b + 1) * OZ_GP + 3 * c + 1] +
-                           S.G[(3 * b + 2) * OZ_GP + 3 * c + 2], kk);
+        if (d == e) kk += S.T[NB * b + c];
         double *dst = vals + S.rowp[rr] + 3 * (int)S.pos[NB * b + c] + e;
         asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(kk) : "memory");
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // before the next element overwrites them
+      asm volatile("bar.sync 1, 192;" ::: "memory");  // before the next element overwrites them
     }
     if (!ok) S.abort = 1;
   }

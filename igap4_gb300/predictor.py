@@ -120,7 +120,12 @@ class Scales:
     u: float = 1.0
     load: float = 1.0   # scale of the third input block (load increment or residual)
     out: float = 1.0
-    mode: str = "load"  # third input block: "load" increment or "residual" F(u_ext)
+    # "load": inputs u_n, u_{n-1}, load increment; "residual": u_n, u_{n-1},
+    # F(u_ext); "relative": u_n, the last increment u_n - u_{n-1} and the load
+    # increment, the increment and the output measured in units of the
+    # sample's own largest increment component (the state of a transforming
+    # material grows by orders of magnitude along a trajectory)
+    mode: str = "load"
 
 
 def features(u_n, u_nm1, third, scales: Scales):
@@ -131,12 +136,23 @@ def features(u_n, u_nm1, third, scales: Scales):
     P = u_n.numel() // 3
     x = torch.empty((P, 9), dtype=torch.float32, device=u_n.device)
     x[:, 0:3] = (u_n.view(P, 3) / scales.u).float()
-    x[:, 3:6] = (u_nm1.view(P, 3) / scales.u).float()
+    if scales.mode == "relative":
+        inc = u_n - u_nm1
+        x[:, 3:6] = (inc / step_scale(inc)).view(P, 3).float()
+    else:
+        x[:, 3:6] = (u_nm1.view(P, 3) / scales.u).float()
     if scales.mode == "residual":
         x[:, 6:9] = (torch.as_tensor(third, device=u_n.device).view(P, 3) / scales.load).float()
     else:
         x[:, 6:9] = torch.as_tensor(np.asarray(third, np.float32) / scales.load, device=u_n.device)
     return x
+
+
+def step_scale(inc):
+    """The largest component of a state increment (a device scalar), 1e-300 at rest."""
+    import torch
+
+    return torch.clamp(inc.abs().max(), min=1e-300)
 
 
 class LearnedPredictor:
@@ -168,7 +184,10 @@ class LearnedPredictor:
         else:
             x = features(u_n, u_nm1, self.dir * dload_scalar, self.scales)[None]
         self.net.forward(x, self.out)
-        return self.out.view(-1).double() * self.scales.out
+        corr = self.out.view(-1).double() * self.scales.out
+        if self.scales.mode == "relative":
+            corr = corr * step_scale(u_n - u_nm1)
+        return corr
 
     def __call__(self, u_n, u_nm1, dload_scalar):
         return u_n + (u_n - u_nm1) + self.correction(u_n, u_nm1, dload_scalar)

@@ -77,17 +77,24 @@ def residual_inputs(A, trajs, dt):
     return R
 
 
-def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None, R=None):
+def train(A, X, Y, epochs=40, batch=8, lr=2e-3, seed=0, storage="bf16", log=None, R=None, relative=False):
     """Adam on the samples; R (residual inputs, residual_inputs()) selects
-    the residual-input network, else the load-increment input."""
+    the residual-input network, relative=True the step-relative one, else the
+    load-increment input."""
     import torch
 
     from .predictor import ConvNet, Scales, features
 
     lattice = tuple(n + 2 for n in A.nelem)
     su = max(1e-30, max(np.abs(x[0]).max() for x in X))
+    if relative:  # targets in units of each sample's largest increment component
+        sd = [max(1e-300, np.abs(x[0] - x[1]).max()) for x in X]
+        Y = [y / s for y, s in zip(Y, sd)]
     so = max(1e-30, max(np.abs(y).max() for y in Y))
-    if R is not None:
+    if relative:
+        scales = Scales(u=su, load=max(1e-30, max(np.abs(x[2]).max() for x in X)), out=so, mode="relative")
+        thirds = [x[2] for x in X]
+    elif R is not None:
         scales = Scales(u=su, load=max(1e-30, max(np.abs(r).max() for r in R)), out=so, mode="residual")
         thirds = R
     else:
@@ -171,8 +178,9 @@ def main():
     ap.add_argument("--amax", type=float, default=1e-3)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval-nelem", default=None, help="evaluate on another mesh (default: same)")
-    ap.add_argument("--features", default="load", choices=["load", "residual", "both"],
-                    help="third input block of the network: load increment, residual at the extrapolation")
+    ap.add_argument("--features", default="load", choices=["load", "residual", "both", "relative"],
+                    help="network inputs: load increment, residual at the extrapolation, or the step-relative "
+                         "form (last increment and correction in units of the sample's largest increment)")
     ap.add_argument("--compare-shortened", action="store_true",
                     help="also evaluate the best of the guess and two shortened steps along its correction")
     ap.add_argument("--prec", default="fp64", choices=["fp64", "split"], help="Newton tangent precision")
@@ -199,7 +207,7 @@ def main():
     for mode in modes:
         t0 = time.perf_counter()
         nets[mode] = train(A, X, Y, epochs=a.epochs, R=R if mode == "residual" else None,
-                           log=lambda msg: print(msg, file=sys.stderr, flush=True))
+                           relative=mode == "relative", log=lambda msg: print(msg, file=sys.stderr, flush=True))
         t_train[mode] = time.perf_counter() - t0
     if a.eval_nelem:
         A.close()

@@ -51,3 +51,18 @@ def test_feature_channels(mode):
     np.testing.assert_allclose(x[:, 3:6].numpy().ravel(), -un.numpy() / 2.0)
     expect = np.tile([0.0, 0.0, 2.0], (P, 1)) if mode == "load" else np.full((P, 3), 2.0)
     np.testing.assert_allclose(x[:, 6:9].numpy(), expect)
+
+
+def test_feature_channels_relative():
+    """Step-relative inputs: u_n / s_u, the last increment in units of its own
+    largest component, the load increment / s_load."""
+    P = 4
+    un = torch.arange(3 * P, dtype=torch.float64) * 0.5
+    unm1 = un - torch.linspace(-3.0, 1.5, 3 * P, dtype=torch.float64)
+    sc = Scales(u=2.0, load=4.0, out=1.0, mode="relative")
+    x = features(un, unm1, np.array([0.0, 0.0, 8.0]), sc)
+    inc = (un - unm1).numpy()
+    np.testing.assert_allclose(x[:, 0:3].numpy().ravel(), un.numpy() / 2.0)
+    np.testing.assert_allclose(x[:, 3:6].numpy().ravel(), inc / np.abs(inc).max(), rtol=1e-6)
+    assert np.abs(x[:, 3:6].numpy()).max() == pytest.approx(1.0)
+    np.testing.assert_allclose(x[:, 6:9].numpy(), np.tile([0.0, 0.0, 2.0], (P, 1)))
