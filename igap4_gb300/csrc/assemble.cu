@@ -886,6 +886,7 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   int rc = init_pairs();
   if (rc) return rc;
   if (c->batch) return launch_batch_assembly(c, do_res, do_tan, RR, vals);
+  if (c->porder == 3) return launch_assembly_p3(c, do_res, do_tan, RR, vals);
   if (do_res) {
     IGAP_CUDA(cudaMemcpyAsync(RR, c->d_Fneu, sizeof(double) * c->ndof, cudaMemcpyDeviceToDevice,
                               c->stream));
@@ -1043,6 +1044,7 @@ int launch_impose_dirichlet(Context *c, double *U)
 
 int launch_dirichlet_matrix(Context *c, double *vals)
 {
+  if (c->porder == 3) return launch_dirichlet_matrix_p3(c, vals);
   if (c->n_dir == 0) return IGAPGPU_OK;
   dirichlet_matrix_kernel<<<(unsigned)((c->n_dir + 127) / 128), 128, 0, c->stream>>>(
       c->d_dir_rows, c->n_dir, c->d_rowptr, c->d_cols, c->nbasis[0], c->nbasis[1], c->nbasis[2],
@@ -1082,8 +1084,8 @@ extern "C" int igapgpu_debug_slot_counts(igapgpu_t c, double *counts)
 {
   using namespace igap;
   if (!c || !counts) return IGAPGPU_ERR_ARG;
-  if (c->batch) {
-    set_error("debug_slot_counts: not available on a batch context");
+  if (c->batch || c->porder != P) {
+    set_error("debug_slot_counts: quadratic single-lattice contexts only");
     return IGAPGPU_ERR_ARG;
   }
   const bool host = !is_device_ptr(counts);

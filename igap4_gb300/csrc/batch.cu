@@ -329,6 +329,10 @@ int igapgpu_batch_init(igapgpu_t *out, int ninst, const igapgpu_mesh_desc *meshe
   for (int i = 0; i < ninst; i++) {
     int r = check_instance_args(meshes + i, phys + i, bcs + i, nquad);
     if (r) return r;
+    if (meshes[i].porder != P) {
+      set_error("batch: instance %d has degree %d; batches hold quadratic instances", i, meshes[i].porder);
+      return IGAPGPU_ERR_ARG;
+    }
     if (phys[i].law != phys[0].law) {
       set_error("batch: instance %d has law %d, instance 0 law %d (one law per batch)", i, phys[i].law,
                 phys[0].law);

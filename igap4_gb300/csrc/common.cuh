@@ -31,6 +31,14 @@ constexpr int NDD = 10;                 // value, 3 first, 6 second derivatives
 constexpr int NE = 3 * NB;              // 81 element DOFs
 constexpr int TAB = 3 * P1 + 2;         // 1-D table entry: N, dN, ddN of 3 functions, xi, h
 constexpr int MAXQ = 6;                 // max Gauss points per direction
+// sizes that follow the B-spline degree (the kernels above P are the quadratic
+// ones; the cubic path of cubic.cu instantiates these for degree 3)
+template <int PD>
+struct Deg {
+  static constexpr int P1 = PD + 1, NB = P1 * P1 * P1, NE = 3 * NB, TAB = 3 * P1 + 2;
+};
+// basis-table entry length of a degree
+__host__ __device__ constexpr int tab_len(int pd) { return 3 * (pd + 1) + 2; }
 
 // Reference-ABI constants (include/physimpl.h, src/assmcore_iga.c)
 constexpr int NFACE = 6;
@@ -118,6 +126,7 @@ struct BatchArgs {
 struct Context {
   // problem
   int law, torder, nquad, prec;
+  int porder = P;                  // B-spline degree: 2, or 3 (cubic.cu)
   double par[9];
   int nelem[3], nbasis[3];
   int64_t ndof, nnz, nelem_total, ncp;
@@ -265,6 +274,13 @@ int launch_tc_tangent(Context *c, double *vals, const DevLaw &L);
 int launch_tc_gram(Context *c, double *vals);
 // cached: every instance has its Gram operands (d_gop); persistent CTAs per SM of nsm
 int launch_tc_gram_batch(Context *c, const BatchArgs &a, int nsm, double *vals, bool cached);
+// cubic.cu (degree 3: basis tables, pattern, Neumann load, Dirichlet columns,
+// FP64 element kernel)
+int launch_basis_tables_p3(Context *c);
+int launch_pattern_cols_p3(Context *c);
+int launch_neumann_p3(Context *c, const double nfac[NFACE][2]);
+int launch_dirichlet_matrix_p3(Context *c, double *vals);
+int launch_assembly_p3(Context *c, bool do_res, bool do_tan, double *RR, double *vals);
 // tc_ozaki.cu (linear law, BF16 slices, FP64-quality)
 int ensure_ozaki_operands(Context *c);
 int launch_tc_ozaki(Context *c, double *vals);

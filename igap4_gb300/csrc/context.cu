@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <map>
+#include <utility>
 #include <mutex>
 #include <vector>
 
@@ -123,7 +124,7 @@ static void dirichlet_face(const Context *c, const std::vector<double> kn[3], in
 {
   int da, db, dn;
   face_dirs(face, da, db, dn);
-  const int p = P;
+  const int p = c->porder;
   const int dirs[2] = {da, db};
   double pf[3] = {c->bc.par_dirichlet[3 * d + da], c->bc.par_dirichlet[3 * d + db],
                   c->bc.par_dirichlet[3 * d + dn]};
@@ -137,17 +138,34 @@ static void dirichlet_face(const Context *c, const std::vector<double> kn[3], in
     const double W0 = kv[p];
     // value and slope of the affine function at the first knot, matched by
     // the first p control values: solve  sum_j N_j^(i)(W0) x_j = v_i
-    double A[P][P], v[P];
+    double A[4][4], v[4];
     for (int i = 0; i < p; i++) {
       v[i] = (i == 0) ? pf[bb] * W0 : (i == 1 ? pf[bb] : 0.0);
       for (int j = 0; j < p; j++) A[i][j] = basis_deriv(kv.data(), (int)kv.size(), i, j, p, W0);
     }
-    // 2x2 solve (P = 2)
-    double det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
-    double x0 = (v[0] * A[1][1] - A[0][1] * v[1]) / det;
-    double x1 = (A[0][0] * v[1] - A[1][0] * v[0]) / det;
-    d1[bb][0] = x0;
-    d1[bb][1] = x1;
+    if (p == 2) {  // the 2 x 2 solve by Cramer's rule
+      double det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+      d1[bb][0] = (v[0] * A[1][1] - A[0][1] * v[1]) / det;
+      d1[bb][1] = (A[0][0] * v[1] - A[1][0] * v[0]) / det;
+    } else {  // p x p: Gaussian elimination with partial pivoting
+      for (int k = 0; k < p; k++) {
+        int pr = k;
+        for (int i = k + 1; i < p; i++)
+          if (fabs(A[i][k]) > fabs(A[pr][k])) pr = i;
+        for (int j = 0; j < p; j++) std::swap(A[k][j], A[pr][j]);
+        std::swap(v[k], v[pr]);
+        for (int i = k + 1; i < p; i++) {
+          const double f = A[i][k] / A[k][k];
+          for (int j = k; j < p; j++) A[i][j] -= f * A[k][j];
+          v[i] -= f * v[k];
+        }
+      }
+      for (int k = p - 1; k >= 0; k--) {
+        double s = v[k];
+        for (int j = k + 1; j < p; j++) s -= A[k][j] * d1[bb][j];
+        d1[bb][k] = s / A[k][k];
+      }
+    }
     for (int i = p; i < nb; i++) d1[bb][i] = d1[bb][i - 1] + (kv[i + p] - kv[i]) / ((double)p) * pf[bb];
   }
   const int n0 = c->nbasis[da], n1 = c->nbasis[db];
@@ -213,14 +231,15 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   }
   // mesh
   std::vector<double> kn[3];
+  const int pd = c->porder;
   for (int d = 0; d < 3; d++) {
-    const int nk = c->nelem[d] + 1 + 2 * P;
+    const int nk = c->nelem[d] + 1 + 2 * pd;
     kn[d].assign(mesh->knots[d], mesh->knots[d] + nk);
     int r = dev_alloc(&c->d_knots[d], nk);
     if (r) return r;
     IGAP_CUDA(cudaMemcpy(c->d_knots[d], kn[d].data(), sizeof(double) * nk, cudaMemcpyHostToDevice));
-    if ((r = dev_alloc(&c->d_tab[d], (size_t)c->nelem[d] * c->nquad * TAB))) return r;
-    if ((r = dev_alloc(&c->d_tabn[d], (size_t)c->nelem[d] * c->nquad * TAB))) return r;
+    if ((r = dev_alloc(&c->d_tab[d], (size_t)c->nelem[d] * c->nquad * tab_len(pd)))) return r;
+    if ((r = dev_alloc(&c->d_tabn[d], (size_t)c->nelem[d] * c->nquad * tab_len(pd)))) return r;
   }
   int r;
   if ((r = dev_alloc(&c->d_w, c->ncp))) return r;
@@ -234,12 +253,13 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   if ((r = dev_alloc(&c->d_wq, c->nquad))) return r;
   IGAP_CUDA(cudaMemcpy(c->d_xq, xq, sizeof(double) * c->nquad, cudaMemcpyHostToDevice));
   IGAP_CUDA(cudaMemcpy(c->d_wq, wq, sizeof(double) * c->nquad, cudaMemcpyHostToDevice));
-  if ((r = launch_basis_tables(c))) return r;
+  if ((r = pd == 3 ? launch_basis_tables_p3(c) : launch_basis_tables(c))) return r;
   // geometry cache: built once when it fits (leaving headroom for the matrix
-  // and the Krylov workspace); IGAPGPU_GEOMETRY_CACHE=0 disables it
+  // and the Krylov workspace); IGAPGPU_GEOMETRY_CACHE=0 disables it; the
+  // cubic path evaluates its geometry in the element kernel
   {
     const char *env = getenv("IGAPGPU_GEOMETRY_CACHE");
-    const bool want = !(env && env[0] == '0');
+    const bool want = !(env && env[0] == '0') && pd == P;
     const size_t npts = (size_t)c->nquad * c->nquad * c->nquad;
     const size_t bytes = sizeof(double) * (size_t)c->nelem_total * npts * (NB * NDD + 2);
     size_t freeb = 0, totb = 0;
@@ -275,7 +295,7 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   rowptr[0] = 0;
   {
     int64_t row = 0;
-    auto cnt = [&](int i, int nb) { return (i < P ? i : P) + 1 + (i > nb - 1 - P ? nb - 1 - i : P); };
+    auto cnt = [&](int i, int nb) { return (i < pd ? i : pd) + 1 + (i > nb - 1 - pd ? nb - 1 - i : pd); };
     for (int ix = 0; ix < c->nbasis[0]; ix++)
       for (int iy = 0; iy < c->nbasis[1]; iy++)
         for (int iz = 0; iz < c->nbasis[2]; iz++) {
@@ -298,7 +318,7 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
   if ((r = dev_alloc(&c->d_cols, c->nnz))) return r;
   if ((r = dev_alloc(&c->d_vals, c->nnz))) return r;
   IGAP_CUDA(cudaMemcpy(c->d_rowptr, rowptr.data(), sizeof(int64_t) * (c->ndof + 1), cudaMemcpyHostToDevice));
-  if ((r = launch_pattern_cols(c))) return r;
+  if ((r = pd == 3 ? launch_pattern_cols_p3(c) : launch_pattern_cols(c))) return r;
   // state, residual, staging
   if ((r = dev_alloc(&c->d_Uhist, (size_t)(c->torder + 1) * c->ndof))) return r;
   IGAP_CUDA(cudaMemset(c->d_Uhist, 0, sizeof(double) * (c->torder + 1) * c->ndof));
@@ -357,12 +377,12 @@ static int init_impl(Context *c, const igapgpu_mesh_desc *mesh)
     const std::vector<double> &kz = kn[dn];
     const int nk = (int)kz.size();
     const double zq = (face % 2 == 0) ? kz[0] : kz[nk - 1];
-    const int lay0 = (face % 2 == 0) ? 0 : c->nelem[dn] + P - 1;
-    const int lay1 = (face % 2 == 0) ? 1 : c->nelem[dn] + P - 2;
-    nfac[face][0] = basis_deriv(kz.data(), nk, 1, lay0, P, zq);
-    nfac[face][1] = basis_deriv(kz.data(), nk, 1, lay1, P, zq);
+    const int lay0 = (face % 2 == 0) ? 0 : c->nelem[dn] + pd - 1;
+    const int lay1 = (face % 2 == 0) ? 1 : c->nelem[dn] + pd - 2;
+    nfac[face][0] = basis_deriv(kz.data(), nk, 1, lay0, pd, zq);
+    nfac[face][1] = basis_deriv(kz.data(), nk, 1, lay1, pd, zq);
   }
-  if ((r = launch_neumann(c, nfac))) return r;
+  if ((r = pd == 3 ? launch_neumann_p3(c, nfac) : launch_neumann(c, nfac))) return r;
   // Dirichlet rows and values, in the reference's insertion order; a row
   // listed twice keeps the last value (INSERT_VALUES, src/assmcore_iga.c:467,489)
   {
@@ -443,12 +463,13 @@ int check_instance_args(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *
     set_error("null argument");
     return IGAPGPU_ERR_ARG;
   }
-  if (mesh->porder != P) {
-    set_error("porder %d unsupported: the device basis is quadratic (as eval_Bspline)", mesh->porder);
+  if (mesh->porder != 2 && mesh->porder != 3) {
+    set_error("porder %d unsupported: the device bases are quadratic (as eval_Bspline) and cubic",
+              mesh->porder);
     return IGAPGPU_ERR_ARG;
   }
   for (int d = 0; d < 3; d++)
-    if (mesh->nelem[d] < P || !mesh->knots[d]) {
+    if (mesh->nelem[d] < mesh->porder || !mesh->knots[d]) {
       set_error("direction %d has %d elements; at least porder are required", d, mesh->nelem[d]);
       return IGAPGPU_ERR_ARG;
     }
@@ -488,11 +509,12 @@ Context *new_context(const igapgpu_mesh_desc *mesh, const igapgpu_phys_desc *phy
   c->nquad = nquad;
   c->prec = IGAPGPU_PREC_FP64;
   c->bc = *bc;
+  c->porder = mesh->porder;
   c->ncp = 1;
   c->nelem_total = 1;
   for (int d = 0; d < 3; d++) {
     c->nelem[d] = mesh->nelem[d];
-    c->nbasis[d] = mesh->nelem[d] + P;
+    c->nbasis[d] = mesh->nelem[d] + mesh->porder;
     c->ncp *= c->nbasis[d];
     c->nelem_total *= c->nelem[d];
   }
@@ -749,7 +771,7 @@ int igapgpu_set_neumann(igapgpu_t c, const double *table)
   if (!c || !table) return IGAPGPU_ERR_ARG;
   if (c->batch) return batch_set_neumann(c, table);
   for (int i = 0; i < 36; i++) c->bc.neumann[i] = table[i];
-  return launch_neumann(c, c->nfac);
+  return c->porder == 3 ? launch_neumann_p3(c, c->nfac) : launch_neumann(c, c->nfac);
 }
 
 int igapgpu_set_precision(igapgpu_t c, int mode)
@@ -757,6 +779,10 @@ int igapgpu_set_precision(igapgpu_t c, int mode)
   if (!c) return IGAPGPU_ERR_ARG;
   if (mode != IGAPGPU_PREC_FP64 && mode != IGAPGPU_PREC_SPLIT && mode != IGAPGPU_PREC_OZAKI) {
     set_error("unknown precision mode %d", mode);
+    return IGAPGPU_ERR_ARG;
+  }
+  if (mode != IGAPGPU_PREC_FP64 && c->porder != P) {
+    set_error("degree %d assembles in FP64 only (the tensor-core tangents are quadratic)", c->porder);
     return IGAPGPU_ERR_ARG;
   }
   if (mode == IGAPGPU_PREC_OZAKI && c->batch) {

@@ -402,6 +402,10 @@ extern "C" int igapgpu_density(igapgpu_t c, double *HH, int *ndensity)
     set_error("density: null argument");
     return IGAPGPU_ERR_ARG;
   }
+  if (c->porder != P) {
+    set_error("density: quadratic meshes only");
+    return IGAPGPU_ERR_ARG;
+  }
   if (c->batch) {
     set_error("density: not available on a batch context");
     return IGAPGPU_ERR_ARG;
@@ -441,6 +445,10 @@ extern "C" int igapgpu_sample_field(igapgpu_t c, int nppe, double *field, double
   NvtxRange range("igapgpu_sample_field");
   if (!c) {
     set_error("sample_field: null context");
+    return IGAPGPU_ERR_ARG;
+  }
+  if (c->porder != P) {
+    set_error("sample_field: quadratic meshes only");
     return IGAPGPU_ERR_ARG;
   }
   if (c->batch) {

@@ -17,12 +17,14 @@ __device__ __forceinline__ int hess_slot(int i, int m)
 // float -> double on the integer pipe (bit-exact with the conversion for
 // normal numbers and zeros; subnormals, infinities and NaN take the
 // conversion instruction): FP64 work is scarce on this GPU.
+static __device__ __noinline__ double f32_to_f64_rare(float f) { return (double)f; }
+
 __device__ __forceinline__ double f32_to_f64(float f)
 {
   const uint32_t b = __float_as_uint(f);
   const uint32_t e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu)
-    return (b & 0x7fffffffu) == 0u ? __hiloint2double((int)(b & 0x80000000u), 0) : (double)f;
+  if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+  if (__builtin_expect(e == 0u || e == 0xffu, 0)) return f32_to_f64_rare(f);
   const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
   return __hiloint2double((int)hi, (int)(b << 29));
 }

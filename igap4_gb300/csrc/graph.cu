@@ -318,7 +318,7 @@ static int build_gmres_graph(Context *c, int m, int pc, int orth)
   int64_t nodes = 0;
   IGAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   gm_reset<<<1, 1, 0, s>>>(gw->st);
-  const int nb0 = c->batch ? 0 : c->nbasis[0];
+  const int nb0 = (c->batch || c->porder != P) ? 0 : c->nbasis[0];
   gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->x, gw->r, n, nullptr, nb0, c->nbasis[1],
                              c->nbasis[2]);
   gm_sub_from<<<vb, 256, 0, s>>>(gw->r, gw->b, n);
@@ -389,6 +389,10 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
   const int orth = o->orth == 1 ? 1 : 0;
   if (m > 1000) {
     set_error("graph GMRES: restart %d above 1000", m);
+    return IGAPGPU_ERR_ARG;
+  }
+  if ((pc == 3 || pc == 4) && c->porder != P) {
+    set_error("block preconditioners (pc = 3, 4) use the quadratic stencil; degree 3 takes pc 0, 1 or 2");
     return IGAPGPU_ERR_ARG;
   }
   if ((pc == 3 || pc == 4) && c->batch) {

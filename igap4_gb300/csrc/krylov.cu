@@ -138,7 +138,9 @@ static unsigned vec_blocks(int64_t n)
 int spmv(Context *c, const double *vals, const double *x, double *y)
 {
   const int64_t n = c->ndof;
-  const int nb0 = c->batch ? 0 : c->nbasis[0];  // a batch's rows belong to different lattices
+  // a batch's rows belong to different lattices; the structured columns are
+  // those of the quadratic stencil
+  const int nb0 = (c->batch || c->porder != P) ? 0 : c->nbasis[0];
   spmv_csr_kernel<<<(unsigned)((n * SPMV_G + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n,
                                                                             nb0, c->nbasis[1], c->nbasis[2]);
   count_launch();
@@ -272,6 +274,10 @@ int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts 
   const unsigned vb = vec_blocks(n);
   const CellGeom cg = cell_geom(c);
   const int64_t ncell = cell_count(cg);
+  if ((o->pc == 3 || o->pc == 4) && c->porder != P) {
+    set_error("block preconditioners (pc = 3, 4) use the quadratic stencil; degree 3 takes pc 0, 1 or 2");
+    return IGAPGPU_ERR_ARG;
+  }
   if (o->pc == 1) {
     get_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, c->d_vals, c->d_diag, n);
     count_launch();

@@ -54,6 +54,23 @@
 namespace igap {
 
 namespace {
+// Error-free transformations on the FP32 pipe (Knuth's two-sum; the
+// fused-multiply-add two-product): s + e == a + b and p + e == a * b exactly.
+__device__ __forceinline__ float two_sum(float a, float b, float &e)
+{
+  const float s = __fadd_rn(a, b), bv = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+  return s;
+}
+__device__ __forceinline__ float two_prod(float a, float b, float &e)
+{
+  const float p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+  return p;
+}
+// 2^k as a float (k in the normal range)
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
 constexpr int OZ_THREADS = 256;
 constexpr int OZ_ROWS = 81;
 constexpr int OZ_RG = 11;                               // row groups holding rows 0..87
@@ -71,8 +88,8 @@ static_assert(OZ_STAGE % 16 == 0 && OZ_CH_BYTES % 16 == 0, "bulk copies and desc
 
 struct OzSmem {
   unsigned char stage[OZ_NS][OZ_STAGE];
-  double G[OZ_ROWS * OZ_GP];
-  double T[NB * NB];                    // mu * trace of each 3 x 3 block of G
+  float2 G[OZ_ROWS * OZ_GP];            // G as an unevaluated pair (x + y, |y| << |x|)
+  float2 T[NB * NB];                    // mu * trace of each 3 x 3 block of G, likewise
   float X[OZ_ROWS * OZ_XP];
   unsigned char pos[NB * NB];
   int64_t rowp[NE];
@@ -296,7 +313,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const bool drain = warp >= 4;
     const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
     const int nbv[3] = {m.nbasis[0], nb1, nb2};
-    const double lam = L.par[0], mu = L.par[1];
+    // lam and mu as FP32 pairs (hi + lo = the double to 48 bits)
+    const float lamh = (float)L.par[0], laml = (float)(L.par[0] - (double)lamh);
+    const float muh = (float)L.par[1], mul = (float)(L.par[1] - (double)muh);
     bool ok = true;
     for (int j = 0; j < nmine && ok; j++) {
       int ex, ey, ez;
@@ -352,13 +371,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             for (int jj = 0; jj < 32; jj++) {
               const int c = cb * 32 + jj;
               if (c < OZ_ROWS) {
-                const int sh = er + S.ex[c];
-                const float xa = S.X[r * OZ_XP + c], xb = S.X[c * OZ_XP + r];
-                const float tt = xa + xb, bv = tt - xa;  // two-sum: tt + e = xa + xb
-                const float e = (xa - (tt - bv)) + (xb - bv);
-                const float lo = e + (__uint_as_float(v2[jj]) + __uint_as_float(v3[jj]));
-                S.G[r * OZ_GP + c] = (f32_to_f64_scaled(__uint_as_float(v0[jj]), sh) + f32_to_f64_scaled(tt, sh)) +
-                                     f32_to_f64_scaled(lo, sh);
+                // G = 2^sh (acc0 + X + X^T + acc2 + acc3) as a pair: acc0 and X + X^T
+                // exactly (two-sum), the small terms rounded once; the power of
+                // two is exact in FP32 (|sh| < 100)
+                const float sc = pow2f(er + S.ex[c]);
+                float e, err;
+                const float tt = two_sum(S.X[r * OZ_XP + c], S.X[c * OZ_XP + r], e);
+                const float small = __fadd_rn(e, __fadd_rn(__uint_as_float(v2[jj]), __uint_as_float(v3[jj])));
+                const float s = two_sum(__fmul_rn(__uint_as_float(v0[jj]), sc), __fmul_rn(tt, sc), err);
+                S.G[r * OZ_GP + c] = make_float2(s, __fadd_rn(err, __fmul_rn(small, sc)));
               }
             }
           }
@@ -367,18 +388,38 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         mbar_arrive1(&S.accempty);  // the next element's MMAs may overwrite the accumulators
       }
       asm volatile("bar.sync 1, 192;" ::: "memory");  // G, rowp, pos of the element complete
-      for (int u = t; u < NB * NB; u += 192) {  // mu tr G_bc
+      for (int u = t; u < NB * NB; u += 192) {  // mu tr G_bc, as a pair
         const int b = u / NB, c = u % NB;
-        S.T[u] = mu * ((S.G[(3 * b) * OZ_GP + 3 * c] + S.G[(3 * b + 1) * OZ_GP + 3 * c + 1]) +
-                       S.G[(3 * b + 2) * OZ_GP + 3 * c + 2]);
+        const float2 g0 = S.G[(3 * b) * OZ_GP + 3 * c], g1 = S.G[(3 * b + 1) * OZ_GP + 3 * c + 1],
+                     g2 = S.G[(3 * b + 2) * OZ_GP + 3 * c + 2];
+        float e0, e1, q;
+        const float a = two_sum(g0.x, g1.x, e0);
+        const float s = two_sum(a, g2.x, e1);
+        const float low = __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(__fadd_rn(g0.y, g1.y), g2.y));
+        const float th = two_prod(muh, s, q);
+        S.T[u] = make_float2(th, __fadd_rn(q, __fadd_rn(__fmul_rn(muh, low), __fmul_rn(mul, s))));
       }
       asm volatile("bar.sync 1, 192;" ::: "memory");
-      // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc
+      // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc on the
+      // FP32 pipe with error-free products and sums (lam, mu as FP32 pairs); one
+      // FP64 add per entry joins the pair for the FP64 reduction into the CSR values
       for (int u = t; u < NE * NE; u += 192) {
         const int rr = u / NE, cc = u - NE * rr;
         const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
-        double kk = fma(lam, S.G[(3 * b + d) * OZ_GP + 3 * c + e], mu * S.G[(3 * b + e) * OZ_GP + 3 * c + d]);
-        if (d == e) kk += S.T[NB * b + c];
+        const float2 g1 = S.G[(3 * b + d) * OZ_GP + 3 * c + e], g2 = S.G[(3 * b + e) * OZ_GP + 3 * c + d];
+        float e1, e2, e3;
+        const float p1 = two_prod(lamh, g1.x, e1), p2 = two_prod(muh, g2.x, e2);
+        float s = two_sum(p1, p2, e3);
+        float rest = __fadd_rn(__fadd_rn(e1, e2), e3);
+        rest = __fadd_rn(rest, __fadd_rn(__fmaf_rn(lamh, g1.y, __fmul_rn(laml, g1.x)),
+                                         __fmaf_rn(muh, g2.y, __fmul_rn(mul, g2.x))));
+        if (d == e) {
+          const float2 tr = S.T[NB * b + c];
+          float e4;
+          s = two_sum(s, tr.x, e4);
+          rest = __fadd_rn(rest, __fadd_rn(e4, tr.y));
+        }
+        const double kk = f32_to_f64(s) + f32_to_f64(rest);
         double *dst = vals + S.rowp[rr] + 3 * (int)S.pos[NB * b + c] + e;
         asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(kk) : "memory");
       }

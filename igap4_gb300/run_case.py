@@ -6,8 +6,10 @@ profilers and quick timings).
 --what: assemble (residual + tangent), residual, tangent, spmv (after one
 assembly), batch (seeded uneven instances, --ninst of them), solve (Newton-
 GMRES from U = 0 with preconditioner --pc: 0 none, 1 Jacobi, 2 point-block
-Jacobi; prints Newton and Krylov iterations).  Prints the wall time of each
-repetition after the first.
+Jacobi, 3 cell-block Jacobi, 4 additive Schwarz; prints Newton and Krylov
+iterations).  --prec fp64 | split | fp64q (the FP64-quality tensor-core
+tangent), --porder 2 | 3.  Prints the wall time of each repetition after the
+first.
 """
 from __future__ import annotations
 
@@ -20,7 +22,8 @@ import numpy as np
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nelem", default="64,16,16")
-    ap.add_argument("--prec", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--prec", default="fp64", choices=["fp64", "split", "fp64q"])
+    ap.add_argument("--porder", type=int, default=2, choices=[2, 3])
     ap.add_argument("--what", default="assemble",
                     choices=["assemble", "residual", "tangent", "spmv", "batch", "solve"])
     ap.add_argument("--pc", type=int, default=1)
@@ -41,10 +44,10 @@ def main():
     else:
         nelem = tuple(int(v) for v in a.nelem.split(","))
         bct, neu = ig.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
-        knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0))
+        knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0), a.porder)
         par = (1.0, 1.0, 0.1) if law == ig.LAW_LINGRAD else None
-        A = ig.Assembly(nelem, knots, w, X, law=law, par=par, bc_type=bct, neumann=neu)
-    A.set_precision(ig.PREC_SPLIT if a.prec == "split" else ig.PREC_FP64)
+        A = ig.Assembly(nelem, knots, w, X, law=law, par=par, bc_type=bct, neumann=neu, porder=a.porder)
+    A.set_precision({"split": ig.PREC_SPLIT, "fp64q": ig.PREC_OZAKI}.get(a.prec, ig.PREC_FP64))
     dev = torch.device("cuda")
     U = torch.tensor(np.random.default_rng(1).uniform(-1e-2, 1e-2, A.ndof), device=dev)
     RR = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
