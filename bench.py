@@ -3,9 +3,10 @@
 One step = one fused assembly of the residual Vec and the CSR tangent of the
 whole beam (131,072 elements, 64 Gauss points each) on the GPU, state already
 resident in HBM.  Metric: assembled elements/s.  The headline is the
-FP64-quality mode (FP64 residual; tangent on the tensor cores from error-free
-BF16 slices of the Gram operands, its error against the FP64 tangent measured
-in the same run); the pure FP64 and the TF32x3 split modes follow in `modes`.
+FP64-quality mode (residual in double-FP32 arithmetic on the FP32 pipe;
+tangent on the tensor cores from error-free BF16 slices of the Gram operands;
+both errors against the FP64 kernels measured in the same run); the pure FP64
+and the TF32x3 split modes follow in `modes`.
 Also reported:
 
 * e2e  -- the same step through the C ABI with HOST buffers (state in from
@@ -60,6 +61,14 @@ EXEC_FLOP_TC_ELEM = 3 * 2 * 128 * 96 * 256                         # 18.9 M
 EXEC_FLOP_OZ_ELEM = 12 * 2 * 128 * 96 * 256                        # 75.5 M
 # residual-only FP64 kernel: state interpolation, law and projection per point
 EXEC_FLOP_RES_ELEM = 64 * 3420 + 64 * 243
+# double-FP32 residual kernel (res_df_kernel), FP32-pipe lane instructions per
+# point: 2 x 729 compensated dot-product terms of 12 instructions
+# (interpolation, projection), the law in pair arithmetic (~1,090), pair
+# renormalisations (324) and the per-warp column sums (~863)
+EXEC_F32_RES_DF_ELEM = 64 * (2 * 729 * 12 + 1090 + 324 + 863)
+# its HBM bytes per element: the pair cache (64 points x 244 pairs) and the
+# element's 81 residual pairs
+ALG_BYTES_RES_DF_ELEM = 64 * 244 * 8 + 81 * 8
 # FP64-quality tangent: per element the slices (8 chunks x 22,528 B), the row
 # exponents (88 B) and the read-modify-write of its 6,561 FP64 CSR slots
 ALG_BYTES_OZ_ELEM = 8 * 22528 + 88 + 2 * 8 * 6561
@@ -475,20 +484,24 @@ def main():
     for name in others:
         prepare(name)
         runs[name] = measure(precs[name], a.steps, max(1, a.warmup - 1))
-    # tangent error of each mode against the FP64 tangent, at full size
+    # tangent and residual error of each mode against the FP64 kernels, at full size
     A.set_precision(ig.PREC_FP64)
     K64 = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
+    R64 = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
     A.tangent(U, K64)
-    errs = {"fp64": 0.0}
-    Kx = torch.zeros_like(K64)
+    A.residual(U, R64)
+    errs, rerrs = {"fp64": 0.0}, {"fp64": 0.0}
+    Kx, Rx = torch.zeros_like(K64), torch.zeros_like(R64)
     for name in runs:
         if name == "fp64":
             continue
         A.set_precision(precs[name])
         A.tangent(U, Kx)
+        A.residual(U, Rx)
         A.synchronize()
         errs[name] = (torch.linalg.norm(Kx - K64) / torch.linalg.norm(K64)).item()
-    del K64, Kx
+        rerrs[name] = (torch.linalg.norm(Rx - R64) / torch.linalg.norm(R64)).item()
+    del K64, Kx, R64, Rx
     A.set_precision(precs[head])
 
     # e2e through the C ABI with pinned host buffers
@@ -524,6 +537,7 @@ def main():
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     fp64_peak = ig.measure_fp64_peak()
+    fp32_peak = ig.measure_fp32_peak()
     nelem_total, ndof_total, nnz_total = A.nelem_total, A.ndof, A.nnz
     A.close()  # frees the beam's matrix and geometry cache before the batched workload
     del x, y
@@ -561,6 +575,30 @@ def main():
                                 "executed_frac is the FP64 pipe fraction")
         return out
 
+    def res_df_roofline(kms, kl, kc, step_total_ms):
+        """The double-FP32 residual kernel of the tensor-core modes: bound by the
+        FP32 pipe (lane instructions against the measured FMA issue rate)."""
+        per_launch_ms = kms / max(kl, 1)
+        per_launch_el = kc / max(kl, 1)
+        sec = per_launch_ms * 1e-3
+        ach = EXEC_F32_RES_DF_ELEM * per_launch_el / sec / 1e12
+        peak = fp32_peak / 2  # FMA issue rate: one lane instruction per FMA (2 FLOP)
+        gbs = ALG_BYTES_RES_DF_ELEM * per_launch_el / sec / 1e9
+        return {"bound": "fp32", "kernel": "res_df_kernel (linear-law residual in double-FP32 arithmetic: "
+                                          "pair cache, compensated dot products, a thread per Gauss point)",
+                "achieved": ach, "peak": peak, "unit": "T FP32-pipe lane instructions/s", "frac": ach / peak,
+                "executed_fp32_instructions_per_element": EXEC_F32_RES_DF_ELEM,
+                "peak_source": "measured in-run FP32 FMA throughput / 2 (MEASURED_PEAKS.json has no FP32 figure)",
+                "fp32_fma_tflops_measured": fp32_peak,
+                "fp64_equivalent_tflops": RES_FLOP_PER_ELEM * per_launch_el / sec / 1e12,
+                "fp64_equivalent_note": "the residual's FP64 FLOPs per element / kernel time: "
+                                        "against the FP64 pipe's measured peak",
+                "fp64_peak": fp64_peak,
+                "hbm_algorithmic_bytes_per_element": ALG_BYTES_RES_DF_ELEM, "hbm_achieved_gbs": gbs,
+                "hbm_frac": gbs / hbm_peak, "traffic": None,
+                "avg_launch_ms": per_launch_ms, "elements_per_launch": per_launch_el,
+                "kernel_share_of_step": kms / step_total_ms if step_total_ms > 0 else None}
+
     def tc_roofline(name, kms, kl, kc):
         per_launch_ms = kms / max(kl, 1)
         per_launch_el = kc / max(kl, 1)
@@ -582,9 +620,10 @@ def main():
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy) and bf16_tflops",
                 "avg_launch_ms": per_launch_ms, "elements_per_launch": per_launch_el}
 
-    mode_desc = {"fp64q": "FP64 residual; tangent on the tensor cores from error-free BF16 slices (FP64 quality)",
+    mode_desc = {"fp64q": "double-FP32 residual (FP32 pipe); tangent on the tensor cores from error-free BF16 "
+                          "slices (FP64 quality)",
                  "fp64": "FP64 residual and tangent (FP64 pipe)",
-                 "split": "FP64 residual; TF32x3 tensor-core tangent"}
+                 "split": "double-FP32 residual (FP32 pipe); TF32x3 tensor-core tangent"}
     blocks = {}
     for name, (mms, mstep, mkinds, mlaunch) in runs.items():
         res_ms, res_l, res_c = mkinds[0]
@@ -592,25 +631,34 @@ def main():
         tot = mms * a.steps
         b = {"value": world * nelem_total / (mms * 1e-3), "unit": "elements/s", "ms_per_step": mms,
              "step_ms": mstep, "gpu_launches": mlaunch, "precision": mode_desc[name],
-             "tangent_rel_err_vs_fp64": errs.get(name), "setup_launches": prep_launches.get(name),
-             "fp64_kernel_ms_per_step": res_ms / a.steps, "tc_kernel_ms_per_step": tc_ms / a.steps,
-             "fp64_kernel_roofline": fp64_roofline(name, res_ms, res_l, res_c, tot)}
-        if name != "fp64" and tc_l > 0:
-            b["tc_kernel_roofline"] = tc_roofline(name, tc_ms, tc_l, tc_c)
+             "tangent_rel_err_vs_fp64": errs.get(name), "residual_rel_err_vs_fp64": rerrs.get(name),
+             "setup_launches": prep_launches.get(name)}
+        if name == "fp64":
+            b["fp64_kernel_ms_per_step"] = res_ms / a.steps
+            b["fp64_kernel_roofline"] = fp64_roofline(name, res_ms, res_l, res_c, tot)
+        else:
+            b["res_kernel_ms_per_step"] = res_ms / a.steps
+            b["res_kernel_roofline"] = res_df_roofline(res_ms, res_l, res_c, tot)
+            b["tc_kernel_ms_per_step"] = tc_ms / a.steps
+            if tc_l > 0:
+                b["tc_kernel_roofline"] = tc_roofline(name, tc_ms, tc_l, tc_c)
         blocks[name] = b
     hb = blocks[head]
     # the headline's roofline: its dominant kernel
-    if head != "fp64" and "tc_kernel_roofline" in hb and hb["tc_kernel_ms_per_step"] > hb["fp64_kernel_ms_per_step"]:
+    if head == "fp64":
+        roofline = hb["fp64_kernel_roofline"]
+    elif "tc_kernel_roofline" in hb and hb["tc_kernel_ms_per_step"] > hb["res_kernel_ms_per_step"]:
         roofline = hb["tc_kernel_roofline"]
     else:
-        roofline = hb["fp64_kernel_roofline"]
+        roofline = hb["res_kernel_roofline"]
     if rank == 0:
         out = {
             "metric": "assembled elements/s (tangent+residual)", "value": value, "unit": "elements/s",
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp64q": "f64 (tangent: bf16 slices, exact f32 accumulation, f64 recombination)",
-                      "fp64": "f64", "split": "tf32x3/f32-acc tangent, f64 residual"}[head],
+            "dtype": {"fp64q": "f64-quality (residual: f32 pairs; tangent: bf16 slices, exact f32 accumulation, "
+                               "f32-pair recombination; f64 global accumulation)",
+                      "fp64": "f64", "split": "tf32x3/f32-acc tangent, f32-pair residual"}[head],
             "data": "synthetic",
             "config": {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} "
                                    f"({nelem_total} elements, {ndof_total} DOF, nnz {nnz_total}) "
@@ -620,6 +668,7 @@ def main():
                        "state": "seeded uniform [-1e-2,1e-2] per DOF",
                        "precision": mode_desc[head],
                        "tangent_rel_err_vs_fp64": errs.get(head),
+                       "residual_rel_err_vs_fp64": rerrs.get(head),
                        "l2": "flushed (256 MiB write) before every timed step; the 1.25 GB CSR output also exceeds L2",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": ndof_total * 8,

@@ -110,6 +110,7 @@ def lib():
         L.igapgpu_profile_read.argtypes = [vp, vp, vp, vp]
         L.igapgpu_profile_read_kind.argtypes = [vp, ctypes.c_int, vp, vp, vp]
         L.igapgpu_measure_fp64_peak.argtypes = [vp]
+        L.igapgpu_measure_fp32_peak.argtypes = [vp]
         L.igapgpu_tc_selftest.argtypes = [ctypes.c_int, vp]
         L.igapgpu_wait_selftest.argtypes = [ctypes.c_int, ctypes.c_uint, vp]
         L.igapgpu_batch_init.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(MeshDesc),
@@ -430,6 +431,12 @@ def tc_selftest(variant=0):
 def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     _check(lib().igapgpu_measure_fp64_peak(ctypes.byref(t)))
+    return t.value
+
+
+def measure_fp32_peak() -> float:
+    t = ctypes.c_double()
+    _check(lib().igapgpu_measure_fp32_peak(ctypes.byref(t)))
     return t.value
 
 

@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libigapgpu.so")
 
 CU_SOURCES = ["context.cu", "assemble.cu", "krylov.cu", "noalloc.cu", "tc_tangent.cu", "graph.cu", "predictor.cu",
-              "batch.cu", "tc_gram.cu", "tc_ozaki.cu", "density.cu", "cubic.cu"]
+              "batch.cu", "tc_gram.cu", "tc_ozaki.cu", "density.cu", "cubic.cu", "res_df.cu"]
 C_SOURCES: list[str] = []
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

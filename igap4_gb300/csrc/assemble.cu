@@ -906,7 +906,14 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   DevLaw L = c->devlaw();
   rc = launch_law_points(c, do_res, do_tan, L);
   if (rc) return rc;
-  const bool k_res = do_res, k_tan = fp64_tan;
+  // the residual of the tensor-core modes: double-FP32 kernel when its pair
+  // cache was built (linear law)
+  const bool df_res = do_res && c->prec != IGAPGPU_PREC_FP64 && c->d_rpc;
+  if (df_res) {
+    rc = launch_res_df(c, RR);
+    if (rc) return rc;
+  }
+  const bool k_res = do_res && !df_res, k_tan = fp64_tan;
   if (k_res || k_tan) {
     const bool do_res_k = k_res, do_tan_k = k_tan;
     {
@@ -1131,11 +1138,24 @@ __global__ void fp64_peak_kernel(double *out, int iters)
   }
   if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5) out[0] = 1.0;
 }
-}  // namespace igap
 
-extern "C" int igapgpu_measure_fp64_peak(double *tflops)
+__global__ void fp32_peak_kernel(double *out, int iters)
 {
-  using namespace igap;
+  float a0 = threadIdx.x * 1e-6f, a1 = a0 + 1e-6f, a2 = a0 + 2e-6f, a3 = a0 + 3e-6f;
+  float a4 = a0 + 4e-6f, a5 = a0 + 5e-6f, a6 = a0 + 6e-6f, a7 = a0 + 7e-6f;
+  const float b = 0.9999f, cc = 1e-7f;
+  for (int i = 0; i < iters; i++) {
+    a0 = fmaf(a0, b, cc); a1 = fmaf(a1, b, cc); a2 = fmaf(a2, b, cc); a3 = fmaf(a3, b, cc);
+    a4 = fmaf(a4, b, cc); a5 = fmaf(a5, b, cc); a6 = fmaf(a6, b, cc); a7 = fmaf(a7, b, cc);
+  }
+  if (a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7 == 1234.5f) out[0] = 1.0;
+}
+
+// FMA throughput of a register-only kernel (8 independent chains a thread,
+// 8 CTAs of 256 threads per SM), in TFLOP/s.
+template <typename K>
+static int measure_peak(K kern, int iters, double *tflops)
+{
   int dev = 0, nsm = 0;
   IGAP_CUDA(cudaGetDevice(&dev));
   IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1144,10 +1164,10 @@ extern "C" int igapgpu_measure_fp64_peak(double *tflops)
   cudaEvent_t e0, e1;
   IGAP_CUDA(cudaEventCreate(&e0));
   IGAP_CUDA(cudaEventCreate(&e1));
-  const int iters = 1 << 14, blocks = nsm * 8, threads = 256;
-  fp64_peak_kernel<<<blocks, threads>>>(d, 64);  // warm-up
+  const int blocks = nsm * 8, threads = 256;
+  kern<<<blocks, threads>>>(d, 64);  // warm-up
   IGAP_CUDA(cudaEventRecord(e0));
-  fp64_peak_kernel<<<blocks, threads>>>(d, iters);
+  kern<<<blocks, threads>>>(d, iters);
   IGAP_CUDA(cudaEventRecord(e1));
   count_launch(2);
   IGAP_CUDA(cudaEventSynchronize(e1));
@@ -1158,6 +1178,19 @@ extern "C" int igapgpu_measure_fp64_peak(double *tflops)
   cudaEventDestroy(e1);
   cudaFree(d);
   return IGAPGPU_OK;
+}
+}  // namespace igap
+
+extern "C" int igapgpu_measure_fp64_peak(double *tflops)
+{
+  if (!tflops) return IGAPGPU_ERR_ARG;
+  return igap::measure_peak(igap::fp64_peak_kernel, 1 << 14, tflops);
+}
+
+extern "C" int igapgpu_measure_fp32_peak(double *tflops)
+{
+  if (!tflops) return IGAPGPU_ERR_ARG;
+  return igap::measure_peak(igap::fp32_peak_kernel, 1 << 18, tflops);
 }
 
 // Runs wait_selftest_kernel on a zeroed counter: target 0 (satisfied at once)

@@ -156,6 +156,10 @@ struct Context {
   void *d_oz = nullptr;        // linear law: BF16 slices of the Gram operands (FP64-quality tensor-core tangent)
   void *d_ozexp = nullptr;     // their per-row power-of-two exponents (int8, 88 per element)
   int oz_state = -1;           // -1 not decided, 0 off, 1 on
+  float2 *d_rpc = nullptr;     // linear law: derivative and weight pairs per point (double-FP32 residual)
+  float2 *d_rel = nullptr;     // its per-element residual pairs [element][81]
+  float2 *d_upair = nullptr;   // the state as pairs [ndof]
+  int rpc_state = -1;          // -1 not decided, 0 off, 1 on
   double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
   double *d_preD = nullptr;
   int pre_state = -1;          // -1 not decided, 0 off, 1 on
@@ -284,6 +288,9 @@ int launch_assembly_p3(Context *c, bool do_res, bool do_tan, double *RR, double 
 // tc_ozaki.cu (linear law, BF16 slices, FP64-quality)
 int ensure_ozaki_operands(Context *c);
 int launch_tc_ozaki(Context *c, double *vals);
+// res_df.cu (linear law residual in double-FP32 arithmetic)
+int ensure_res_pairs(Context *c);
+int launch_res_df(Context *c, double *RR);
 // builds d_gop once (linear law, FP64 geometry cache present, memory allows)
 int ensure_gram_operands(Context *c);
 // krylov.cu

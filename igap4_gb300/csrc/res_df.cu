@@ -1,0 +1,315 @@
+// Residual of the linear strain-gradient law on the FP32 pipe in double-FP32
+// arithmetic (the split-precision and FP64-quality modes; the FP64 mode keeps
+// the FP64 element kernel).
+//
+// The residual is the reference's element loop (src/assmcore_iga.c:209-258:
+// interpolate the state's first and second derivatives at every Gauss
+// point, evaluate the law, project on every basis function) with the linear
+// law of laws.cuh (lingrad_residual_dev), element by element:
+//   u_dk(q) = sum_b N_bk(q) u_bd                 (k: 3 first, 6 second derivatives)
+//   rr_dk(q) = w_q (D u)_dk(q)                   (the law's stress slots)
+//   R_bd = sum_q sum_k N_bk(q) rr_dk(q)
+// On this GPU the FP64 pipe is the bottleneck of that loop (about 1/64 of the
+// FP32 rate), so every product and sum runs on float pairs (df32.cuh): the
+// derivatives N_bk and weights come from a pair cache built once from the
+// FP64 geometry cache, the state is split into pairs once per assembly, the
+// two contractions are compensated dot products (Dot2) and the law is pair
+// arithmetic.  Measured against the FP64 kernel: about 1e-14 relative.
+//
+// Layout and work split: one thread per Gauss point (a warp holds 32 points
+// of one element), the pair cache point-minor ([element][value][point]), so
+// that a warp's loads are contiguous; a point's projection partials are
+// summed over the element's points through shared memory; the element sums
+// go to a per-element buffer, and a gather kernel adds them per DOF in a fixed
+// order (deterministic, no atomics).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#include "common.cuh"
+#include "element.cuh"
+#include "df32.cuh"
+
+namespace igap {
+
+constexpr int RP_V = NB * 9 + 1;  // pair-cache values per point: 27 x 9 derivatives, weight
+constexpr int RD_THREADS = 128;
+
+struct DfLaw {
+  float2 lam, mu, l2;
+};
+
+// FP64 -> pair on the FP64 pipe (cache build and state split only)
+__device__ __forceinline__ float2 split_pair(double x)
+{
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+__global__ void res_pair_cache_kernel(const double *__restrict__ geo, int npts, int64_t nelem,
+                                      float2 *__restrict__ pc)
+{
+  const int64_t n = nelem * npts * RP_V;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(i % npts);
+    const int64_t t = i / npts;
+    const int v = (int)(t % RP_V);
+    const int64_t e = t / RP_V;
+    const double *g = geo + (e * npts + q) * GEO_STRIDE;
+    pc[i] = split_pair(v < NB * 9 ? g[NDD * (v / 9) + 1 + v % 9] : g[NB * NDD]);
+  }
+}
+
+__global__ void state_pair_kernel(const double *__restrict__ U, int64_t n, float2 *__restrict__ up)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    up[i] = split_pair(U[i]);
+}
+
+__device__ __forceinline__ constexpr int hs6(int i, int m)
+{
+  return i < m ? (i == 0 ? m : (i == 1 ? 2 + m : 5)) : (m == 0 ? i : (m == 1 ? 2 + i : 5));
+}
+
+__device__ __forceinline__ float2 twice(float2 a) { return make_float2(2.f * a.x, 2.f * a.y); }
+
+// The linear law of lingrad_residual_dev in pair arithmetic.  ud[9d + k]:
+// derivatives of displacement component d (k 0..2 gradient, 3..8 Hessian
+// xx, xy, xz, yy, yz, zz); rr[9d + k]: the weighted stress slots.
+__device__ __forceinline__ void lin_law_df(const float2 *ud, float2 wt, const DfLaw &L, float2 *rr)
+{
+  const float2 ldiv = df_mul(L.lam, df_add(df_add(ud[0], ud[9 + 1]), ud[18 + 2]));
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      float2 s = df_mul(L.mu, df_add(ud[9 * d + i], ud[9 * i + d]));
+      if (d == i) s = df_add(s, ldiv);
+      rr[9 * d + i] = df_mul(wt, s);
+    }
+  float2 Dm[3];  // derivatives of the divergence
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+    Dm[m] = df_add(df_add(ud[3 + hs6(0, m)], ud[9 + 3 + hs6(1, m)]), ud[18 + 3 + hs6(2, m)]);
+  const float2 wl2 = df_mul(wt, L.l2);
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int m = i; m < 3; m++) {
+        // slot (i, m): T_d[i][m] (+ T_d[m][i] off the diagonal), with
+        // T_d[i][m] = mu (H_d(i,m) + H_i(d,m)) + lam delta_di Dm[m]
+        float2 t;
+        if (i == m) {
+          t = df_mul(L.mu, df_add(ud[9 * d + 3 + hs6(i, i)], ud[9 * i + 3 + hs6(d, i)]));
+          if (d == i) t = df_add(t, df_mul(L.lam, Dm[i]));
+        } else {
+          const float2 h = df_add(twice(ud[9 * d + 3 + hs6(i, m)]),
+                                  df_add(ud[9 * i + 3 + hs6(d, m)], ud[9 * m + 3 + hs6(d, i)]));
+          t = df_mul(L.mu, h);
+          if (d == i) t = df_add(t, df_mul(L.lam, Dm[m]));
+          if (d == m) t = df_add(t, df_mul(L.lam, Dm[i]));
+        }
+        rr[9 * d + 3 + hs6(i, m)] = df_mul(wl2, t);
+      }
+}
+
+// NW warps per element (npts <= 32 NW), RD_THREADS / (32 NW) elements per CTA.
+// rel[e][3b + d]: the element's residual pairs.
+template <int NW>
+__global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__restrict__ pc,
+                                                            const float2 *__restrict__ up, int npts,
+                                                            int64_t nelem, int ne1, int ne2, int nb1, int nb2,
+                                                            DfLaw L, float2 *__restrict__ rel)
+{
+  constexpr int NWARP = RD_THREADS / 32, EPB = NWARP / NW;
+  __shared__ float2 su[EPB][NE];
+  __shared__ float2 red[NWARP][32][27];
+  __shared__ float2 part[EPB][NW][NE];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int le = warp / NW, wq = warp % NW;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  for (int t = tid; t < EPB * NE; t += RD_THREADS) {
+    const int l = t / NE, i = t % NE, b = i / 3, d = i % 3;
+    const int64_t ee = e0 + l;
+    float2 v = make_float2(0.f, 0.f);
+    if (ee < nelem) {
+      const int ez = (int)(ee % ne2), ey = (int)((ee / ne2) % ne1);
+      const int64_t ex = ee / ((int64_t)ne1 * ne2);
+      const int64_t cp = ((ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+      v = __ldg(up + 3 * cp + d);
+    }
+    su[l][i] = v;
+  }
+  __syncthreads();
+  const int64_t e = e0 + le;
+  const int q = 32 * wq + lane;
+  const bool act = e < nelem && q < npts;
+  const float2 *p = pc + (act ? ((e * RP_V) * npts + q) : 0);
+  float2 rr[27];
+  {
+    float s[27], c[27];
+#pragma unroll
+    for (int i = 0; i < 27; i++) s[i] = c[i] = 0.f;
+    float2 wt = make_float2(0.f, 0.f);
+    if (act) {
+#pragma unroll 1
+      for (int b = 0; b < NB; b++) {
+        float2 n[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) n[k] = __ldg(p + (size_t)(9 * b + k) * npts);
+        const float2 u0 = su[le][3 * b], u1 = su[le][3 * b + 1], u2 = su[le][3 * b + 2];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+          dot2(s[k], c[k], n[k], u0);
+          dot2(s[9 + k], c[9 + k], n[k], u1);
+          dot2(s[18 + k], c[18 + k], n[k], u2);
+        }
+      }
+      wt = __ldg(p + (size_t)(NB * 9) * npts);
+    }
+    float2 ud[27];
+#pragma unroll
+    for (int i = 0; i < 27; i++) ud[i] = dot2_pair(s[i], c[i]);
+    lin_law_df(ud, wt, L, rr);
+  }
+  // projection: block j of 9 basis functions at a time, summed over the
+  // warp's points through red[warp]
+#pragma unroll 1
+  for (int j = 0; j < 3; j++) {
+#pragma unroll 1
+    for (int bb = 0; bb < 9; bb++) {
+      const int b = 9 * j + bb;
+      float2 n[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) n[k] = act ? __ldg(p + (size_t)(9 * b + k) * npts) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        float s = 0.f, c = 0.f;
+#pragma unroll
+        for (int k = 0; k < 9; k++) dot2(s, c, n[k], rr[9 * d + k]);
+        red[warp][lane][3 * bb + d] = dot2_pair(s, c);
+      }
+    }
+    __syncwarp();
+    if (lane < 27) {
+      float2 t = red[warp][0][lane];
+#pragma unroll 4
+      for (int l = 1; l < 32; l++) t = df_add(t, red[warp][l][lane]);
+      part[le][wq][27 * j + lane] = t;
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int t = tid; t < EPB * NE; t += RD_THREADS) {
+    const int l = t / NE, i = t % NE;
+    if (e0 + l >= nelem) continue;
+    float2 v = part[l][0][i];
+#pragma unroll
+    for (int w = 1; w < NW; w++) v = df_add(v, part[l][w][i]);
+    rel[(e0 + l) * NE + i] = v;
+  }
+}
+
+// RR[dof] += the sum of its elements' residual pairs, elements in a fixed order.
+__global__ void res_gather_kernel(const float2 *__restrict__ rel, int ne0, int ne1, int ne2, int nb0, int nb1,
+                                  int nb2, double *__restrict__ RR)
+{
+  const int64_t ndof = 3 * (int64_t)nb0 * nb1 * nb2;
+  for (int64_t dof = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; dof < ndof;
+       dof += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cp = dof / 3;
+    const int d = (int)(dof % 3);
+    const int iz = (int)(cp % nb2), iy = (int)((cp / nb2) % nb1), ix = (int)(cp / ((int64_t)nb1 * nb2));
+    float2 s = make_float2(0.f, 0.f);
+    for (int ex = max(ix - P, 0); ex <= min(ix, ne0 - 1); ex++)
+      for (int ey = max(iy - P, 0); ey <= min(iy, ne1 - 1); ey++)
+        for (int ez = max(iz - P, 0); ez <= min(iz, ne2 - 1); ez++) {
+          const int64_t el = ((int64_t)ex * ne1 + ey) * ne2 + ez;
+          const int b = (ix - ex) * 9 + (iy - ey) * 3 + (iz - ez);
+          s = df_add(s, __ldg(rel + el * NE + 3 * b + d));
+        }
+    RR[dof] += (double)s.x + (double)s.y;
+  }
+}
+
+static float2 host_pair(double x)
+{
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+
+// Builds the pair cache once (linear law, quadratic, single lattice, FP64
+// geometry cache present, memory allows; IGAPGPU_RES_DF=0 turns it off).
+int ensure_res_pairs(Context *c)
+{
+  if (c->rpc_state >= 0) return IGAPGPU_OK;
+  c->rpc_state = 0;
+  const char *env = getenv("IGAPGPU_RES_DF");
+  if (env && env[0] == '0') return IGAPGPU_OK;
+  if (c->law != IGAPGPU_LAW_LINGRAD || !c->d_geo || c->batch || c->porder != 2) return IGAPGPU_OK;
+  const int npts = c->nquad * c->nquad * c->nquad;
+  if (npts > 64) return IGAPGPU_OK;
+  const size_t bytes = (size_t)c->nelem_total * npts * RP_V * sizeof(float2);
+  const size_t rbytes = (size_t)c->nelem_total * NE * sizeof(float2);
+  const size_t ubytes = (size_t)c->ndof * sizeof(float2);
+  size_t freeb = 0, totb = 0;
+  IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
+  if (bytes + rbytes + ubytes + ((size_t)4 << 30) > freeb) return IGAPGPU_OK;
+  if (cudaMalloc(&c->d_rpc, bytes) != cudaSuccess || cudaMalloc(&c->d_rel, rbytes) != cudaSuccess ||
+      cudaMalloc(&c->d_upair, ubytes) != cudaSuccess) {
+    cudaGetLastError();
+    if (c->d_rpc) cudaFree(c->d_rpc);
+    if (c->d_rel) cudaFree(c->d_rel);
+    if (c->d_upair) cudaFree(c->d_upair);
+    c->d_rpc = c->d_rel = c->d_upair = nullptr;
+    return IGAPGPU_OK;
+  }
+  res_pair_cache_kernel<<<152 * 16, 256, 0, c->stream>>>(c->d_geo, npts, c->nelem_total, c->d_rpc);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  c->rpc_state = 1;
+  return IGAPGPU_OK;
+}
+
+// RR += element residuals of the linear law from the pair cache.
+int launch_res_df(Context *c, double *RR)
+{
+  const int npts = c->nquad * c->nquad * c->nquad;
+  const DfLaw L = {host_pair(c->par[0]), host_pair(c->par[1]), host_pair(c->par[2] * c->par[2])};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+  }
+  state_pair_kernel<<<152 * 4, 256, 0, c->stream>>>(c->d_Uhist, c->ndof, c->d_upair);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  if (c->prof) IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  const int64_t ne = c->nelem_total;
+  if (npts <= 32) {
+    constexpr int EPB = RD_THREADS / 32;
+    res_df_kernel<1><<<(unsigned)((ne + EPB - 1) / EPB), RD_THREADS, 0, c->stream>>>(
+        c->d_rpc, c->d_upair, npts, ne, c->nelem[1], c->nelem[2], c->nbasis[1], c->nbasis[2], L, c->d_rel);
+  } else {
+    constexpr int EPB = RD_THREADS / 64;
+    res_df_kernel<2><<<(unsigned)((ne + EPB - 1) / EPB), RD_THREADS, 0, c->stream>>>(
+        c->d_rpc, c->d_upair, npts, ne, c->nelem[1], c->nelem[2], c->nbasis[1], c->nbasis[2], L, c->d_rel);
+  }
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[0].emplace_back(e0, e1);
+    c->prof_launches[0]++;
+    c->prof_elements[0] += ne;
+  }
+  res_gather_kernel<<<152 * 4, 256, 0, c->stream>>>(c->d_rel, c->nelem[0], c->nelem[1], c->nelem[2],
+                                                   c->nbasis[0], c->nbasis[1], c->nbasis[2], RR);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+}  // namespace igap

@@ -48,26 +48,15 @@
 
 #include "common.cuh"
 #include "element.cuh"
+#include "df32.cuh"
 #include "gram_common.cuh"
 #include "tcgen05.cuh"
 
 namespace igap {
 
 namespace {
-// Error-free transformations on the FP32 pipe (Knuth's two-sum; the
-// fused-multiply-add two-product): s + e == a + b and p + e == a * b exactly.
-__device__ __forceinline__ float two_sum(float a, float b, float &e)
-{
-  const float s = __fadd_rn(a, b), bv = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
-  return s;
-}
-__device__ __forceinline__ float two_prod(float a, float b, float &e)
-{
-  const float p = __fmul_rn(a, b);
-  e = __fmaf_rn(a, b, -p);
-  return p;
-}
+// (two_sum, two_prod: the error-free transformations of df32.cuh,
+// s + e == a + b and p + e == a * b exactly)
 // 2^k as a float (k in the normal range)
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
 

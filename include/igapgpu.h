@@ -276,6 +276,9 @@ int igapgpu_tc_selftest(int variant, float *out);
 /* Measured FP64 FMA throughput of this GPU (TFLOP/s) from a register-only
  * kernel; used as the denominator of FP64-bound roofline fractions. */
 int igapgpu_measure_fp64_peak(double *tflops);
+/* The same for FP32 FMA (TFLOP/s, an FMA counted as 2): the denominator of the
+ * double-FP32 residual kernel's roofline. */
+int igapgpu_measure_fp32_peak(double *tflops);
 /* Failure-detection self-test (no counterpart in the reference): a kernel
  * waits, with the bounded acquire-poll loop of the batched kernels, for a
  * zeroed counter to reach `target` (0: at once; 1: never, so the wait expires

@@ -68,6 +68,10 @@ def test_batch_bit_identical_to_single_instances(law, cached, prec, monkeypatch)
     # single instances here (their all-points law launch is compared with this
     # in test_gpu_assembly.py: identical in FP64, within the split bound in split)
     monkeypatch.setenv("IGAPGPU_LAW_PRECOMPUTE", "0")
+    # batches keep the FP64 residual kernel in split mode; so do the single
+    # instances here (their double-FP32 residual is compared with FP64 in
+    # test_gpu_split.py)
+    monkeypatch.setenv("IGAPGPU_RES_DF", "0")
     # linear law, split: Gram operands cached (sqrt(w) folded in) or built in the kernel
     monkeypatch.setenv("IGAPGPU_TC_GRAM_CACHE", cached)
     insts = instances(law, seed=3)

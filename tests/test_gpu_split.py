@@ -6,7 +6,10 @@
   FP32 tensor-memory accumulation dominates), for all three laws and every GEMM form
   of the linear law (Gram form from cached sqrt(w)-weighted operands, Gram form built
   from the FP32 geometry cache, and the two-stage form used by the other laws);
-* the residual of the split mode is the FP64 residual, unchanged.
+* the residual of the split mode is the FP64 residual, unchanged, for the
+  reference's laws; the linear law's residual runs in double-FP32 arithmetic
+  (pairs of floats, compensated dot products) within 1e-12 of the FP64
+  residual (measured ~1e-15) and of the CPU oracle.
 """
 import numpy as np
 import pytest
@@ -17,6 +20,7 @@ import pyoracle as po
 pytestmark = pytest.mark.gpu
 
 SPLIT_TOL = 1e-5
+DF_TOL = 1e-12  # double-FP32 residual of the linear law vs FP64
 
 
 def rel(a, b):
@@ -51,19 +55,27 @@ def test_split_tangent_vs_fp64(law, nelem, perturb, form, monkeypatch):
     R64 = A.residual()
     n0 = ig.launch_count()
     A.set_precision(ig.PREC_SPLIT)
-    # the cached form builds its operands once, in one launch, when split precision is set
-    assert ig.launch_count() - n0 == (1 if law == po.LAW_LINGRAD and form != "gram" else 0)
+    # the cached form builds its operands once, in one launch, when split
+    # precision is set; the linear law's residual pairs in one more
+    lin = law == po.LAW_LINGRAD
+    assert ig.launch_count() - n0 == (1 if lin and form != "gram" else 0) + (1 if lin else 0)
     Ks = A.tangent()
     Rs = A.residual()
     e = rel(Ks, K64)
     print(f"split tangent rel err {e:.3e}")
     assert e <= SPLIT_TOL
-    np.testing.assert_array_equal(Rs, R64)
-    # fused assemble in split mode = FP64 residual + split tangent
+    if lin:
+        er = rel(Rs, R64)
+        print(f"double-FP32 residual rel err {er:.3e}")
+        assert er <= DF_TOL
+        np.testing.assert_array_equal(A.residual(), Rs)  # deterministic
+    else:
+        np.testing.assert_array_equal(Rs, R64)
+    # fused assemble in split mode = the residual above + split tangent
     RR = np.zeros(A.ndof)
     V = np.zeros(A.nnz)
     A.assemble(None, RR, V)
-    np.testing.assert_array_equal(RR, R64)
+    np.testing.assert_array_equal(RR, Rs)
     assert rel(V, K64) <= SPLIT_TOL
 
 
@@ -146,10 +158,14 @@ def test_split_and_fp64_vs_cpu_oracle(law, nelem):
     A.set_state(U)
     R64, K64 = A.residual(), A.tangent()
     A.set_precision(ig.PREC_SPLIT)
-    Ks = A.tangent()
+    Ks, Rs = A.tangent(), A.residual()
     orc = po.OracleCase(prob)
     rowptr, _ = orc.pattern()
-    assert rel(R64, orc.residual(U)) <= 1e-12
+    Ro = orc.residual(U)
+    assert rel(R64, Ro) <= 1e-12
+    ers = rel(Rs, Ro)
+    print(f"law {law} {nelem}: split-mode residual {ers:.2e} vs the CPU oracle")
+    assert ers <= (DF_TOL if law == po.LAW_LINGRAD else 1e-12)
     ix = nelem[0] // 2 + 1
     rows, e0, e1 = slab_rows(prob, ix)
     Ko = rows_of(orc.tangent_elements(U, e0, e1), rowptr, rows)
@@ -175,7 +191,7 @@ def test_tcgen05_selftest_bf16_exact():
 def test_ozaki_tangent_vs_fp64(nelem, perturb, nquad):
     """Tangent from error-free BF16 slices of the Gram operands (one
     power-of-two scale per row, exact leading product): within 1e-9 of the
-    FP64 tangent; the residual is the FP64 residual, bit for bit."""
+    FP64 tangent; the residual (double-FP32) within 1e-12 of the FP64 one."""
     bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0), 2, perturb)
     A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct, neumann=neu,
@@ -184,18 +200,48 @@ def test_ozaki_tangent_vs_fp64(nelem, perturb, nquad):
     K64, R64 = A.tangent(U.copy()), A.residual(U.copy())
     n0 = ig.launch_count()
     A.set_precision(ig.PREC_OZAKI)
-    assert ig.launch_count() - n0 == 1  # the slices are built once, in one launch
+    assert ig.launch_count() - n0 == 2  # slices and residual pairs are built once, one launch each
     Ko, Ro = A.tangent(U.copy()), A.residual(U.copy())
     e = rel(Ko, K64)
-    print(f"FP64-quality tensor-core tangent rel err {e:.3e}")
+    er = rel(Ro, R64)
+    print(f"FP64-quality tensor-core tangent rel err {e:.3e}, residual {er:.3e}")
     assert e <= OZAKI_TOL
-    np.testing.assert_array_equal(Ro, R64)
+    assert er <= DF_TOL
     RR, V = np.zeros(A.ndof), np.zeros(A.nnz)
     A.assemble(U.copy(), RR, V)
-    np.testing.assert_array_equal(RR, R64)
+    np.testing.assert_array_equal(RR, Ro)
     assert rel(V, K64) <= OZAKI_TOL
     # twice in a row: the same values (the slices are state independent)
     np.testing.assert_array_equal(A.tangent(U.copy()), Ko)
+
+
+@pytest.mark.parametrize("nquad", [4, 3])
+def test_df_residual_switch_and_large_state(nquad, monkeypatch):
+    """IGAPGPU_RES_DF=0 keeps the FP64 residual kernel in the tensor-core
+    modes (bit-identical to FP64 mode); with it on, the double-FP32 residual
+    stays within 1e-12 of FP64 for a state with a large rigid translation (the
+    interpolation's terms cancel) and for a state near 1e3."""
+    nelem = (6, 3, 3)
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0), 2, True)
+    rng = np.random.default_rng(11)
+    mk = lambda: ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct,
+                             neumann=neu, nquad=nquad)
+    A = mk()
+    n = A.ndof
+    states = [rng.uniform(-1e-2, 1e-2, n), 5.0 + rng.uniform(-1e-3, 1e-3, n), rng.uniform(-1e3, 1e3, n)]
+    R64 = [A.residual(U.copy()) for U in states]
+    monkeypatch.setenv("IGAPGPU_RES_DF", "0")
+    B = mk()
+    B.set_precision(ig.PREC_SPLIT)
+    for U, R in zip(states, R64):
+        np.testing.assert_array_equal(B.residual(U.copy()), R)
+    monkeypatch.delenv("IGAPGPU_RES_DF")
+    A.set_precision(ig.PREC_OZAKI)
+    for U, R in zip(states, R64):
+        er = rel(A.residual(U.copy()), R)
+        print(f"nquad {nquad}: double-FP32 residual rel err {er:.3e}")
+        assert er <= DF_TOL
 
 
 def test_ozaki_vs_cpu_oracle_sweep_mesh():
