@@ -115,8 +115,34 @@ __device__ __forceinline__ void lin_law_df(const float2 *ud, float2 wt, const Df
       }
 }
 
+// Loads of the pair cache with an L2 eviction-priority hint: the
+// interpolation pass marks its lines evict-last (the projection pass reads
+// them again), the projection pass evict-first.
+__device__ __forceinline__ uint64_t l2_policy_last()
+{
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first()
+{
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float2 ld_pair(const float2 *p, uint64_t pol)
+{
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+
 // NW warps per element (npts <= 32 NW), RD_THREADS / (32 NW) elements per CTA.
-// rel[e][3b + d]: the element's residual pairs.
+// rel[e][3b + d]: the element's residual pairs.  The interpolation loads the
+// next basis function's derivatives ahead; the projection visits the basis
+// functions in the reverse order of the interpolation, so that the lines read
+// last are read again first (with the eviction hints, 7.9 -> 6.8 ms per
+// residual at 128x32x32; fewer CTAs per SM for more L2 reuse measured slower).
 template <int NW>
 __global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__restrict__ pc,
                                                             const float2 *__restrict__ up, int npts,
@@ -147,6 +173,7 @@ __global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__rest
   const int q = 32 * wq + lane;
   const bool act = e < nelem && q < npts;
   const float2 *p = pc + (act ? ((e * RP_V) * npts + q) : 0);
+  const uint64_t pol1 = l2_policy_last(), pol2 = l2_policy_first();
   float2 rr[27];
   {
     float s[27], c[27];
@@ -154,11 +181,15 @@ __global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__rest
     for (int i = 0; i < 27; i++) s[i] = c[i] = 0.f;
     float2 wt = make_float2(0.f, 0.f);
     if (act) {
+      float2 n[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) n[k] = ld_pair(p + (size_t)k * npts, pol1);
 #pragma unroll 1
       for (int b = 0; b < NB; b++) {
-        float2 n[9];
+        float2 nn[9];  // the next basis function's derivatives, loaded ahead
+        const int bn = b + 1 < NB ? b + 1 : b;
 #pragma unroll
-        for (int k = 0; k < 9; k++) n[k] = __ldg(p + (size_t)(9 * b + k) * npts);
+        for (int k = 0; k < 9; k++) nn[k] = ld_pair(p + (size_t)(9 * bn + k) * npts, pol1);
         const float2 u0 = su[le][3 * b], u1 = su[le][3 * b + 1], u2 = su[le][3 * b + 2];
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -166,6 +197,8 @@ __global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__rest
           dot2(s[9 + k], c[9 + k], n[k], u1);
           dot2(s[18 + k], c[18 + k], n[k], u2);
         }
+#pragma unroll
+        for (int k = 0; k < 9; k++) n[k] = nn[k];
       }
       wt = __ldg(p + (size_t)(NB * 9) * npts);
     }
@@ -177,13 +210,16 @@ __global__ void __launch_bounds__(RD_THREADS) res_df_kernel(const float2 *__rest
   // projection: block j of 9 basis functions at a time, summed over the
   // warp's points through red[warp]
 #pragma unroll 1
-  for (int j = 0; j < 3; j++) {
+  for (int jj = 0; jj < 3; jj++) {
+    const int j = 2 - jj;
 #pragma unroll 1
-    for (int bb = 0; bb < 9; bb++) {
+    for (int bi = 0; bi < 9; bi++) {
+      const int bb = 8 - bi;
       const int b = 9 * j + bb;
       float2 n[9];
 #pragma unroll
-      for (int k = 0; k < 9; k++) n[k] = act ? __ldg(p + (size_t)(9 * b + k) * npts) : make_float2(0.f, 0.f);
+      for (int k = 0; k < 9; k++)
+        n[k] = act ? ld_pair(p + (size_t)(9 * b + k) * npts, pol2) : make_float2(0.f, 0.f);
 #pragma unroll
       for (int d = 0; d < 3; d++) {
         float s = 0.f, c = 0.f;

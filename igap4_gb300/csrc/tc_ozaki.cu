@@ -17,16 +17,18 @@
 // the tensor core rounds its sums; acc2 = the products with i + j = 4 and
 // acc3 those with i + j = 5, 6, each rounded at its own scale (2^-16 and
 // 2^-24 of the leading term).  Products with i + j >= 7 are left out.  The
-// epilogue stages X and forms G = (acc0 + t) + (e + acc2 + acc3) in FP64,
-// t + e = X + X^T exactly (FP32 two-sum), the power of two applied on the
-// integer pipe.  A model of the scheme on random operands with this row
+// epilogue stages X and forms G = 2^sh ((acc0 + t) + (e + acc2 + acc3)) as an
+// unevaluated FP32 pair, t + e = X + X^T exactly (two-sum), the power of two
+// exact in FP32.  A model of the scheme on random operands with this row
 // scaling gives 2e-10 relative Frobenius error whether the tensor core
 // rounds its sums to nearest or towards zero (one accumulator for i + j >= 4
 // and an FP32 X + X^T: 1e-9 towards zero; stopping at i + j = 5: 1e-8).
-// K = lam G + mu (G^T + tr G I) per 3 x 3 block in FP64
-// and adds it into the FP64 CSR values with L2 reductions (colour order, as
-// every other tangent kernel here).  Relative error of the tangent: about
-// 2^-32 of the entries' natural scale (~1e-10), against the 2e-6 of TF32x3.
+// K = lam G + mu (G^T + tr G I) per 3 x 3 block on the FP32 pipe with
+// error-free products and sums (lam, mu as FP32 pairs), one FP64 add per
+// entry joining the pair, added into the FP64 CSR values with L2 reductions
+// (colour order, as every other tangent kernel here).  Relative error of the
+// tangent: about 2^-32 of the entries' natural scale (~1e-10), against the
+// 2e-6 of TF32x3.
 //
 // One persistent CTA per SM (four accumulators of 96 columns fill the tensor
 // memory, so they are single buffered and drained into shared memory right
@@ -37,7 +39,7 @@
 //     into four accumulators
 //     straight from the stage (the slices are built once, already in the
 //     operand layout; the same tile is A and B),
-//   warps 4-7: drain TMEM -> G (FP64, shared memory), free the accumulators;
+//   warps 4-7: drain TMEM -> G (FP32 pairs, shared memory), free the accumulators;
 //   warps 2-7: form K and scatter it.
 // Every mbarrier wait is bounded; a CTA that gives up waits (bounded) for
 // its copies and MMAs in flight and frees its tensor memory.
@@ -500,6 +502,14 @@ int launch_tc_ozaki(Context *c, double *vals)
   int dev = 0, nsm = 0;
   IGAP_CUDA(cudaGetDevice(&dev));
   IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // IGAPGPU_TCO_GRID caps the persistent grid (profiling: many elements per
+  // CTA on a small mesh show the steady state of one SM)
+  static int grid_cap = -1;
+  if (grid_cap < 0) {
+    const char *g = getenv("IGAPGPU_TCO_GRID");
+    grid_cap = g ? atoi(g) : 0;
+  }
+  const int cap = grid_cap > 0 && grid_cap < nsm ? grid_cap : nsm;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->prof) {
     IGAP_CUDA(cudaEventCreate(&e0));
@@ -513,7 +523,7 @@ int launch_tc_ozaki(Context *c, double *vals)
                   ncz = (c->nelem[2] - cz + 2) / 3;
         const int nel = ncx * ncy * ncz;
         if (nel <= 0) continue;
-        const int grid = nel < nsm ? nel : nsm;
+        const int grid = nel < cap ? nel : cap;
         tco_kernel<<<grid, OZ_THREADS, smem, c->stream>>>(m, L, cx, cy, cz, ncx, ncy, ncz, vals, c->d_err,
                                                           (const unsigned char *)c->d_oz,
                                                           (const signed char *)c->d_ozexp);
