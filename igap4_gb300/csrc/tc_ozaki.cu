@@ -39,8 +39,14 @@
 //     into four accumulators
 //     straight from the stage (the slices are built once, already in the
 //     operand layout; the same tile is A and B),
-//   warps 4-7: drain TMEM -> G (FP32 pairs, shared memory), free the accumulators;
-//   warps 2-7: form K and scatter it.
+//   warps 4-7: copy the accumulators from TMEM to shared memory (X, and acc0
+//     with acc2 + acc3 per entry) and free them for the next element;
+//   warps 2-11: a thread per basis pair b <= c forms its 3 x 3 block of G and
+//     of K (K is symmetric) and adds it at (b, c) and, transposed, at (c, b).
+// Measured at 128x32x32: 15.8 ms per tangent with 6 epilogue warps forming
+// all 81 x 81 entries through staged G and trace arrays, 11.4 ms with 10
+// warps and the symmetric blocks (staged G and trace), 8.6 ms with a thread per
+// basis pair forming its block of G, the trace and K in registers.
 // Every mbarrier wait is bounded; a CTA that gives up waits (bounded) for
 // its copies and MMAs in flight and frees its tensor memory.
 #include <cuda_runtime.h>
@@ -62,7 +68,8 @@ namespace {
 // 2^k as a float (k in the normal range)
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
 
-constexpr int OZ_THREADS = 256;
+constexpr int OZ_THREADS = 384;
+constexpr int OZ_EPI = OZ_THREADS - 64;                 // epilogue threads: warps 2..11
 constexpr int OZ_ROWS = 81;
 constexpr int OZ_RG = 11;                               // row groups holding rows 0..87
 constexpr int OZ_KS_BYTES = OZ_RG * 256;                // 2816: one K-step of 16 BF16 values
@@ -70,8 +77,9 @@ constexpr int OZ_SLICE_BYTES = 2 * OZ_KS_BYTES;         // 5632: a chunk of 8 po
 constexpr int OZ_CH_BYTES = 4 * OZ_SLICE_BYTES;         // 22528: the four slices of a chunk
 constexpr int OZ_STAGE = OZ_CH_BYTES + 5 * 256;         // an M = 128 read of the last K-step stays inside
 constexpr int OZ_NS = 5;                                // copy stages
-constexpr int OZ_GP = 82;                               // row stride (doubles) of the staged G
-constexpr int OZ_XP = 84;                               // row stride (floats) of the staged X
+constexpr int OZ_GP = 83;                               // row stride (float2) of the raw accumulators
+constexpr int OZ_XP = 85;                               // row stride (floats, odd) of the staged X
+constexpr int OZ_NPAIR = NB * (NB + 1) / 2;             // 378 basis pairs b <= c
 constexpr int OZ_EXP = 88;                              // exponent bytes per element
 constexpr uint32_t OZ_TMEM_COLS = 512;
 constexpr uint32_t OZ_WAIT_LIMIT = 1u << 26;
@@ -79,10 +87,10 @@ static_assert(OZ_STAGE % 16 == 0 && OZ_CH_BYTES % 16 == 0, "bulk copies and desc
 
 struct OzSmem {
   unsigned char stage[OZ_NS][OZ_STAGE];
-  float2 G[OZ_ROWS * OZ_GP];            // G as an unevaluated pair (x + y, |y| << |x|)
-  float2 T[NB * NB];                    // mu * trace of each 3 x 3 block of G, likewise
-  float X[OZ_ROWS * OZ_XP];
+  float2 G[OZ_ROWS * OZ_GP];            // raw accumulators (acc0, acc2 + acc3) per entry
+  float X[OZ_ROWS * OZ_XP];             // acc1 = D1 D2'^T (its transpose is needed)
   unsigned char pos[NB * NB];
+  unsigned char pb[OZ_NPAIR], pc[OZ_NPAIR];  // the pairs b <= c
   int64_t rowp[NE];
   int ex[OZ_EXP];
   uint64_t full[OZ_NS], empty[OZ_NS], accfull, accempty;
@@ -201,6 +209,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     tc::tmem_alloc(&S.taddr, OZ_TMEM_COLS);
     tc::tmem_relinquish();
   }
+  for (int b = tid; b < NB; b += OZ_THREADS) {  // pair table: row b's pairs (b, c >= b)
+    const int off = b * NB - b * (b - 1) / 2;
+    for (int c = b; c < NB; c++) {
+      S.pb[off + c - b] = (unsigned char)b;
+      S.pc[off + c - b] = (unsigned char)c;
+    }
+  }
   if (tid == 0) {
     for (int i = 0; i < OZ_NS; i++) {
       tc::mbar_init(&S.full[i], 1);
@@ -298,10 +313,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       S.accf_n = accn;
     }
   } else if (warp >= 2) {
-    // epilogue, warps 2-7 (192 threads); warps 4-7 also drain the tensor
-    // memory (warp & 3 is their lane quarter)
+    // epilogue, warps 2-11 (320 threads); warps 4-7 also drain the tensor
+    // memory (warp & 3 is their lane quarter).  K is symmetric, so only the
+    // 3 x 3 blocks of the basis pairs b <= c are formed; each is added at
+    // (b, c) and, transposed, at (c, b).
     const int t = tid - 64, quarter = warp & 3;
-    const bool drain = warp >= 4;
+    const bool drain = warp >= 4 && warp < 8;
     const int nb1 = m.nbasis[1], nb2 = m.nbasis[2];
     const int nbv[3] = {m.nbasis[0], nb1, nb2};
     // lam and mu as FP32 pairs (hi + lo = the double to 48 bits)
@@ -317,19 +334,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         S.rowp[t] = __ldg(m.rowptr + 3 * cpb + dd);
       }
       if (t < OZ_EXP) S.ex[t] = (int)__ldg(expo + eg * OZ_EXP + t);
-      for (int i = t; i < NB * NB; i += 192) {
+      for (int i = t; i < NB * NB; i += OZ_EPI) {
         const int b = i / NB, c = i % NB;
         S.pos[i] = (unsigned char)stencil_pos(ex + b / 9, ey + (b / 3) % 3, ez + b % 3, ex + c / 9,
                                               ey + (c / 3) % 3, ez + c % 3, nbv);
       }
-      // the six warps take the same decision (a named-barrier OR): only the
+      // the ten warps take the same decision (a named-barrier OR): only the
       // draining warps wait for the accumulators
       const uint32_t got = (!drain || oz_wait(&S.accfull, (uint32_t)j & 1, abort)) ? 1u : 0u;
       uint32_t any_failed;
       asm volatile(
           "{\n\t.reg .pred p, q;\n\t"
           "setp.eq.u32 p, %1, 0;\n\t"
-          "bar.red.or.pred q, 1, 192, p;\n\t"
+          "bar.red.or.pred q, 1, 320, p;\n\t"
           "selp.u32 %0, 1, 0, q;\n\t}\n"
           : "=r"(any_failed)
           : "r"(got)
@@ -338,11 +355,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         ok = false;
         break;
       }
-      if (drain) {
+      if (drain && quarter < 3) {  // rows 96..127 are padding
+        // raw copy of the accumulators, so that the next element's MMAs may
+        // start: X = acc1, and (acc0, acc2 + acc3) per entry
         tc::fence_after_sync();
         const int r = quarter * 32 + lane;
         const uint32_t rowb = (uint32_t)(quarter * 32) << 16;
-        for (int cb = 0; cb < 3; cb++) {  // X = acc1 to shared memory (its transpose is needed)
+        for (int cb = 0; cb < 3; cb++) {
           uint32_t v1[32];
           tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(128 + cb * 32), v1);
           if (r < OZ_ROWS)
@@ -350,71 +369,84 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             for (int jj = 0; jj < 32; jj++)
               if (cb * 32 + jj < OZ_ROWS) S.X[r * OZ_XP + cb * 32 + jj] = __uint_as_float(v1[jj]);
         }
-        asm volatile("bar.sync 2, 128;" ::: "memory");  // X complete
         for (int cb = 0; cb < 3; cb++) {
           uint32_t v0[32], v2[32], v3[32];
           tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(cb * 32), v0);
           tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(256 + cb * 32), v2);
           tc::tmem_ld_32x32b_x32(taddr + rowb + (uint32_t)(384 + cb * 32), v3);
-          if (r < OZ_ROWS) {
-            const int er = S.ex[r] - 16;
+          if (r < OZ_ROWS)
 #pragma unroll
-            for (int jj = 0; jj < 32; jj++) {
-              const int c = cb * 32 + jj;
-              if (c < OZ_ROWS) {
-                // G = 2^sh (acc0 + X + X^T + acc2 + acc3) as a pair: acc0 and X + X^T
-                // exactly (two-sum), the small terms rounded once; the power of
-                // two is exact in FP32 (|sh| < 100)
-                const float sc = pow2f(er + S.ex[c]);
-                float e, err;
-                const float tt = two_sum(S.X[r * OZ_XP + c], S.X[c * OZ_XP + r], e);
-                const float small = __fadd_rn(e, __fadd_rn(__uint_as_float(v2[jj]), __uint_as_float(v3[jj])));
-                const float s = two_sum(__fmul_rn(__uint_as_float(v0[jj]), sc), __fmul_rn(tt, sc), err);
-                S.G[r * OZ_GP + c] = make_float2(s, __fadd_rn(err, __fmul_rn(small, sc)));
-              }
-            }
-          }
+            for (int jj = 0; jj < 32; jj++)
+              if (cb * 32 + jj < OZ_ROWS)
+                S.G[r * OZ_GP + cb * 32 + jj] =
+                    make_float2(__uint_as_float(v0[jj]), __fadd_rn(__uint_as_float(v2[jj]), __uint_as_float(v3[jj])));
         }
+      }
+      if (drain) {
         tc::fence_before_sync();
         mbar_arrive1(&S.accempty);  // the next element's MMAs may overwrite the accumulators
       }
-      asm volatile("bar.sync 1, 192;" ::: "memory");  // G, rowp, pos of the element complete
-      for (int u = t; u < NB * NB; u += 192) {  // mu tr G_bc, as a pair
-        const int b = u / NB, c = u % NB;
-        const float2 g0 = S.G[(3 * b) * OZ_GP + 3 * c], g1 = S.G[(3 * b + 1) * OZ_GP + 3 * c + 1],
-                     g2 = S.G[(3 * b + 2) * OZ_GP + 3 * c + 2];
-        float e0, e1, q;
-        const float a = two_sum(g0.x, g1.x, e0);
-        const float s = two_sum(a, g2.x, e1);
-        const float low = __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(__fadd_rn(g0.y, g1.y), g2.y));
-        const float th = two_prod(muh, s, q);
-        S.T[u] = make_float2(th, __fadd_rn(q, __fadd_rn(__fmul_rn(muh, low), __fmul_rn(mul, s))));
-      }
-      asm volatile("bar.sync 1, 192;" ::: "memory");
-      // K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc on the
+      asm volatile("bar.sync 1, 320;" ::: "memory");  // raw accumulators, rowp, pos of the element staged
+      // a thread per basis pair b <= c: its 3 x 3 block of
+      //   G = 2^sh ((acc0 + t) + (e + acc2 + acc3)),  t + e = X + X^T exactly,
+      // then K[(b,d),(c,e)] = lam G[(b,d),(c,e)] + mu G[(b,e),(c,d)] + delta_de mu tr G_bc on the
       // FP32 pipe with error-free products and sums (lam, mu as FP32 pairs); one
-      // FP64 add per entry joins the pair for the FP64 reduction into the CSR values
-      for (int u = t; u < NE * NE; u += 192) {
-        const int rr = u / NE, cc = u - NE * rr;
-        const int b = rr / 3, d = rr - 3 * b, c = cc / 3, e = cc - 3 * c;
-        const float2 g1 = S.G[(3 * b + d) * OZ_GP + 3 * c + e], g2 = S.G[(3 * b + e) * OZ_GP + 3 * c + d];
-        float e1, e2, e3;
-        const float p1 = two_prod(lamh, g1.x, e1), p2 = two_prod(muh, g2.x, e2);
-        float s = two_sum(p1, p2, e3);
-        float rest = __fadd_rn(__fadd_rn(e1, e2), e3);
-        rest = __fadd_rn(rest, __fadd_rn(__fmaf_rn(lamh, g1.y, __fmul_rn(laml, g1.x)),
-                                         __fmaf_rn(muh, g2.y, __fmul_rn(mul, g2.x))));
-        if (d == e) {
-          const float2 tr = S.T[NB * b + c];
-          float e4;
-          s = two_sum(s, tr.x, e4);
-          rest = __fadd_rn(rest, __fadd_rn(e4, tr.y));
+      // FP64 add per entry joins the pair for the FP64 reductions into the CSR
+      // values, at (b, c) and, transposed, at (c, b)
+      for (int pr = t; pr < OZ_NPAIR; pr += OZ_EPI) {
+        const int b = S.pb[pr], c = S.pc[pr];
+        float2 g[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+#pragma unroll
+          for (int e = 0; e < 3; e++) {
+            const int r = 3 * b + d, col = 3 * c + e;
+            const float2 raw = S.G[r * OZ_GP + col];
+            const float sc = pow2f(S.ex[r] + S.ex[col] - 16);
+            float e0, e1;
+            const float tt = two_sum(S.X[r * OZ_XP + col], S.X[col * OZ_XP + r], e0);
+            const float small = __fadd_rn(e0, raw.y);
+            const float sh = two_sum(__fmul_rn(raw.x, sc), __fmul_rn(tt, sc), e1);
+            g[d][e] = make_float2(sh, __fadd_rn(e1, __fmul_rn(small, sc)));
+          }
+        float2 tr;  // mu tr G_bc, as a pair
+        {
+          float e0, e1, q;
+          const float a = two_sum(g[0][0].x, g[1][1].x, e0);
+          const float sm = two_sum(a, g[2][2].x, e1);
+          const float low = __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(__fadd_rn(g[0][0].y, g[1][1].y), g[2][2].y));
+          const float th = two_prod(muh, sm, q);
+          tr = make_float2(th, __fadd_rn(q, __fadd_rn(__fmul_rn(muh, low), __fmul_rn(mul, sm))));
         }
-        const double kk = f32_to_f64(s) + f32_to_f64(rest);
-        double *dst = vals + S.rowp[rr] + 3 * (int)S.pos[NB * b + c] + e;
-        asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(kk) : "memory");
+        const int pbc = 3 * (int)S.pos[NB * b + c], pcb = 3 * (int)S.pos[NB * c + b];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const int64_t rowb = S.rowp[3 * b + d];
+#pragma unroll
+          for (int e = 0; e < 3; e++) {
+            const float2 g1 = g[d][e], g2 = g[e][d];
+            float e1, e2, e3;
+            const float p1 = two_prod(lamh, g1.x, e1), p2 = two_prod(muh, g2.x, e2);
+            float sk = two_sum(p1, p2, e3);
+            float rest = __fadd_rn(__fadd_rn(e1, e2), e3);
+            rest = __fadd_rn(rest, __fadd_rn(__fmaf_rn(lamh, g1.y, __fmul_rn(laml, g1.x)),
+                                             __fmaf_rn(muh, g2.y, __fmul_rn(mul, g2.x))));
+            if (d == e) {
+              float e4;
+              sk = two_sum(sk, tr.x, e4);
+              rest = __fadd_rn(rest, __fadd_rn(e4, tr.y));
+            }
+            const double kk = f32_to_f64(sk) + f32_to_f64(rest);
+            double *dst = vals + rowb + pbc + e;
+            asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst), "d"(kk) : "memory");
+            if (b != c) {
+              double *dst2 = vals + S.rowp[3 * c + e] + pcb + d;
+              asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(dst2), "d"(kk) : "memory");
+            }
+          }
+        }
       }
-      asm volatile("bar.sync 1, 192;" ::: "memory");  // before the next element overwrites them
+      asm volatile("bar.sync 1, 320;" ::: "memory");  // before the next element overwrites them
     }
     if (!ok) S.abort = 1;
   }
