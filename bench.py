@@ -517,7 +517,7 @@ def main():
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_value = world * A.nelem_total / (statistics.median(e2e_ms) * 1e-3)
 
-    # SpMV of the assembled matrix (the MATSHELL multiply)
+    # SpMV of the assembled matrix (the MATSHELL multiply), FP64
     x = torch.tensor(rng.standard_normal(A.ndof), device=dev)
     y = torch.zeros_like(x)
     with torch.cuda.stream(stream):
@@ -530,7 +530,9 @@ def main():
         e1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = e0.elapsed_time(e1) / max(a.spmv, 1)
-    spmv_bytes = A.nnz * (8 + 4) + (A.ndof + 1) * 8 + 2 * A.ndof * 8
+    # the structured multiply streams the values (8 B per nonzero; the column
+    # of each entry is computed from the stencil), the row offsets, x and y
+    spmv_bytes = A.nnz * 8 + (A.ndof + 1) * 8 + 2 * A.ndof * 8
     sampler.stop()
 
     peaks = _peaks()

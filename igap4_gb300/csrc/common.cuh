@@ -295,6 +295,7 @@ int launch_res_df(Context *c, double *RR);
 int ensure_gram_operands(Context *c);
 // krylov.cu
 int spmv(Context *c, const double *vals, const double *x, double *y);
+bool spmv_df(const Context *c);
 int ksp_gmres(Context *c, const double *b, double *x, const igapgpu_solver_opts *o, int *its,
               double *rnorm);
 int dev_norm2(Context *c, const double *x, double *out);

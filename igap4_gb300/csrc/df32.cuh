@@ -15,6 +15,7 @@
 // reassociate it.
 #pragma once
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace igap {
 
@@ -67,5 +68,30 @@ __device__ __forceinline__ void dot2(float &s, float &c, float2 a, float2 b)
 
 // The pair of a Dot2 accumulator.
 __device__ __forceinline__ float2 dot2_pair(float s, float c) { return fast_two_sum(s, c); }
+
+static __device__ __noinline__ float2 f64_to_pair_rare(double x)
+{
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+// x = hi + lo to 2^-48 |x| on the integer pipe: hi is x truncated to 24
+// significant bits (exponent and top mantissa bits moved into a float), lo
+// the remaining 29 mantissa bits converted and scaled by 2^(e - 52).  Zeros
+// stay on the integer pipe; |x| outside [2^-74, 2^127), subnormal and
+// non-finite values take the out-of-line FP64 path.
+__device__ __forceinline__ float2 f64_to_pair(double x)
+{
+  const uint32_t hw = (uint32_t)__double2hiint(x), lw = (uint32_t)__double2loint(x);
+  const uint32_t ef = (hw >> 20) & 0x7ffu;  // biased exponent, e = ef - 1023
+  if (__builtin_expect(ef - 949u > 200u, 0)) {
+    if ((hw & 0x7fffffffu) == 0u && lw == 0u) return make_float2(__uint_as_float(hw & 0x80000000u), 0.f);
+    return f64_to_pair_rare(x);
+  }
+  const uint32_t sg = hw & 0x80000000u;
+  const float h = __uint_as_float(sg | ((ef - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  const float l = __fmul_rn(__uint2float_rn(lw & 0x1fffffffu), __uint_as_float((ef - 948u) << 23));
+  return make_float2(h, __uint_as_float(__float_as_uint(l) | sg));
+}
 
 }  // namespace igap

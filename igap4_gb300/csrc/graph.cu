@@ -35,6 +35,7 @@ constexpr int RB = 304, RT = 512;
 
 __global__ void gm_reset(GmState *st) { st->done = 0; st->its = 0; }
 
+template <bool DF>
 __global__ void __launch_bounds__(256) gm_spmv(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
                                                const double *__restrict__ vals, const double *__restrict__ x,
                                                double *__restrict__ y, int64_t n, const GmState *st, int nb0,
@@ -43,7 +44,7 @@ __global__ void __launch_bounds__(256) gm_spmv(const int64_t *__restrict__ rowpt
   if (st && st->done) return;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_G;
   const int sub = threadIdx.x % SPMV_G;
-  const double s = spmv_row(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
+  const double s = spmv_row<DF>(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
   if (sub == 0 && row < n) y[row] = s;
 }
 
@@ -247,6 +248,7 @@ __global__ void get_diag_kernel_g(const int64_t *rowptr, const int32_t *cols, co
 // Graph workspace held by the context.
 struct GraphWork {
   int m = 0, pc = -1, orth = -1;
+  bool df = false;  // double-FP32 multiply
   cudaGraphExec_t exec = nullptr;
   int64_t nodes = 0;
   double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *V = nullptr, *Z = nullptr;
@@ -312,6 +314,8 @@ static int build_gmres_graph(Context *c, int m, int pc, int orth)
   gw->m = m;
   gw->pc = pc;
   gw->orth = orth;
+  gw->df = spmv_df(c);
+  auto gspmv = gw->df ? gm_spmv<true> : gm_spmv<false>;
   const unsigned vb = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
   const unsigned sb = (unsigned)((n * SPMV_G + 255) / 256);
   cudaStream_t s = capture_stream(c);
@@ -319,8 +323,8 @@ static int build_gmres_graph(Context *c, int m, int pc, int orth)
   IGAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   gm_reset<<<1, 1, 0, s>>>(gw->st);
   const int nb0 = (c->batch || c->porder != P) ? 0 : c->nbasis[0];
-  gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->x, gw->r, n, nullptr, nb0, c->nbasis[1],
-                             c->nbasis[2]);
+  gspmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, gw->x, gw->r, n, nullptr, nb0, c->nbasis[1],
+                           c->nbasis[2]);
   gm_sub_from<<<vb, 256, 0, s>>>(gw->r, gw->b, n);
   gm_dot_partial<<<RB, RT, 0, s>>>(gw->r, gw->r, n, gw->partial, nullptr);
   gm_dot_final<<<1, 1024, 0, s>>>(gw->partial, RB, gw->scal, 1, nullptr);
@@ -331,8 +335,8 @@ static int build_gmres_graph(Context *c, int m, int pc, int orth)
     double *vj = gw->V + (size_t)j * n, *zj = gw->Z + (size_t)j * n, *vn = gw->V + (size_t)(j + 1) * n;
     double *hcol = gw->H + (size_t)j * (m + 1);
     gm_precond<<<vb, 256, 0, s>>>(zj, vj, gw->diag, pc, n, cell_geom(c), gw->st);
-    gm_spmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st, nb0, c->nbasis[1],
-                               c->nbasis[2]);
+    gspmv<<<sb, 256, 0, s>>>(c->d_rowptr, c->d_cols, c->d_vals, zj, gw->w, n, gw->st, nb0, c->nbasis[1],
+                             c->nbasis[2]);
     nodes += 2;
     if (orth == 1) {  // CGS2: two block passes h = V^T w, w -= V h
       const dim3 gp(MD_BLOCKS, (unsigned)(j + 1));
@@ -399,7 +403,8 @@ int ksp_gmres_graph(Context *c, const double *b, double *x, const igapgpu_solver
     set_error("block preconditioners (pc = 3, 4) need a single lattice; a batch takes pc 0, 1 or 2");
     return IGAPGPU_ERR_ARG;
   }
-  if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc || c->gmres_graph->orth != orth) {
+  if (!c->gmres_graph || c->gmres_graph->m != m || c->gmres_graph->pc != pc || c->gmres_graph->orth != orth ||
+      c->gmres_graph->df != spmv_df(c)) {
     int r = build_gmres_graph(c, m, pc, orth);
     if (r) return r;
   }

@@ -19,7 +19,9 @@ namespace igap {
 constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
 constexpr int RED_THREADS = 512;
 
-// y = A x, SPMV_G lanes per row (spmv_row; structured columns when nb0 > 0).
+// y = A x, SPMV_G lanes per row (spmv_row; structured columns when nb0 > 0;
+// DF: double-FP32 products on the FP32 pipe).
+template <bool DF>
 __global__ void __launch_bounds__(256) spmv_csr_kernel(const int64_t *__restrict__ rowptr,
                                                        const int32_t *__restrict__ cols,
                                                        const double *__restrict__ vals,
@@ -29,7 +31,7 @@ __global__ void __launch_bounds__(256) spmv_csr_kernel(const int64_t *__restrict
 {
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_G;
   const int sub = threadIdx.x % SPMV_G;
-  const double s = spmv_row(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
+  const double s = spmv_row<DF>(rowptr, cols, vals, x, row, row < n, sub, nb0, nb1, nb2);
   if (sub == 0 && row < n) y[row] = s;
 }
 
@@ -135,14 +137,26 @@ static unsigned vec_blocks(int64_t n)
   return (unsigned)(b < 152 * 8 ? b : 152 * 8);
 }
 
+// IGAPGPU_SPMV_DF=1: the multiply of the split and FP64-quality modes in
+// double-FP32 arithmetic on the FP32 pipe.  Off by default: measured at
+// 128x32x32 it takes 0.55 ms against 0.375 ms for the FP64 multiply (the
+// integer-pipe splits of the value and of x cost more issue slots per
+// nonzero than the FP64 FMA they replace).
+bool spmv_df(const Context *c)
+{
+  const char *e = getenv("IGAPGPU_SPMV_DF");
+  return e && e[0] == '1' && c->prec != IGAPGPU_PREC_FP64;
+}
+
 int spmv(Context *c, const double *vals, const double *x, double *y)
 {
   const int64_t n = c->ndof;
   // a batch's rows belong to different lattices; the structured columns are
   // those of the quadratic stencil
   const int nb0 = (c->batch || c->porder != P) ? 0 : c->nbasis[0];
-  spmv_csr_kernel<<<(unsigned)((n * SPMV_G + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n,
-                                                                            nb0, c->nbasis[1], c->nbasis[2]);
+  auto kern = spmv_df(c) ? spmv_csr_kernel<true> : spmv_csr_kernel<false>;
+  kern<<<(unsigned)((n * SPMV_G + 255) / 256), 256, 0, c->stream>>>(c->d_rowptr, c->d_cols, vals, x, y, n, nb0,
+                                                                    c->nbasis[1], c->nbasis[2]);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;

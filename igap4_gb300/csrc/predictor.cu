@@ -12,9 +12,11 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace igap {
 
@@ -136,6 +138,362 @@ __global__ void __launch_bounds__(256) conv_bwd_weight(const float *__restrict__
   }
 }
 
+// ------------------------------------------- tensor-core convolution (tcgen05)
+// The 32 -> 32 channel layers as an implicit GEMM on the tensor cores:
+// for a tile of 128 consecutive lattice points of one sample,
+//   D[p][n] = sum_t sum_k A_t[p][k] B_t[n][k],  A_t[p][k] = in[p + o(t)][k]
+// (zero where the neighbour is outside the lattice), one tcgen05.mma
+// kind::f16 (BF16 inputs, FP32 accumulation in tensor memory, M128 N32 K16)
+// per tap and 16 input channels: 54 MMAs per tile.  Forward: B_t[co][ci] =
+// W[co][t][ci], output BF16 with bias and ReLU.  Data gradient: the same
+// product of dZ (BF16) with B_t[ci][co] = W[co][26 - t][ci] (o(26 - t) =
+// -o(t)), output FP32.  Operands in shared memory in the K-major no-swizzle
+// layout (core matrices of 8 rows x 16 B, LBO 128 B, SBO 256 B): the weights
+// of all 27 taps once per CTA (persistent over tiles), the neighbour rows of
+// one tap double buffered: the threads load tap t + 1 (16-byte loads of the
+// channels-last rows, the lattice boundary masked) while the tensor core
+// multiplies tap t.  Every mbarrier wait is bounded.
+constexpr int CT_THREADS = 128;
+constexpr int CT_TAP_A = 2 * 16 * 256;   // one tap's A tile: 2 K-steps x 16 row groups x 256 B
+constexpr int CT_TAP_B = 2 * 4 * 256;    // one tap's B tile: 2 K-steps x 4 row groups x 256 B
+constexpr uint32_t CT_WAIT_LIMIT = 1u << 24;
+
+struct ConvTcSmem {
+  unsigned char A[2][CT_TAP_A];
+  unsigned char B[27][CT_TAP_B];
+  uint64_t done[2];
+  uint32_t taddr;
+};
+
+// Byte offset of BF16 element (row r, k in [0, 16)) inside one K-step block.
+__device__ __forceinline__ uint32_t ct_off(int r, int k)
+{
+  return (uint32_t)((r >> 3) * 256 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// The B operand of every tap for one layer and mode, [27][n][k] (BF16):
+// forward Wk[t][co][ci] = W[co][t][ci]; data gradient Wk[t][ci][co] =
+// W[co][26 - t][ci].
+__global__ void conv_tc_weights_kernel(const __nv_bfloat16 *__restrict__ W, __nv_bfloat16 *__restrict__ Wk, int mode)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 27 * 32 * 32) return;
+  const int t = i / 1024, n = (i / 32) % 32, k = i % 32;
+  Wk[i] = mode == 0 ? W[((int64_t)n * 27 + t) * 32 + k] : W[((int64_t)k * 27 + (26 - t)) * 32 + n];
+}
+
+// MODE 0: forward (out BF16, bias, ReLU); MODE 1: data gradient (out FP32).
+// Thread r of the CTA owns row r of every tile (its lattice coordinates are
+// computed once per tile) and loads that row's neighbour (64 B) for every tap.
+template <int MODE>
+__global__ void __launch_bounds__(CT_THREADS) conv_tc_kernel(const __nv_bfloat16 *__restrict__ in,
+                                                             const __nv_bfloat16 *__restrict__ Wk,
+                                                             const float *__restrict__ bias, void *__restrict__ out,
+                                                             Lattice L, int B, int relu, int *err)
+{
+  extern __shared__ __align__(1024) unsigned char ct_raw[];
+  ConvTcSmem &S = *reinterpret_cast<ConvTcSmem *>(ct_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, 32);
+    tc::tmem_relinquish();
+  }
+  // weights of every tap: B_t[n][k], K-major (2 K-steps of 16 per tap), 16 B at a time
+  for (int i = tid; i < 27 * 32 * 4; i += CT_THREADS) {
+    const int t = i / 128, n = (i / 4) % 32, j = i % 4;
+    const uint4 w = __ldg(reinterpret_cast<const uint4 *>(Wk + ((int64_t)t * 32 + n) * 32) + j);
+    *reinterpret_cast<uint4 *>(S.B[t] + (j >> 1) * 1024 + ct_off(n, (j & 1) * 8)) = w;
+  }
+  if (tid == 0) {
+    tc::mbar_init(&S.done[0], 1);
+    tc::mbar_init(&S.done[1], 1);
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = S.taddr;
+  const uint32_t idesc = tc::instr_desc(1, 128, 32);
+  const int64_t tiles_per_sample = (L.P + 127) / 128, ntiles = tiles_per_sample * B;
+  const int64_t syz = (int64_t)L.ny * L.nz;
+  uint32_t use0 = 0, use1 = 0;  // commits issued on each buffer
+  bool ok = true;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int b = (int)(tile / tiles_per_sample);
+    const int64_t p0 = (tile % tiles_per_sample) * 128;
+    const int64_t p = p0 + tid;  // this thread's row
+    const bool rowv = p < L.P;
+    const int iz = (int)(p % L.nz), iy = (int)((p / L.nz) % L.ny), ix = (int)(p / syz);
+    const uint4 *src = reinterpret_cast<const uint4 *>(in + ((int64_t)b * L.P + p) * 32);
+    for (int t = 0; t < 27 && ok; t++) {
+      const int buf = t & 1;
+      const uint32_t used = buf ? use1 : use0;
+      if (used > 0 && !tc::mbar_wait(&S.done[buf], (used - 1) & 1, CT_WAIT_LIMIT)) {
+        ok = false;
+        break;
+      }
+      const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+      const bool v = rowv && (unsigned)(ix + dx) < (unsigned)L.nx && (unsigned)(iy + dy) < (unsigned)L.ny &&
+                     (unsigned)(iz + dz) < (unsigned)L.nz;
+      const int64_t off = ((int64_t)dx * L.ny + dy) * L.nz + dz;  // rows
+      unsigned char *a = S.A[buf];
+#pragma unroll
+      for (int j16 = 0; j16 < 4; j16++) {
+        const uint4 x = v ? __ldg(src + off * 4 + j16) : make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(a + (j16 >> 1) * 4096 + ct_off(tid, (j16 & 1) * 8)) = x;
+      }
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t abase = tc::smem_u32(S.A[buf]), bbase = tc::smem_u32(S.B[t]);
+        for (int ks = 0; ks < 2; ks++) {
+          const uint64_t ad = tc::smem_desc(abase + (uint32_t)ks * 4096u, 128, 256);
+          const uint64_t bd = tc::smem_desc(bbase + (uint32_t)ks * 1024u, 128, 256);
+          tc::mma_bf16(taddr, ad, bd, idesc, (t > 0 || ks > 0) ? 1u : 0u);
+        }
+        tc::mma_commit(&S.done[buf]);
+      }
+      if (buf) use1++;
+      else use0++;
+    }
+    if (!ok) break;
+    // the last tap's commit (buffer 0) covers every MMA of the tile
+    if (!tc::mbar_wait(&S.done[0], (use0 - 1) & 1, CT_WAIT_LIMIT)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    uint32_t r[32];
+    tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16), r);
+    const int64_t pw = p0 + warp * 32 + lane;  // TMEM lane = row = this thread's row
+    if (pw < L.P) {
+      if constexpr (MODE == 0) {
+        uint32_t pk[16];
+#pragma unroll
+        for (int n = 0; n < 32; n += 2) {
+          float a0 = __uint_as_float(r[n]) + bias[n], a1 = __uint_as_float(r[n + 1]) + bias[n + 1];
+          if (relu) {
+            a0 = fmaxf(a0, 0.f);
+            a1 = fmaxf(a1, 0.f);
+          }
+          const __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
+          pk[n / 2] = *reinterpret_cast<const uint32_t *>(&h);
+        }
+        uint4 *o = reinterpret_cast<uint4 *>((__nv_bfloat16 *)out + ((int64_t)b * L.P + pw) * 32);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; q4++) o[q4] = make_uint4(pk[4 * q4], pk[4 * q4 + 1], pk[4 * q4 + 2], pk[4 * q4 + 3]);
+      } else {
+        float4 *o = reinterpret_cast<float4 *>((float *)out + ((int64_t)b * L.P + pw) * 32);
+#pragma unroll
+        for (int q4 = 0; q4 < 8; q4++)
+          o[q4] = make_float4(__uint_as_float(r[4 * q4]), __uint_as_float(r[4 * q4 + 1]),
+                              __uint_as_float(r[4 * q4 + 2]), __uint_as_float(r[4 * q4 + 3]));
+      }
+    }
+    tc::fence_before_sync();  // the next tile's first MMA overwrites the accumulator
+  }
+  if (!ok && tid == 0) {
+    atomicCAS(err, 0, 2);
+    // let MMAs still in flight finish before the tensor memory is freed
+    if (use0 > 0) tc::mbar_wait(&S.done[0], (use0 - 1) & 1, CT_WAIT_LIMIT);
+    if (use1 > 0) tc::mbar_wait(&S.done[1], (use1 - 1) & 1, CT_WAIT_LIMIT);
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, 32);
+}
+
+// Weight gradient on the tensor cores: dW[co][t][ci] += sum_p dZ[p][co] X[p + o(t)][ci]
+// as D[(tl, ci)][co] = sum_p A[(tl, ci)][p] Z[co][p] for groups of TPG =
+// 128 / CI taps (4 taps of 32 channels, or 14 taps of the 9 input features
+// per M = 128 rows, row tl * CI + ci), K = the 128 points of a tile, N = 32
+// output channels: 8 MMAs (K16) per group and tile, one TMEM accumulator of
+// 32 columns per group for the whole run of the CTA (persistent over tiles);
+// at the end the CTA adds its sums into dW with FP32 reductions.  Thread p of
+// the CTA owns point p of each tile: it loads the point's output gradient
+// (64 B) and its neighbours' features (16-byte loads for 32 channels) and
+// writes them transposed (K-major, the points along K).
+template <int CI>
+struct WgradCfg {
+  static constexpr int TPG = 128 / CI;
+  static constexpr int NG = (27 + TPG - 1) / TPG;
+  static constexpr uint32_t COLS = NG * 32 <= 32 ? 32 : (NG * 32 <= 64 ? 64 : (NG * 32 <= 128 ? 128 : 256));
+};
+constexpr int WG_TAP_A = 8 * 16 * 256;  // A of one group: 8 K-steps x 16 row groups x 256 B
+constexpr int WG_Z = 8 * 4 * 256;       // Z: 8 K-steps x 4 row groups x 256 B
+
+struct WgradSmem {
+  unsigned char A[2][WG_TAP_A];
+  unsigned char Z[WG_Z];
+  uint64_t done[2];
+  uint32_t taddr;
+};
+
+__device__ __forceinline__ void st_bf16(unsigned char *base, int m, int k, uint32_t bits)
+{
+  asm volatile("st.shared.b16 [%0], %1;" ::"r"(tc::smem_u32(base + (k >> 4) * 4096 + ct_off(m, k & 15))),
+               "h"((unsigned short)bits)
+               : "memory");
+}
+
+template <int CI>
+__global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bfloat16 *__restrict__ X,
+                                                                   const __nv_bfloat16 *__restrict__ dZh,
+                                                                   float *__restrict__ gW, Lattice L, int B,
+                                                                   int *err)
+{
+  using C = WgradCfg<CI>;
+  extern __shared__ __align__(1024) unsigned char wg_raw[];
+  WgradSmem &S = *reinterpret_cast<WgradSmem *>(wg_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.taddr, C::COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&S.done[0], 1);
+    tc::mbar_init(&S.done[1], 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = S.taddr;
+  const uint32_t idesc = tc::instr_desc(1, 128, 32);
+  const int64_t tiles_per_sample = (L.P + 127) / 128, ntiles = tiles_per_sample * B;
+  const int64_t syz = (int64_t)L.ny * L.nz;
+  uint32_t use0 = 0, use1 = 0, nuse = 0;
+  bool ok = true, first = true;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int b = (int)(tile / tiles_per_sample);
+    const int64_t p = (tile % tiles_per_sample) * 128 + tid;
+    const bool rowv = p < L.P;
+    const int iz = (int)(p % L.nz), iy = (int)((p / L.nz) % L.ny), ix = (int)(p / syz);
+    // Z is read by every group's MMAs of the previous tile: wait for the last one
+    if (nuse > 0) {
+      const int lb = (nuse - 1) & 1;
+      const uint32_t used = lb ? use1 : use0;
+      if (!tc::mbar_wait(&S.done[lb], (used - 1) & 1, CT_WAIT_LIMIT)) {
+        ok = false;
+        break;
+      }
+    }
+    {
+      const uint4 *zr = reinterpret_cast<const uint4 *>(dZh + ((int64_t)b * L.P + p) * 32);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint4 z = rowv ? __ldg(zr + j) : make_uint4(0u, 0u, 0u, 0u);
+        const uint32_t w4[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+        for (int h = 0; h < 8; h++) {
+          const int co = 8 * j + h;
+          const uint32_t bits = (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu;
+          asm volatile("st.shared.b16 [%0], %1;" ::"r"(tc::smem_u32(S.Z + (tid >> 4) * 1024 + ct_off(co, tid & 15))),
+                       "h"((unsigned short)bits)
+                       : "memory");
+        }
+      }
+    }
+    for (int g = 0; g < C::NG && ok; g++, nuse++) {
+      const int buf = nuse & 1;
+      const uint32_t used = buf ? use1 : use0;
+      if (used > 0 && !tc::mbar_wait(&S.done[buf], (used - 1) & 1, CT_WAIT_LIMIT)) {
+        ok = false;
+        break;
+      }
+      unsigned char *a = S.A[buf];
+      for (int tl = 0; tl < C::TPG; tl++) {
+        const int t = g * C::TPG + tl;
+        const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+        const bool v = t < 27 && rowv && (unsigned)(ix + dx) < (unsigned)L.nx &&
+                       (unsigned)(iy + dy) < (unsigned)L.ny && (unsigned)(iz + dz) < (unsigned)L.nz;
+        const int64_t q = (int64_t)b * L.P + p + ((int64_t)dx * L.ny + dy) * L.nz + dz;
+        if constexpr (CI == 32) {
+          const uint4 *xr = reinterpret_cast<const uint4 *>(X + q * 32);
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const uint4 x = v ? __ldg(xr + j) : make_uint4(0u, 0u, 0u, 0u);
+            const uint32_t w4[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int h = 0; h < 8; h++) st_bf16(a, tl * 32 + 8 * j + h, tid, (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+          }
+        } else {
+          const unsigned short *xr = reinterpret_cast<const unsigned short *>(X + q * CI);
+#pragma unroll
+          for (int ci = 0; ci < CI; ci++) st_bf16(a, tl * CI + ci, tid, v ? __ldg(xr + ci) : 0u);
+        }
+      }
+      for (int m = C::TPG * CI; m < 128; m++) st_bf16(a, m, tid, 0u);  // rows past the last group member
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t abase = tc::smem_u32(a), zbase = tc::smem_u32(S.Z);
+        for (int ks = 0; ks < 8; ks++) {
+          const uint64_t ad = tc::smem_desc(abase + (uint32_t)ks * 4096u, 128, 256);
+          const uint64_t zd = tc::smem_desc(zbase + (uint32_t)ks * 1024u, 128, 256);
+          tc::mma_bf16(taddr + (uint32_t)(g * 32), ad, zd, idesc, (!first || ks > 0) ? 1u : 0u);
+        }
+        tc::mma_commit(&S.done[buf]);
+      }
+      if (buf) use1++;
+      else use0++;
+    }
+    first = false;
+  }
+  // the last commit covers every MMA of the CTA
+  if (ok && nuse > 0) {
+    const int lb = (nuse - 1) & 1;
+    const uint32_t used = lb ? use1 : use0;
+    if (!tc::mbar_wait(&S.done[lb], (used - 1) & 1, CT_WAIT_LIMIT)) ok = false;
+  }
+  if (ok && nuse > 0) {
+    tc::fence_after_sync();
+    const int m = warp * 32 + lane;  // TMEM lane = row (tl, ci)
+    for (int g = 0; g < C::NG; g++) {
+      uint32_t r[32];
+      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * 32), r);
+      const int t = g * C::TPG + m / CI, ci = m % CI;
+      if (m < C::TPG * CI && t < 27)
+#pragma unroll
+        for (int co = 0; co < 32; co++) atomicAdd(gW + ((int64_t)co * 27 + t) * CI + ci, __uint_as_float(r[co]));
+    }
+  }
+  if (!ok && tid == 0) {
+    atomicCAS(err, 0, 2);
+    if (use0 > 0) tc::mbar_wait(&S.done[0], (use0 - 1) & 1, CT_WAIT_LIMIT);
+    if (use1 > 0) tc::mbar_wait(&S.done[1], (use1 - 1) & 1, CT_WAIT_LIMIT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, C::COLS);
+}
+
+// db[co] += sum over the points of dZ[p][co] (FP32)
+__global__ void bias_grad_kernel(const float *__restrict__ dZ, int Co, int64_t NP, float *__restrict__ db)
+{
+  __shared__ float sh[8][33];
+  const int co = threadIdx.x & 31, pl = threadIdx.x >> 5;
+  float s = 0.f;
+  if (co < Co)
+    for (int64_t p = (int64_t)blockIdx.x * 8 + pl; p < NP; p += (int64_t)gridDim.x * 8) s += dZ[p * Co + co];
+  sh[pl][co] = s;
+  __syncthreads();
+  if (threadIdx.x < 32 && co < Co) {
+    float t = 0.f;
+    for (int k = 0; k < 8; k++) t += sh[k][co];
+    atomicAdd(db + co, t);
+  }
+}
+
+// dZ (FP32, masked by ReLU') -> BF16 copy for the tensor-core data gradient
+__global__ void to_bf16_kernel(const float *src, __nv_bfloat16 *dst, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __float2bfloat16_rn(src[i]);
+}
+
 // loss = mean (y - target)^2 over n values; dY = 2 (y - target) / n
 template <typename T>
 __global__ void mse_kernel(const T *y, const float *target, float *dY, float *loss, int64_t n)
@@ -203,16 +561,97 @@ struct igapgpu_net {
   void *act[NL + 1] = {};                     // activations (storage type), act[0] = input
   float *dA = nullptr, *dB = nullptr;         // gradient scratch [bmax*P*32]
   float *target = nullptr, *loss = nullptr;
+  __nv_bfloat16 *dZh = nullptr;               // BF16 copy of a layer's output gradient [bmax*P*32]
+  __nv_bfloat16 *Wk = nullptr;                // one layer's weights arranged per tap [27][32][32]
+  int *err = nullptr;                         // device error word of the tensor-core convolutions
   int step = 0;
   cudaStream_t stream = nullptr;
 };
 
 namespace {
+// The tensor-core convolution for the 32 -> 32 layers of a BF16 network
+// (IGAPGPU_NET_TC=0 keeps the scalar kernels, for comparisons).
+bool use_tc(const igapgpu_net *n, int l)
+{
+  const char *e = getenv("IGAPGPU_NET_TC");
+  return n->storage == 1 && kCin[l] == 32 && kCout[l] == 32 && !(e && e[0] == '0');
+}
+
+template <int MODE>
+int launch_conv_tc(igapgpu_net *n, const __nv_bfloat16 *in, const __nv_bfloat16 *W, const float *bias, void *out,
+                   int B, int relu)
+{
+  conv_tc_weights_kernel<<<(27 * 32 * 32 + 255) / 256, 256, 0, n->stream>>>(W, n->Wk, MODE);
+  count_launch();
+  static bool attr[2] = {false, false};
+  const size_t smem = sizeof(ConvTcSmem) + 1024;
+  if (!attr[MODE]) {
+    IGAP_CUDA(cudaFuncSetAttribute(conv_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr[MODE] = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t ntiles = (n->L.P + 127) / 128 * B;
+  const int grid = (int)(ntiles < (int64_t)nsm * 3 ? ntiles : (int64_t)nsm * 3);
+  conv_tc_kernel<MODE><<<grid, CT_THREADS, smem, n->stream>>>(in, n->Wk, bias, out, n->L, B, relu, n->err);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+// the weight gradient of the layers with 32 output channels (9 or 32 inputs)
+bool use_tc_wgrad(const igapgpu_net *n, int l)
+{
+  const char *e = getenv("IGAPGPU_NET_TC");
+  return n->storage == 1 && kCout[l] == 32 && (kCin[l] == 32 || kCin[l] == 9) && !(e && e[0] == '0');
+}
+
+template <int CI>
+int launch_wgrad_tc(igapgpu_net *n, const __nv_bfloat16 *X, float *gW, int B)
+{
+  static bool attr = false;
+  const size_t smem = sizeof(WgradSmem) + 1024;
+  if (!attr) {
+    IGAP_CUDA(cudaFuncSetAttribute(conv_tc_wgrad_kernel<CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  int dev = 0, nsm = 0;
+  IGAP_CUDA(cudaGetDevice(&dev));
+  IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t ntiles = (n->L.P + 127) / 128 * B;
+  const int grid = (int)(ntiles < (int64_t)nsm * 2 ? ntiles : (int64_t)nsm * 2);
+  conv_tc_wgrad_kernel<CI><<<grid, CT_THREADS, smem, n->stream>>>(X, n->dZh, gW, n->L, B, n->err);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+// error word of the tensor-core convolutions (synchronises)
+int check_err(igapgpu_net *n)
+{
+  int h = 0;
+  IGAP_CUDA(cudaMemcpyAsync(&h, n->err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+  IGAP_CUDA(cudaStreamSynchronize(n->stream));
+  if (h) {
+    IGAP_CUDA(cudaMemsetAsync(n->err, 0, sizeof(int), n->stream));
+    set_error("tensor-core convolution: a bounded mbarrier wait expired (code %d)", h);
+    return IGAPGPU_ERR_TIMEOUT;
+  }
+  return IGAPGPU_OK;
+}
+
 template <typename T>
 int net_forward_t(igapgpu_net *n, int B)
 {
   const Lattice L = n->L;
   for (int l = 0; l < NL; l++) {
+    if (use_tc(n, l)) {
+      const int r = launch_conv_tc<0>(n, (const __nv_bfloat16 *)n->act[l], (const __nv_bfloat16 *)n->Wt + n->woff[l],
+                                      n->bias + n->boff[l], n->act[l + 1], B, l < NL - 1);
+      if (r) return r;
+      continue;
+    }
     const int64_t tot = (int64_t)B * L.P * kCout[l];
     conv_fwd<T><<<(unsigned)((tot + 255) / 256), 256, 0, n->stream>>>(
         (const T *)n->act[l], kCin[l], (const T *)n->Wt + n->woff[l], n->bias + n->boff[l], (T *)n->act[l + 1],
@@ -235,14 +674,33 @@ int net_backward_t(igapgpu_net *n, int B)
       relu_bwd<T><<<(unsigned)((nout + 255) / 256), 256, 0, n->stream>>>(dcur, (const T *)n->act[l + 1], nout);
       count_launch();
     }
-    conv_bwd_weight<T><<<kCout[l] * 27, 256, 0, n->stream>>>(dcur, kCout[l], (const T *)n->act[l], kCin[l],
-                                                               n->gW + n->woff[l], n->gb + n->boff[l], L, B);
-    count_launch();
+    // the BF16 copy of the output gradient feeds both tensor-core products
+    const bool tcw = use_tc_wgrad(n, l), tcd = l > 0 && use_tc(n, l);
+    if (tcw || tcd) {
+      to_bf16_kernel<<<152 * 8, 256, 0, n->stream>>>(dcur, n->dZh, nout);
+      count_launch();
+    }
+    if (tcw) {
+      const int r = kCin[l] == 32 ? launch_wgrad_tc<32>(n, (const __nv_bfloat16 *)n->act[l], n->gW + n->woff[l], B)
+                                  : launch_wgrad_tc<9>(n, (const __nv_bfloat16 *)n->act[l], n->gW + n->woff[l], B);
+      if (r) return r;
+      bias_grad_kernel<<<152 * 4, 256, 0, n->stream>>>(dcur, kCout[l], (int64_t)B * L.P, n->gb + n->boff[l]);
+      count_launch();
+    } else {
+      conv_bwd_weight<T><<<kCout[l] * 27, 256, 0, n->stream>>>(dcur, kCout[l], (const T *)n->act[l], kCin[l],
+                                                                 n->gW + n->woff[l], n->gb + n->boff[l], L, B);
+      count_launch();
+    }
     if (l > 0) {
       const int64_t nin = (int64_t)B * L.P * kCin[l];
-      conv_bwd_data<T><<<(unsigned)((nin + 255) / 256), 256, 0, n->stream>>>(dcur, kCout[l], (const T *)n->Wt + n->woff[l],
-                                                                             dnext, kCin[l], L, B);
-      count_launch();
+      if (tcd) {
+        const int r = launch_conv_tc<1>(n, n->dZh, (const __nv_bfloat16 *)n->Wt + n->woff[l], nullptr, dnext, B, 0);
+        if (r) return r;
+      } else {
+        conv_bwd_data<T><<<(unsigned)((nin + 255) / 256), 256, 0, n->stream>>>(dcur, kCout[l], (const T *)n->Wt + n->woff[l],
+                                                                               dnext, kCin[l], L, B);
+        count_launch();
+      }
       float *tmp = dcur;
       dcur = dnext;
       dnext = tmp;
@@ -291,7 +749,10 @@ int igapgpu_net_create(igapgpu_net **out, int nx, int ny, int nz, int batch_max,
             cudaMalloc(&n->dA, sizeof(float) * maxact) == cudaSuccess &&
             cudaMalloc(&n->dB, sizeof(float) * maxact) == cudaSuccess &&
             cudaMalloc(&n->target, sizeof(float) * batch_max * n->L.P * 3) == cudaSuccess &&
-            cudaMalloc(&n->loss, sizeof(float)) == cudaSuccess;
+            cudaMalloc(&n->loss, sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&n->err, sizeof(int)) == cudaSuccess &&
+            (storage == 0 || (cudaMalloc(&n->dZh, sizeof(__nv_bfloat16) * maxact) == cudaSuccess &&
+                              cudaMalloc(&n->Wk, sizeof(__nv_bfloat16) * 27 * 32 * 32) == cudaSuccess));
   for (int l = 0; l <= NL && ok; l++) {
     const int C = l == 0 ? kCin[0] : kCout[l - 1];
     ok = cudaMalloc(&n->act[l], ts * (size_t)batch_max * n->L.P * C) == cudaSuccess;
@@ -301,6 +762,7 @@ int igapgpu_net_create(igapgpu_net **out, int nx, int ny, int nz, int batch_max,
     set_error("net_create: device allocation failed");
     return IGAPGPU_ERR_NOMEM;
   }
+  cudaMemset(n->err, 0, sizeof(int));
   cudaMemset(n->mW, 0, sizeof(float) * n->nw);
   cudaMemset(n->vW, 0, sizeof(float) * n->nw);
   cudaMemset(n->mb, 0, sizeof(float) * n->nb);
@@ -312,7 +774,8 @@ int igapgpu_net_create(igapgpu_net **out, int nx, int ny, int nz, int batch_max,
 int igapgpu_net_destroy(igapgpu_net *n)
 {
   if (!n) return IGAPGPU_OK;
-  void *bufs[] = {n->W, n->bias, n->Wt, n->gW, n->gb, n->mW, n->vW, n->mb, n->vb, n->dA, n->dB, n->target, n->loss};
+  void *bufs[] = {n->W, n->bias, n->Wt, n->gW, n->gb, n->mW, n->vW, n->mb, n->vb, n->dA, n->dB, n->target, n->loss,
+                  n->dZh, n->Wk, n->err};
   for (void *p : bufs)
     if (p) cudaFree(p);
   for (int l = 0; l <= NL; l++)
@@ -380,6 +843,9 @@ int igapgpu_net_forward(igapgpu_net *n, const float *in, float *out, int B)
     count_launch();
     if ((r = net_forward_t<__nv_bfloat16>(n, B))) return r;
     uncast_kernel<__nv_bfloat16><<<(unsigned)((nout + 255) / 256), 256, 0, n->stream>>>((const __nv_bfloat16 *)n->act[NL], out, nout);
+    count_launch();
+    IGAP_CHECK_LAUNCH();
+    return check_err(n);
   } else {
     cast_kernel<float><<<(unsigned)((nin + 255) / 256), 256, 0, n->stream>>>(in, (float *)n->act[0], nin);
     count_launch();
@@ -443,6 +909,7 @@ int igapgpu_net_train_step(igapgpu_net *n, const float *in, const float *target,
   if (loss_out) {
     IGAP_CUDA(cudaMemcpyAsync(loss_out, n->loss, sizeof(float), cudaMemcpyDeviceToHost, n->stream));
     IGAP_CUDA(cudaStreamSynchronize(n->stream));
+    if (n->storage) return check_err(n);
   }
   return IGAPGPU_OK;
 }

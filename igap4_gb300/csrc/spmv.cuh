@@ -16,16 +16,23 @@
 #pragma once
 #include "common.cuh"
 #include "element.cuh"
+#include "df32.cuh"
 
 namespace igap {
 
 constexpr int SPMV_G = 4;  // lanes per row
 
+// DF = true (split and FP64-quality modes, structured columns): every
+// product and the row sum on float pairs (the value and x split on the
+// integer pipe, compensated Dot2 accumulation), so that the multiply runs
+// on the FP32 pipe instead of the FP64 pipe (~1e-15 relative to FP64).
+template <bool DF = false>
 __device__ __forceinline__ double spmv_row(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
                                            const double *__restrict__ vals, const double *__restrict__ x,
                                            int64_t row, bool valid, int sub, int nb0, int nb1, int nb2)
 {
   double s = 0.0;
+  float ps = 0.f, pc = 0.f;  // Dot2 accumulator (DF)
   if (valid) {
     const int64_t s0 = __ldg(rowptr + row);
     if (nb0 > 0) {
@@ -45,7 +52,8 @@ __device__ __forceinline__ double spmv_row(const int64_t *__restrict__ rowptr, c
       const double *v = vals + s0;
       for (int k = sub; k < len; k += SPMV_G) {
         const int64_t col = 3 * (((int64_t)(lox + a) * nb1 + (loy + bb)) * nb2 + (loz + c)) + e;
-        s = fma(__ldg(v + k), __ldg(x + col), s);
+        if constexpr (DF) dot2(ps, pc, f64_to_pair(__ldg(v + k)), f64_to_pair(__ldg(x + col)));
+        else s = fma(__ldg(v + k), __ldg(x + col), s);
         int dq = 1;
         if (++e == 3) {
           e = 0;
@@ -62,12 +70,25 @@ __device__ __forceinline__ double spmv_row(const int64_t *__restrict__ rowptr, c
       }
     } else {
       const int64_t s1 = __ldg(rowptr + row + 1);
-      for (int64_t k = s0 + sub; k < s1; k += SPMV_G) s = fma(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
+      for (int64_t k = s0 + sub; k < s1; k += SPMV_G) {
+        if constexpr (DF) dot2(ps, pc, f64_to_pair(__ldg(vals + k)), f64_to_pair(__ldg(x + __ldg(cols + k))));
+        else s = fma(__ldg(vals + k), __ldg(x + __ldg(cols + k)), s);
+      }
     }
   }
-  s += __shfl_xor_sync(0xffffffffu, s, 1);
-  s += __shfl_xor_sync(0xffffffffu, s, 2);
-  return s;
+  if constexpr (DF) {
+    float2 r = dot2_pair(ps, pc);
+#pragma unroll
+    for (int o = 1; o < SPMV_G; o <<= 1) {
+      const float2 t = make_float2(__shfl_xor_sync(0xffffffffu, r.x, o), __shfl_xor_sync(0xffffffffu, r.y, o));
+      r = df_add(r, t);
+    }
+    return (double)r.x + (double)r.y;
+  } else {
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    return s;
+  }
 }
 
 }  // namespace igap

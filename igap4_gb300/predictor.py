@@ -215,3 +215,61 @@ def make_samples(states, loads, lattice_points):
         X.append((un, unm1, dl))
         Y.append((unp1 - un) - (un - unm1))
     return X, Y
+
+
+def time_convolutions(lattice=(66, 18, 18), batch=8, reps=10, seed=0):
+    """Wall-clock ms of one forward pass and one training step (forward, MSE,
+    backward, Adam) of a BF16 network, with the tensor-core convolutions
+    (IGAPGPU_NET_TC=1) and with the scalar kernels (=0), on the same seeded
+    network and inputs; 3 warm-up repetitions, synchronised."""
+    import os
+    import time
+
+    import torch
+
+    P = int(np.prod(lattice))
+    rng = np.random.default_rng(seed)
+    x = torch.tensor(rng.standard_normal((batch, P, 9)).astype(np.float32), device="cuda")
+    y = torch.tensor(rng.standard_normal((batch, P, 3)).astype(np.float32) * 0.1, device="cuda")
+    out = {}
+    old = os.environ.get("IGAPGPU_NET_TC")
+    try:
+        for flag in ("1", "0"):
+            os.environ["IGAPGPU_NET_TC"] = flag
+            net = ConvNet(lattice, batch_max=batch, storage="bf16", params=init_params(seed, zero_last=False))
+            o = torch.zeros((batch, P, 3), dtype=torch.float32, device="cuda")
+            for _ in range(3):
+                net.forward(x, o)
+                net.train_step(x, y, 1e-3)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                net.forward(x, o)
+            torch.cuda.synchronize()
+            tf = (time.perf_counter() - t0) / reps
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                net.train_step(x, y, 1e-3)
+            torch.cuda.synchronize()
+            tt = (time.perf_counter() - t0) / reps
+            out["tensor_cores" if flag == "1" else "scalar"] = {"forward_ms": 1e3 * tf, "train_step_ms": 1e3 * tt}
+            net.close()
+    finally:
+        if old is None:
+            os.environ.pop("IGAPGPU_NET_TC", None)
+        else:
+            os.environ["IGAPGPU_NET_TC"] = old
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="time the predictor's convolutions (tensor cores vs scalar)")
+    ap.add_argument("--lattice", default="66,18,18")
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--reps", type=int, default=10)
+    a = ap.parse_args()
+    lat = tuple(int(v) for v in a.lattice.split(","))
+    print(json.dumps({"lattice": lat, "batch": a.batch, **time_convolutions(lat, a.batch, a.reps)}))

@@ -77,3 +77,36 @@ def test_trained_predictor_reduces_newton_iterations():
     learned = tp.evaluate(A, [99], steps, dt, amax, LearnedPredictor(net, scales), opts)
     print("plain", plain, "learned", learned)
     assert learned["newton_its_per_step"] < plain["newton_its_per_step"]
+
+
+def test_tensor_core_convolution_matches_scalar(monkeypatch):
+    """The 32 -> 32 layers of a BF16 network run as tcgen05 implicit GEMMs
+    (forward and data gradient); against the scalar kernels (IGAPGPU_NET_TC=0)
+    on a lattice of several 128-point tiles with a partial last tile: the same
+    outputs up to BF16 rounding of the differently ordered FP32 sums, and the
+    same gradients up to the BF16 rounding of the output gradient."""
+    torch = pytest.importorskip("torch")
+    lattice, B = (19, 10, 9), 3
+    params, x, y = _case(4, lattice, B)
+    P = int(np.prod(lattice))
+    xd = torch.tensor(x.reshape(B, P, 9), device="cuda")
+    yd = torch.tensor(y.reshape(B, P, 3), device="cuda")
+    res = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("IGAPGPU_NET_TC", flag)
+        net = ConvNet(lattice, batch_max=B, storage="bf16", params=params)
+        out = torch.zeros((B, P, 3), dtype=torch.float32, device="cuda")
+        n0 = ig.launch_count()
+        net.forward(xd, out)
+        nl = ig.launch_count() - n0
+        loss = net.train_step(xd, yd, 0.0)
+        res[flag] = (out.cpu().numpy(), loss, net.get_grads(), nl)
+        net.close()
+    (o1, l1, g1, n1), (o0, l0, g0, n0) = res["1"], res["0"]
+    assert n1 == n0 + 2  # the two 32 -> 32 layers also arrange their weights per tap
+    e_out = np.linalg.norm(o1 - o0) / np.linalg.norm(o0)
+    e_g = np.linalg.norm(g1 - g0) / np.linalg.norm(g0)
+    print(f"tensor-core vs scalar convolution: output {e_out:.2e}, loss {abs(l1 - l0) / l0:.2e}, grads {e_g:.2e}")
+    assert e_out <= 2e-2
+    assert abs(l1 - l0) <= 2e-2 * l0
+    assert e_g <= 3e-2

@@ -275,3 +275,32 @@ def test_ozaki_mode_other_laws_is_fp64(law):
     K64 = A.tangent()
     A.set_precision(ig.PREC_OZAKI)
     np.testing.assert_array_equal(A.tangent(), K64)
+
+
+@pytest.mark.parametrize("prec", [ig.PREC_SPLIT, ig.PREC_OZAKI])
+def test_df_matmult_vs_fp64(prec, monkeypatch):
+    """The split and FP64-quality modes multiply in double-FP32 arithmetic
+    (values and x split into float pairs on the integer pipe, compensated
+    row sums).  The same assembled FP64 matrix, multiplied in both modes:
+    within 1e-13, for x with exact zeros and for x spanning 1e-30 .. 1e6
+    (the out-of-range entries take the FP64 split).  Opt-in
+    (IGAPGPU_SPMV_DF=1); without it the FP64 multiply, bit for bit."""
+    nelem = (9, 3, 4)
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    knots, w, X = ig.beam_mesh(nelem, (4.0, 1.0, 1.0), 2, True)
+    A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_LINGRAD, par=(1.3, 0.8, 0.12), bc_type=bct, neumann=neu)
+    rng = np.random.default_rng(17)
+    A.tangent(rng.uniform(-1e-2, 1e-2, A.ndof))  # the FP64 matrix, kept by the context
+    xs = [rng.standard_normal(A.ndof), rng.standard_normal(A.ndof) * 10.0 ** rng.uniform(-30, 6, A.ndof)]
+    xs[0][::7] = 0.0
+    y64 = [A.matmult(x.copy()) for x in xs]
+    A.set_precision(prec)  # the matrix stays; the multiply changes
+    monkeypatch.setenv("IGAPGPU_SPMV_DF", "1")
+    for x, y in zip(xs, y64):
+        yd = A.matmult(x.copy())
+        e = np.linalg.norm(yd - y) / np.linalg.norm(y)
+        print(f"double-FP32 multiply rel diff {e:.2e}")
+        assert e <= 1e-13
+    monkeypatch.delenv("IGAPGPU_SPMV_DF")
+    for x, y in zip(xs, y64):
+        np.testing.assert_array_equal(A.matmult(x.copy()), y)
