@@ -72,13 +72,20 @@ ALG_BYTES_RES_DF_ELEM = 64 * 244 * 8 + 81 * 8
 # FP64-quality tangent: per element the slices (8 chunks x 22,528 B), the row
 # exponents (88 B) and the read-modify-write of its 6,561 FP64 CSR slots
 ALG_BYTES_OZ_ELEM = 8 * 22528 + 88 + 2 * 8 * 6561
-# DRAM traffic per launch of the FP64 element kernel at 128x32x32, from the
-# one-pass ncu launch list (gpu__time_duration and DRAM bytes, 128x32x32)
-TRAFFIC_FP64_LAUNCH = 1.5063e9
 # cached-operand tensor-core tangent: per element the operands (8 chunks x
 # 11,264 B) and the read-modify-write of its 6,561 FP64 CSR slots
 ALG_BYTES_TCS_ELEM = 8 * 11264 + 2 * 8 * 6561
-TRAFFIC_TCS_LAUNCH = 1.1635e9  # ncu launch list at 128x32x32, per colour launch
+# Measured DRAM traffic per element (dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture of the kernel on a smaller mesh, divided by the elements
+# the launch processed; the bench scales it by the elements per launch): FP64
+# fused kernel (64x16x16, one colour launch of 792 elements: 218.6 MB), TF32x3
+# tangent (64x16x16, 792 elements: 155.2 MB), FP64-quality tangent (48x16x16,
+# 455 elements on 16 CTAs: 170.0 MB), double-FP32 residual (48x16x16, 12,288
+# elements: 2.057 GB)
+TRAFFIC_FP64_ELEM = 218.6e6 / 792
+TRAFFIC_TCS_ELEM = 155.2e6 / 792
+TRAFFIC_OZ_ELEM = 170.0e6 / 455
+TRAFFIC_RES_DF_ELEM = 2.057e9 / 12288
 
 
 def parse():
@@ -100,6 +107,8 @@ def parse():
     ap.add_argument("--transient-steps", type=int, default=40,
                     help="time steps of the transient workload per arm (0 skips it)")
     ap.add_argument("--transient-nelem", default="64,16,16")
+    ap.add_argument("--gradelast-nelem", default="64,16,16",
+                    help="the reference's static law assembled at this size ('0' skips the block)")
     return ap.parse_args()
 
 
@@ -114,6 +123,23 @@ def _cpu_worker(args):
     bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
     prob = po.Problem(nelem=(32, 8, 8), L=LBEAM, law=po.LAW_LINGRAD, par=np.array(LAW_PAR + (0,) * 6),
                       bc_type=bct, neumann=neu)
+    case = po.OracleCase(prob)
+    U = po.random_state(prob, seed)
+    t0 = time.perf_counter()
+    case.residual_elements(U, 0, nel)
+    case.tangent_elements(U, 0, nel)
+    return nel, time.perf_counter() - t0
+
+
+def _cpu_worker_law(args):
+    """Time the oracle port on `nel` elements of a 16x4x4 beam with the
+    reference's static law (gradelast, its default material); returns
+    (elements, seconds)."""
+    nel, seed = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+
+    prob = po.Problem(nelem=(16, 4, 4), law=po.LAW_GRADELAST)
     case = po.OracleCase(prob)
     U = po.random_state(prob, seed)
     t0 = time.perf_counter()
@@ -322,6 +348,66 @@ def bench_batched(ig, torch, dev, n, steps, warmup, flush, peaks):
 
 
 PREDICTOR_FILE = os.path.join(ROOT, "igap4_gb300", "data", "predictor_gradelasttime.npz")
+
+
+def bench_gradelast(ig, torch, nelem, steps, warmup, flush, cpu_seconds, cores):
+    """The reference's own static law (gradelast, default material) assembled
+    at `nelem`: residual + tangent per step in FP64 and in split precision,
+    the split tangent's error against FP64, and the oracle port's rate for
+    the same element kind on the host cores (a bounded sample, spawned
+    processes started before this block's first GPU call)."""
+    # the CPU sample first (spawned workers)
+    n1, t1 = _cpu_worker_law((2, SEED))
+    nel_cpu = max(2, min(int(cpu_seconds / (t1 / n1)), 16 * 4 * 4))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker_law, [(nel_cpu, SEED + i) for i in range(cores)])
+    slowest = max(r[1] for r in res)
+    cpu = {"value": sum(r[0] for r in res) / slowest, "unit": "elements/s", "cores": cores, "kind": "port",
+           "per_core": nel_cpu / statistics.median([r[1] for r in res]),
+           "sample": f"{cores} processes x {nel_cpu} elements (p=2, 64 points, gradelast) of a 16x4x4 beam; "
+                     f"{slowest:.1f} s"}
+    dev = torch.device("cuda")
+    knots, w, X = ig.beam_mesh(nelem, LBEAM)
+    bct, neu = ig.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    A = ig.Assembly(nelem, knots, w, X, law=ig.LAW_GRADELAST, bc_type=bct, neumann=neu)
+    stream = torch.cuda.Stream(device=dev)
+    A.set_stream(stream.cuda_stream)
+    U = torch.tensor(np.random.default_rng(SEED).uniform(-1e-2, 1e-2, A.ndof), device=dev)
+    RR = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+    out = {"workload": f"quadratic beam {nelem[0]}x{nelem[1]}x{nelem[2]} ({A.nelem_total} elements), the "
+                       "reference's static strain-gradient law (gradelast, default material), seeded uniform "
+                       "state in [-1e-2, 1e-2]; one step = residual + tangent",
+           "cpu_port": cpu}
+    K64 = None
+    for name, prec in (("fp64", ig.PREC_FP64), ("split", ig.PREC_SPLIT)):
+        A.set_precision(prec)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                A.assemble(U, RR, None)
+        torch.cuda.synchronize()
+        ms = []
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                flush.fill_(float(k))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                A.assemble(U, RR, None)
+                e1.record(stream)
+                ms.append((e0, e1))
+        torch.cuda.synchronize()
+        step_ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in ms)
+        blk = {"ms_per_step": step_ms, "value": A.nelem_total / (step_ms * 1e-3), "unit": "elements/s",
+               "vs_cpu_port": A.nelem_total / (step_ms * 1e-3) / cpu["value"]}
+        K = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
+        A.tangent(U, K)
+        if K64 is None:
+            K64 = K
+        else:
+            blk["tangent_rel_err_vs_fp64"] = (torch.linalg.norm(K - K64) / torch.linalg.norm(K64)).item()
+        out[name] = blk
+    A.close()
+    return out
 
 
 def bench_transient(ig, torch, nelem, steps, start_steps=200, seed=9001, dt=5e-4):
@@ -548,6 +634,12 @@ def main():
         sampler.start()
         batched = bench_batched(ig, torch, dev, a.batch, a.batch_steps, max(3, a.warmup), flush, peaks)
         sampler.stop()
+    gradelast = None
+    if a.gradelast_nelem != "0" and world == 1:
+        sampler.start()
+        gradelast = bench_gradelast(ig, torch, tuple(int(v) for v in a.gradelast_nelem.split(",")), a.steps,
+                                    max(3, a.warmup), flush, 2.0, os.cpu_count() or 1)
+        sampler.stop()
     transient = None
     if a.transient_steps > 0 and world == 1:
         transient = bench_transient(ig, torch, tuple(int(v) for v in a.transient_nelem.split(",")),
@@ -570,7 +662,7 @@ def main():
                "algorithmic_flop_per_element": alg, "elements_per_launch": kc / max(kl, 1),
                "avg_launch_ms": per_launch_ms,
                "kernel_share_of_step": kms / step_total_ms if step_total_ms > 0 else None,
-               "traffic": (TRAFFIC_FP64_LAUNCH if fused else None) if nelem == NELEM else None}
+               "traffic": (TRAFFIC_FP64_ELEM * kc / max(kl, 1)) if fused else None}
         if fused:
             out["frac_note"] = ("achieved counts the dense R^T D R FLOPs per element; the kernel evaluates the "
                                 "same sum through Gram sums with 5.3x fewer FLOPs, so frac exceeds 1; "
@@ -597,7 +689,7 @@ def main():
                                         "against the FP64 pipe's measured peak",
                 "fp64_peak": fp64_peak,
                 "hbm_algorithmic_bytes_per_element": ALG_BYTES_RES_DF_ELEM, "hbm_achieved_gbs": gbs,
-                "hbm_frac": gbs / hbm_peak, "traffic": None,
+                "hbm_frac": gbs / hbm_peak, "traffic": TRAFFIC_RES_DF_ELEM * per_launch_el,
                 "avg_launch_ms": per_launch_ms, "elements_per_launch": per_launch_el,
                 "kernel_share_of_step": kms / step_total_ms if step_total_ms > 0 else None}
 
@@ -607,12 +699,13 @@ def main():
         if name == "split":
             exe, kern = EXEC_FLOP_TC_ELEM, ("tcw_kernel (cached sqrt(w)-weighted Gram operands, warp-specialised "
                                            "copy/split/MMA/scatter; tcgen05.mma kind::tf32, TF32x3)")
-            bytes_el, traffic = ALG_BYTES_TCS_ELEM, (TRAFFIC_TCS_LAUNCH if nelem == NELEM else None)
+            bytes_el, traffic = ALG_BYTES_TCS_ELEM, TRAFFIC_TCS_ELEM * per_launch_el
         else:
             exe, kern = EXEC_FLOP_OZ_ELEM, ("tco_kernel (error-free BF16 slices of the Gram operands, one bulk "
                                            "copy per chunk, 24 tcgen05.mma kind::f16 per chunk into 4 TMEM "
-                                           "accumulators, FP64 recombination and scatter)")
-            bytes_el, traffic = ALG_BYTES_OZ_ELEM, None
+                                           "accumulators; a thread per basis pair recombines its 3x3 block of "
+                                           "G with FP32 error-free sums and adds K at (b,c) and (c,b))")
+            bytes_el, traffic = ALG_BYTES_OZ_ELEM, TRAFFIC_OZ_ELEM * per_launch_el
         gbs = bytes_el * per_launch_el / (per_launch_ms * 1e-3) / 1e9
         ex_ach = exe * per_launch_el / (per_launch_ms * 1e-3) / 1e12
         return {"bound": "hbm", "kernel": kern, "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -688,6 +781,7 @@ def main():
             "cpu_baseline": cpu,
             "modes": blocks,
             "batched": batched,
+            "gradelast": gradelast,
             "transient": transient,
             "clocks": sampler.summary(local),
             "step_ms": step_ms,

@@ -184,7 +184,8 @@ __global__ void conv_tc_weights_kernel(const __nv_bfloat16 *__restrict__ W, __nv
 
 // MODE 0: forward (out BF16, bias, ReLU); MODE 1: data gradient (out FP32).
 // Thread r of the CTA owns row r of every tile (its lattice coordinates are
-// computed once per tile) and loads that row's neighbour (64 B) for every tap.
+// computed once per tile) and loads that row's neighbour (64 B) for every tap,
+// one tap ahead of the one it stores.
 template <int MODE>
 __global__ void __launch_bounds__(CT_THREADS) conv_tc_kernel(const __nv_bfloat16 *__restrict__ in,
                                                              const __nv_bfloat16 *__restrict__ Wk,
@@ -225,6 +226,17 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_kernel(const __nv_bfloat16
     const bool rowv = p < L.P;
     const int iz = (int)(p % L.nz), iy = (int)((p / L.nz) % L.ny), ix = (int)(p / syz);
     const uint4 *src = reinterpret_cast<const uint4 *>(in + ((int64_t)b * L.P + p) * 32);
+    // this row's neighbour for tap t (zero outside the lattice)
+    auto load_tap = [&](int t, uint4 *x) {
+      const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+      const bool v = rowv && (unsigned)(ix + dx) < (unsigned)L.nx && (unsigned)(iy + dy) < (unsigned)L.ny &&
+                     (unsigned)(iz + dz) < (unsigned)L.nz;
+      const int64_t off = ((int64_t)dx * L.ny + dy) * L.nz + dz;  // rows
+#pragma unroll
+      for (int j16 = 0; j16 < 4; j16++) x[j16] = v ? __ldg(src + off * 4 + j16) : make_uint4(0u, 0u, 0u, 0u);
+    };
+    uint4 cur[4];
+    load_tap(0, cur);
     for (int t = 0; t < 27 && ok; t++) {
       const int buf = t & 1;
       const uint32_t used = buf ? use1 : use0;
@@ -232,16 +244,11 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_kernel(const __nv_bfloat16
         ok = false;
         break;
       }
-      const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
-      const bool v = rowv && (unsigned)(ix + dx) < (unsigned)L.nx && (unsigned)(iy + dy) < (unsigned)L.ny &&
-                     (unsigned)(iz + dz) < (unsigned)L.nz;
-      const int64_t off = ((int64_t)dx * L.ny + dy) * L.nz + dz;  // rows
       unsigned char *a = S.A[buf];
 #pragma unroll
-      for (int j16 = 0; j16 < 4; j16++) {
-        const uint4 x = v ? __ldg(src + off * 4 + j16) : make_uint4(0u, 0u, 0u, 0u);
-        *reinterpret_cast<uint4 *>(a + (j16 >> 1) * 4096 + ct_off(tid, (j16 & 1) * 8)) = x;
-      }
+      for (int j16 = 0; j16 < 4; j16++)
+        *reinterpret_cast<uint4 *>(a + (j16 >> 1) * 4096 + ct_off(tid, (j16 & 1) * 8)) = cur[j16];
+      if (t + 1 < 27) load_tap(t + 1, cur);  // in flight across the barrier and the MMA issue
       tc::fence_proxy_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -314,14 +321,24 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_kernel(const __nv_bfloat16
 // the CTA owns point p of each tile: it loads the point's output gradient
 // (64 B) and its neighbours' features (16-byte loads for 32 channels) and
 // writes them transposed (K-major, the points along K).
-template <int CI>
+template <int CI, int CO>
 struct WgradCfg {
   static constexpr int TPG = 128 / CI;
   static constexpr int NG = (27 + TPG - 1) / TPG;
-  static constexpr uint32_t COLS = NG * 32 <= 32 ? 32 : (NG * 32 <= 64 ? 64 : (NG * 32 <= 128 ? 128 : 256));
+  static constexpr int NPAD = CO <= 16 ? 16 : 32;  // N of the MMA (multiple of 16)
+  static constexpr uint32_t COLS = NG * NPAD <= 32 ? 32 : (NG * NPAD <= 64 ? 64 : (NG * NPAD <= 128 ? 128 : 256));
 };
-constexpr int WG_TAP_A = 8 * 16 * 256;  // A of one group: 8 K-steps x 16 row groups x 256 B
-constexpr int WG_Z = 8 * 4 * 256;       // Z: 8 K-steps x 4 row groups x 256 B
+// The transposed operands are written 2 bytes at a time by consecutive points
+// (consecutive K): with the packed layout (LBO 128 B, SBO 256 B, K-steps 4 KB
+// apart) those stores hit four words of four banks, a four-way conflict.  The
+// strides below spread one warp's 32 points over 16 banks (LBO 144 B, SBO
+// 288 B, K-steps 32 B past a multiple of 128 B); they are plain descriptor
+// strides of the K-major no-swizzle layout.
+constexpr int WG_LBO = 144, WG_SBO = 288;
+constexpr int WG_KS_A = 16 * WG_SBO + 32;  // one K-step of A (128 rows)
+constexpr int WG_KS_Z = 4 * WG_SBO + 32;   // one K-step of Z (up to 32 rows)
+constexpr int WG_TAP_A = 8 * WG_KS_A;      // A of one group: 8 K-steps
+constexpr int WG_Z = 8 * WG_KS_Z;
 
 struct WgradSmem {
   unsigned char A[2][WG_TAP_A];
@@ -330,20 +347,33 @@ struct WgradSmem {
   uint32_t taddr;
 };
 
-__device__ __forceinline__ void st_bf16(unsigned char *base, int m, int k, uint32_t bits)
+__device__ __forceinline__ uint32_t wg_off(int m, int k, int ks_bytes)
 {
-  asm volatile("st.shared.b16 [%0], %1;" ::"r"(tc::smem_u32(base + (k >> 4) * 4096 + ct_off(m, k & 15))),
-               "h"((unsigned short)bits)
-               : "memory");
+  return (uint32_t)((k >> 4) * ks_bytes + (m >> 3) * WG_SBO + ((k >> 3) & 1) * WG_LBO + (m & 7) * 16 + (k & 7) * 2);
 }
 
-template <int CI>
+__device__ __forceinline__ void st_bf16(unsigned char *base, uint32_t off, uint32_t bits)
+{
+  asm volatile("st.shared.b16 [%0], %1;" ::"r"(tc::smem_u32(base + off)), "h"((unsigned short)bits) : "memory");
+}
+
+// Weight gradient on the tensor cores: dW[co][t][ci] += sum_p dZ[p][co] X[p + o(t)][ci]
+// as D[(tl, ci)][co] = sum_p A[(tl, ci)][p] Z[co][p] for groups of TPG =
+// 128 / CI taps (4 taps of 32 channels, or 14 taps of the 9 input features
+// per M = 128 rows, row tl * CI + ci), K = the 128 points of a tile, N = the
+// output channels (32, or 3 padded to 16): 8 MMAs (K16) per group and tile,
+// one TMEM accumulator per group for the whole run of the CTA (persistent
+// over tiles); at the end the CTA adds its sums into dW with FP32
+// reductions.  Thread p of the CTA owns point p of each tile: it loads the
+// point's output gradient and its neighbours' features and writes them
+// transposed (K-major, the points along K).
+template <int CI, int CO>
 __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bfloat16 *__restrict__ X,
                                                                    const __nv_bfloat16 *__restrict__ dZh,
                                                                    float *__restrict__ gW, Lattice L, int B,
                                                                    int *err)
 {
-  using C = WgradCfg<CI>;
+  using C = WgradCfg<CI, CO>;
   extern __shared__ __align__(1024) unsigned char wg_raw[];
   WgradSmem &S = *reinterpret_cast<WgradSmem *>(wg_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -355,11 +385,12 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bf
     tc::mbar_init(&S.done[0], 1);
     tc::mbar_init(&S.done[1], 1);
   }
+  for (int co = CO; co < C::NPAD; co++) st_bf16(S.Z, wg_off(co, tid, WG_KS_Z), 0u);  // padding rows of Z
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = S.taddr;
-  const uint32_t idesc = tc::instr_desc(1, 128, 32);
+  const uint32_t idesc = tc::instr_desc(1, 128, C::NPAD);
   const int64_t tiles_per_sample = (L.P + 127) / 128, ntiles = tiles_per_sample * B;
   const int64_t syz = (int64_t)L.ny * L.nz;
   uint32_t use0 = 0, use1 = 0, nuse = 0;
@@ -378,21 +409,20 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bf
         break;
       }
     }
-    {
+    if constexpr (CO == 32) {
       const uint4 *zr = reinterpret_cast<const uint4 *>(dZh + ((int64_t)b * L.P + p) * 32);
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const uint4 z = rowv ? __ldg(zr + j) : make_uint4(0u, 0u, 0u, 0u);
         const uint32_t w4[4] = {z.x, z.y, z.z, z.w};
 #pragma unroll
-        for (int h = 0; h < 8; h++) {
-          const int co = 8 * j + h;
-          const uint32_t bits = (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu;
-          asm volatile("st.shared.b16 [%0], %1;" ::"r"(tc::smem_u32(S.Z + (tid >> 4) * 1024 + ct_off(co, tid & 15))),
-                       "h"((unsigned short)bits)
-                       : "memory");
-        }
+        for (int h = 0; h < 8; h++)
+          st_bf16(S.Z, wg_off(8 * j + h, tid, WG_KS_Z), (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu);
       }
+    } else {
+      const unsigned short *zr = reinterpret_cast<const unsigned short *>(dZh + ((int64_t)b * L.P + p) * CO);
+#pragma unroll
+      for (int co = 0; co < CO; co++) st_bf16(S.Z, wg_off(co, tid, WG_KS_Z), rowv ? __ldg(zr + co) : 0u);
     }
     for (int g = 0; g < C::NG && ok; g++, nuse++) {
       const int buf = nuse & 1;
@@ -415,15 +445,16 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bf
             const uint4 x = v ? __ldg(xr + j) : make_uint4(0u, 0u, 0u, 0u);
             const uint32_t w4[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-            for (int h = 0; h < 8; h++) st_bf16(a, tl * 32 + 8 * j + h, tid, (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+            for (int h = 0; h < 8; h++)
+              st_bf16(a, wg_off(tl * 32 + 8 * j + h, tid, WG_KS_A), (w4[h >> 1] >> (16 * (h & 1))) & 0xffffu);
           }
         } else {
           const unsigned short *xr = reinterpret_cast<const unsigned short *>(X + q * CI);
 #pragma unroll
-          for (int ci = 0; ci < CI; ci++) st_bf16(a, tl * CI + ci, tid, v ? __ldg(xr + ci) : 0u);
+          for (int ci = 0; ci < CI; ci++) st_bf16(a, wg_off(tl * CI + ci, tid, WG_KS_A), v ? __ldg(xr + ci) : 0u);
         }
       }
-      for (int m = C::TPG * CI; m < 128; m++) st_bf16(a, m, tid, 0u);  // rows past the last group member
+      for (int m = C::TPG * CI; m < 128; m++) st_bf16(a, wg_off(m, tid, WG_KS_A), 0u);  // rows past the group
       tc::fence_proxy_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -431,9 +462,9 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bf
         tc::fence_after_sync();
         const uint32_t abase = tc::smem_u32(a), zbase = tc::smem_u32(S.Z);
         for (int ks = 0; ks < 8; ks++) {
-          const uint64_t ad = tc::smem_desc(abase + (uint32_t)ks * 4096u, 128, 256);
-          const uint64_t zd = tc::smem_desc(zbase + (uint32_t)ks * 1024u, 128, 256);
-          tc::mma_bf16(taddr + (uint32_t)(g * 32), ad, zd, idesc, (!first || ks > 0) ? 1u : 0u);
+          const uint64_t ad = tc::smem_desc(abase + (uint32_t)(ks * WG_KS_A), WG_LBO, WG_SBO);
+          const uint64_t zd = tc::smem_desc(zbase + (uint32_t)(ks * WG_KS_Z), WG_LBO, WG_SBO);
+          tc::mma_bf16(taddr + (uint32_t)(g * C::NPAD), ad, zd, idesc, (!first || ks > 0) ? 1u : 0u);
         }
         tc::mma_commit(&S.done[buf]);
       }
@@ -452,12 +483,12 @@ __global__ void __launch_bounds__(CT_THREADS) conv_tc_wgrad_kernel(const __nv_bf
     tc::fence_after_sync();
     const int m = warp * 32 + lane;  // TMEM lane = row (tl, ci)
     for (int g = 0; g < C::NG; g++) {
-      uint32_t r[32];
-      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * 32), r);
+      uint32_t r[32];  // the group's NPAD columns (and the next group's, unused)
+      tc::tmem_ld_32x32b_x32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * C::NPAD), r);
       const int t = g * C::TPG + m / CI, ci = m % CI;
       if (m < C::TPG * CI && t < 27)
 #pragma unroll
-        for (int co = 0; co < 32; co++) atomicAdd(gW + ((int64_t)co * 27 + t) * CI + ci, __uint_as_float(r[co]));
+        for (int co = 0; co < CO; co++) atomicAdd(gW + ((int64_t)co * 27 + t) * CI + ci, __uint_as_float(r[co]));
     }
   }
   if (!ok && tid == 0) {
@@ -600,20 +631,22 @@ int launch_conv_tc(igapgpu_net *n, const __nv_bfloat16 *in, const __nv_bfloat16 
   return IGAPGPU_OK;
 }
 
-// the weight gradient of the layers with 32 output channels (9 or 32 inputs)
+// the weight gradient of every layer (9 or 32 inputs, 32 or 3 outputs)
 bool use_tc_wgrad(const igapgpu_net *n, int l)
 {
   const char *e = getenv("IGAPGPU_NET_TC");
-  return n->storage == 1 && kCout[l] == 32 && (kCin[l] == 32 || kCin[l] == 9) && !(e && e[0] == '0');
+  return n->storage == 1 && (kCout[l] == 32 || kCout[l] == 3) && (kCin[l] == 32 || kCin[l] == 9) &&
+         !(e && e[0] == '0');
 }
 
-template <int CI>
+template <int CI, int CO>
 int launch_wgrad_tc(igapgpu_net *n, const __nv_bfloat16 *X, float *gW, int B)
 {
   static bool attr = false;
   const size_t smem = sizeof(WgradSmem) + 1024;
   if (!attr) {
-    IGAP_CUDA(cudaFuncSetAttribute(conv_tc_wgrad_kernel<CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    IGAP_CUDA(cudaFuncSetAttribute(conv_tc_wgrad_kernel<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr = true;
   }
   int dev = 0, nsm = 0;
@@ -621,7 +654,7 @@ int launch_wgrad_tc(igapgpu_net *n, const __nv_bfloat16 *X, float *gW, int B)
   IGAP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int64_t ntiles = (n->L.P + 127) / 128 * B;
   const int grid = (int)(ntiles < (int64_t)nsm * 2 ? ntiles : (int64_t)nsm * 2);
-  conv_tc_wgrad_kernel<CI><<<grid, CT_THREADS, smem, n->stream>>>(X, n->dZh, gW, n->L, B, n->err);
+  conv_tc_wgrad_kernel<CI, CO><<<grid, CT_THREADS, smem, n->stream>>>(X, n->dZh, gW, n->L, B, n->err);
   count_launch();
   IGAP_CHECK_LAUNCH();
   return IGAPGPU_OK;
@@ -681,8 +714,11 @@ int net_backward_t(igapgpu_net *n, int B)
       count_launch();
     }
     if (tcw) {
-      const int r = kCin[l] == 32 ? launch_wgrad_tc<32>(n, (const __nv_bfloat16 *)n->act[l], n->gW + n->woff[l], B)
-                                  : launch_wgrad_tc<9>(n, (const __nv_bfloat16 *)n->act[l], n->gW + n->woff[l], B);
+      const __nv_bfloat16 *xin = (const __nv_bfloat16 *)n->act[l];
+      float *gw = n->gW + n->woff[l];
+      const int r = kCin[l] == 9   ? launch_wgrad_tc<9, 32>(n, xin, gw, B)
+                    : kCout[l] == 3 ? launch_wgrad_tc<32, 3>(n, xin, gw, B)
+                                    : launch_wgrad_tc<32, 32>(n, xin, gw, B);
       if (r) return r;
       bias_grad_kernel<<<152 * 4, 256, 0, n->stream>>>(dcur, kCout[l], (int64_t)B * L.P, n->gb + n->boff[l]);
       count_launch();
