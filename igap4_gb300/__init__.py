@@ -403,8 +403,9 @@ class Assembly:
         _check(lib().igapgpu_profile(self.h, int(enable)))
 
     def profile_read(self, kind=-1):
-        """(ms, launches, elements) of the timed element kernels; kind 0 = FP64
-        element kernel, 1 = tensor-core tangent kernel, -1 = both."""
+        """(ms, launches, elements) of the timed element kernels; kind 0 = the
+        residual / FP64 element kernel, 1 = tensor-core tangent kernel, 2 = the
+        nonlinear laws' all-points law kernel, -1 = all."""
         ms = ctypes.c_double()
         nl, ne = ctypes.c_int64(), ctypes.c_int64()
         _check(lib().igapgpu_profile_read_kind(self.h, kind, ctypes.byref(ms), ctypes.byref(nl),

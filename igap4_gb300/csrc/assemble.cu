@@ -753,6 +753,12 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
     }
   }
   if (c->pre_state != 1) return IGAPGPU_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
   int rc;
   if (c->law == IGAPGPU_LAW_GRADELAST) {
     rc = (do_res && do_tan) ? run_law_points<1, true, true>(c, L)
@@ -764,6 +770,12 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
                             : run_law_points<2, false, true>(c, L);
   }
   if (rc) return rc;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[2].emplace_back(e0, e1);
+    c->prof_launches[2]++;
+    c->prof_elements[2] += c->nelem_total;
+  }
   L.preR = c->d_preR;
   L.preD = c->d_preD;
   return IGAPGPU_OK;

@@ -201,9 +201,10 @@ struct Context {
   std::vector<int64_t> h_rowptr;  // host CSR offsets (kept for instances of a batch)
   // element-kernel timing (igapgpu_profile)
   bool prof = false;
-  // per kernel kind: 0 = FP64 element kernel, 1 = tensor-core tangent kernel
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[2];
-  int64_t prof_launches[2] = {0, 0}, prof_elements[2] = {0, 0};
+  // per kernel kind: 0 = residual / FP64 element kernel, 1 = tensor-core
+  // tangent kernel, 2 = the nonlinear laws' all-points law kernel
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[3];
+  int64_t prof_launches[3] = {0, 0, 0}, prof_elements[3] = {0, 0, 0};
 
   DevMesh devmesh() const {
     DevMesh m;

@@ -810,7 +810,7 @@ int igapgpu_profile(igapgpu_t c, int enable)
   if (!c) return IGAPGPU_ERR_ARG;
   if (enable) {
     IGAP_CUDA(cudaStreamSynchronize(c->stream));
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 3; k++) {
       for (auto &p : c->prof_ev[k]) {
         cudaEventDestroy(p.first);
         cudaEventDestroy(p.second);
@@ -826,11 +826,11 @@ int igapgpu_profile(igapgpu_t c, int enable)
 int igapgpu_profile_read_kind(igapgpu_t c, int kind, double *elem_ms, int64_t *launches,
                               int64_t *elements)
 {
-  if (!c || kind < -1 || kind > 1) return IGAPGPU_ERR_ARG;
+  if (!c || kind < -1 || kind > 2) return IGAPGPU_ERR_ARG;
   IGAP_CUDA(cudaStreamSynchronize(c->stream));
   double ms = 0.0;
   int64_t nl = 0, ne = 0;
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < 3; k++) {
     if (kind >= 0 && k != kind) continue;
     for (auto &p : c->prof_ev[k]) {
       float t = 0.f;

@@ -149,6 +149,52 @@ def run_transient(A, load: TipLoad, nsteps: int, dt: float, predictor=None, opts
     return (np.array(states) if record_states else None), recs
 
 
+def step_breakdown(A, load, dt, opts, reps=5):
+    """Where one transient step's time goes, after a run_transient call (its
+    last state u_n, the history it left): the residual and the tangent assembly
+    alone (CUDA events; the law kernel, the residual/FP64 element kernel and
+    the tensor-core tangent kernel from the library's profiling), then one
+    step's Newton solve from u_n (Newton and GMRES iterations, wall ms), and
+    the ms per GMRES iteration once the assemblies are taken out."""
+    import torch
+
+    dev = torch.device("cuda")
+    u_n, _, n = run_transient.last
+    U = u_n.clone().to(dev)
+    RR = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+    K = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
+    out = {}
+    for name, fn in (("residual", lambda: A.residual(U, RR)), ("tangent", lambda: A.tangent(U, K))):
+        fn()
+        A.synchronize()
+        A.profile(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        A.synchronize()
+        torch.cuda.synchronize()
+        kinds = {k: A.profile_read(k)[0] / reps for k in (2, 0, 1)}
+        A.profile(False)
+        out[name] = {"ms": e0.elapsed_time(e1) / reps, "law_kernel_ms": kinds[2],
+                     "residual_or_fp64_kernel_ms": kinds[0], "tensor_core_kernel_ms": kinds[1]}
+    # the next step's solve from u_n
+    A.set_neumann(load.table((n + 1) * dt))
+    guess = u_n.clone().to(dev)
+    A.synchronize()
+    t0 = time.perf_counter()
+    st = A.solve(guess, **opts)
+    A.synchronize()
+    solve_ms = 1e3 * (time.perf_counter() - t0)
+    its, kits = st["newton_its"], st["ksp_its_total"]
+    assembly_ms = (its + 1) * (out["residual"]["ms"] + out["tangent"]["ms"])
+    out["solve"] = {"ms": solve_ms, "newton_its": its, "gmres_its": kits, "converged": st["converged"],
+                    "ms_per_gmres_its_excluding_assembly": (solve_ms - assembly_ms) / max(kits, 1),
+                    "note": "the assemblies counted once per Newton iteration plus the initial residual"}
+    return out
+
+
 def main():
     """Config-3 style run: the transient beam under a seeded tip-load history,
     plain Newton from u_n (or a saved predictor), per-step records as JSON.
@@ -171,6 +217,9 @@ def main():
     ap.add_argument("--predictor", default=None, help=".npz written by train_predictor --save")
     ap.add_argument("--states", default=None, help="write the trajectory (FP64 states) to this .npy")
     ap.add_argument("--orth", type=int, default=1, help="GMRES orthogonalisation: 0 MGS, 1 CGS2")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="after the run, time one step's parts on the last state (assembly kernels, "
+                         "Newton and GMRES iterations, ms per GMRES iteration)")
     a = ap.parse_args()
     import sys
     import torch  # noqa: F401
@@ -210,6 +259,8 @@ def main():
            "ms_per_step": float(ms.mean()), "max_fnorm": float(max(r.fnorm for r in recs)),
            "records": [{"t": r.t, "newton": r.newton_its, "ksp": r.ksp_its, "f0": r.fnorm0, "f": r.fnorm,
                         "ms": 1e3 * r.seconds, "pred": r.used_prediction} for r in recs]}
+    if a.breakdown:
+        out["breakdown"] = step_breakdown(A, load, a.dt, opts)
     print(json.dumps(out))
 
 

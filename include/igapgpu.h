@@ -262,8 +262,9 @@ int64_t igapgpu_launch_count(void);
  * elements they processed since the last reset. */
 int igapgpu_profile(igapgpu_t ctx, int enable);
 int igapgpu_profile_read(igapgpu_t ctx, double *elem_ms, int64_t *launches, int64_t *elements);
-/* The same for one kernel kind: 0 = FP64 element kernel (residual and/or
- * FP64 tangent), 1 = tensor-core split-precision tangent kernel. */
+/* The same for one kernel kind: 0 = the residual / FP64 element kernel
+ * (residual and/or FP64 tangent), 1 = the tensor-core tangent kernel, 2 = the
+ * nonlinear laws' all-points law kernel (-1: all kinds). */
 int igapgpu_profile_read_kind(igapgpu_t ctx, int kind, double *elem_ms, int64_t *launches,
                               int64_t *elements);
 
