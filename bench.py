@@ -400,7 +400,9 @@ def bench_gradelast(ig, torch, nelem, steps, warmup, flush, cpu_seconds, cores):
         blk = {"ms_per_step": step_ms, "value": A.nelem_total / (step_ms * 1e-3), "unit": "elements/s",
                "vs_cpu_port": A.nelem_total / (step_ms * 1e-3) / cpu["value"]}
         K = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
-        A.tangent(U, K)
+        torch.cuda.synchronize()
+        A.tangent(U, K)  # on the context's stream: wait for it before torch reads K
+        A.synchronize()
         if K64 is None:
             K64 = K
         else:
@@ -574,10 +576,11 @@ def main():
     A.set_precision(ig.PREC_FP64)
     K64 = torch.zeros(A.nnz, dtype=torch.float64, device=dev)
     R64 = torch.zeros(A.ndof, dtype=torch.float64, device=dev)
+    Kx, Rx = torch.zeros_like(K64), torch.zeros_like(R64)
+    torch.cuda.synchronize()  # the library writes them on the context's stream
     A.tangent(U, K64)
     A.residual(U, R64)
     errs, rerrs = {"fp64": 0.0}, {"fp64": 0.0}
-    Kx, Rx = torch.zeros_like(K64), torch.zeros_like(R64)
     for name in runs:
         if name == "fp64":
             continue
