@@ -629,9 +629,12 @@ struct LawThreadSmem {
   double wt[LT_NT];
   double R[LT_NT / 32][GEO_STRIDE];
   double U[LT_NT / 32][3 * NE];
+  float Uf[LT_NT / 32][3 * NE];  // the element's state in FP32 (float law)
 };
 
-template <int LAWK, bool RES, bool TAN>
+// T: the law's arithmetic (double; float for the tangent of the split mode,
+// whose contraction runs in TF32x3 on the tensor cores).
+template <int LAWK, bool RES, bool TAN, typename T = double>
 __global__ void __launch_bounds__(LT_NT)
     law_thread_kernel(DevMesh m, DevLaw L, const double *__restrict__ Uhist, double *__restrict__ preR,
                       double *__restrict__ preD, int64_t npt_total)
@@ -657,7 +660,9 @@ __global__ void __launch_bounds__(LT_NT)
       for (int i = lane; i < nh * NE; i += 32) {
         const int h = i / NE, r = i % NE, b = r / 3, d = r % 3;
         const int64_t cp = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
-        S.U[warp][i] = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
+        const double u = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
+        if constexpr (sizeof(T) == 4) S.Uf[warp][i] = f64_to_pair(u).x;
+        else S.U[warp][i] = u;
       }
       cur_e = e;
     }
@@ -667,11 +672,24 @@ __global__ void __launch_bounds__(LT_NT)
     if (lane < 30) {
       const int d = lane / NDD, k = lane % NDD;
       double s[3] = {0.0, 0.0, 0.0};
-      for (int h = 0; h < nh; h++) {
-        double acc = 0.0;
+      if constexpr (sizeof(T) == 4) {  // FP32 interpolation (the basis split on the integer pipe)
+        float sf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
-        s[h] = acc;
+        for (int b = 0; b < NB; b++) {
+          const float r = f64_to_pair(S.R[warp][NDD * b + k]).x;
+#pragma unroll
+          for (int h = 0; h < 3; h++)
+            if (h < nh) sf[h] = fmaf(r, S.Uf[warp][h * NE + 3 * b + d], sf[h]);
+        }
+#pragma unroll
+        for (int h = 0; h < 3; h++) s[h] = f32_to_f64(sf[h]);
+      } else {
+        for (int h = 0; h < nh; h++) {
+          double acc = 0.0;
+#pragma unroll
+          for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
+          s[h] = acc;
+        }
       }
       if (!TR) {
         S.sm[lane * LT_NT + t] = s[0];
@@ -690,18 +708,18 @@ __global__ void __launch_bounds__(LT_NT)
   if (p < npt_total) {
     const int64_t e = p / m.npts;
     const int q = (int)(p % m.npts);
-    gradelast_point<TR ? 4 : 1, RES, TAN>(S.sm + tid, S.sd + tid, LT_NT, L.par, S.wt[tid],
+    gradelast_point<TR ? 4 : 1, RES, TAN, T>(S.sm + tid, S.sd + tid, LT_NT, L.par, S.wt[tid],
                                           preR + e * 30 * m.npts + q, preD + e * 900 * m.npts + q, m.npts);
   }
 }
 
-template <int LAWK, bool RES, bool TAN>
+template <int LAWK, bool RES, bool TAN, typename T = double>
 static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
   if (m.geo) {
     const size_t smem = sizeof(LawThreadSmem);
-    auto kern = law_thread_kernel<LAWK, RES, TAN>;
+    auto kern = law_thread_kernel<LAWK, RES, TAN, T>;
     static bool attr_set = false;
     if (!attr_set) {
       IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -759,15 +777,30 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
     IGAP_CUDA(cudaEventCreate(&e1));
     IGAP_CUDA(cudaEventRecord(e0, c->stream));
   }
-  int rc;
+  // split precision: the tangent's law outputs in FP32 arithmetic (they feed
+  // the TF32x3 contraction); the residual's stay FP64.  IGAPGPU_LAW_F32=0
+  // keeps FP64 for both.
+  const char *lf = getenv("IGAPGPU_LAW_F32");
+  const bool tan32 = do_tan && c->prec == IGAPGPU_PREC_SPLIT && c->d_geo && !(lf && lf[0] == '0');
+  int rc = IGAPGPU_OK;
   if (c->law == IGAPGPU_LAW_GRADELAST) {
-    rc = (do_res && do_tan) ? run_law_points<1, true, true>(c, L)
-         : do_res           ? run_law_points<1, true, false>(c, L)
-                            : run_law_points<1, false, true>(c, L);
+    if (tan32) {
+      if (do_res) rc = run_law_points<1, true, false>(c, L);
+      if (!rc) rc = run_law_points<1, false, true, float>(c, L);
+    } else {
+      rc = (do_res && do_tan) ? run_law_points<1, true, true>(c, L)
+           : do_res           ? run_law_points<1, true, false>(c, L)
+                              : run_law_points<1, false, true>(c, L);
+    }
   } else {
-    rc = (do_res && do_tan) ? run_law_points<2, true, true>(c, L)
-         : do_res           ? run_law_points<2, true, false>(c, L)
-                            : run_law_points<2, false, true>(c, L);
+    if (tan32) {
+      if (do_res) rc = run_law_points<2, true, false>(c, L);
+      if (!rc) rc = run_law_points<2, false, true, float>(c, L);
+    } else {
+      rc = (do_res && do_tan) ? run_law_points<2, true, true>(c, L)
+           : do_res           ? run_law_points<2, true, false>(c, L)
+                              : run_law_points<2, false, true>(c, L);
+    }
   }
   if (rc) return rc;
   if (c->prof) {

@@ -25,48 +25,50 @@
 
 namespace igap {
 
-template <int N>
+// Truncated power series (s-jets) c[0] + c[1] s + ... in the scalar type T.
+template <int N, typename T = double>
 struct Jet {
-  double c[N];
+  T c[N];
 };
-template <int N>
-__device__ __forceinline__ Jet<N> jzero()
+template <int N, typename T = double>
+__device__ __forceinline__ Jet<N, T> jzero()
 {
-  Jet<N> r;
+  Jet<N, T> r;
 #pragma unroll
-  for (int i = 0; i < N; i++) r.c[i] = 0.0;
+  for (int i = 0; i < N; i++) r.c[i] = T(0);
   return r;
 }
-template <int N>
-__device__ __forceinline__ Jet<N> jconst(double a)
+template <int N, typename T = double, typename S>
+__device__ __forceinline__ Jet<N, T> jconst(S a)
 {
-  Jet<N> r = jzero<N>();
-  r.c[0] = a;
+  Jet<N, T> r = jzero<N, T>();
+  r.c[0] = T(a);
   return r;
 }
-template <int N>
-__device__ __forceinline__ Jet<N> jadd(const Jet<N> &a, const Jet<N> &b)
+template <int N, typename T>
+__device__ __forceinline__ Jet<N, T> jadd(const Jet<N, T> &a, const Jet<N, T> &b)
 {
-  Jet<N> r;
+  Jet<N, T> r;
 #pragma unroll
   for (int i = 0; i < N; i++) r.c[i] = a.c[i] + b.c[i];
   return r;
 }
-template <int N>
-__device__ __forceinline__ Jet<N> jscale(const Jet<N> &a, double s)
+template <int N, typename T, typename S>
+__device__ __forceinline__ Jet<N, T> jscale(const Jet<N, T> &a, S s)
 {
-  Jet<N> r;
+  Jet<N, T> r;
+  const T st = T(s);
 #pragma unroll
-  for (int i = 0; i < N; i++) r.c[i] = a.c[i] * s;
+  for (int i = 0; i < N; i++) r.c[i] = a.c[i] * st;
   return r;
 }
-template <int N>
-__device__ __forceinline__ Jet<N> jmul(const Jet<N> &a, const Jet<N> &b)
+template <int N, typename T>
+__device__ __forceinline__ Jet<N, T> jmul(const Jet<N, T> &a, const Jet<N, T> &b)
 {
-  Jet<N> r;
+  Jet<N, T> r;
 #pragma unroll
   for (int i = 0; i < N; i++) {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int j = 0; j <= i; j++) s = fma(a.c[j], b.c[i - j], s);
     r.c[i] = s;

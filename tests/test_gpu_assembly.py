@@ -344,7 +344,8 @@ def test_law_at_every_point_identical(law, monkeypatch):
     time); the FP64 assembly agrees to round-off with that step turned off
     (the law evaluated a warp per point inside the colour launches, another
     summation order) and with the oracle, and the split tangent agrees within
-    the split bound."""
+    the split bound (with the step on, the split tangent's law runs in FP32
+    arithmetic, without it the law is FP64)."""
     prob = po.Problem(nelem=(5, 3, 4), law=law, perturb=True)
     U = po.random_state(prob, 21)
     out = {}
@@ -358,7 +359,7 @@ def test_law_at_every_point_identical(law, monkeypatch):
         A.close()
     assert rel(out["1"][0], out["0"][0]) <= 1e-13
     assert rel(out["1"][1], out["0"][1]) <= 1e-13
-    assert rel(out["1"][2], out["0"][2]) <= 1e-6
+    assert rel(out["1"][2], out["0"][2]) <= 1e-5
     orc = po.OracleCase(prob)
     assert rel(out["1"][0], orc.residual(U)) <= 1e-12
     assert rel(out["1"][1], orc.tangent(U)) <= 1e-12
