@@ -708,8 +708,10 @@ __global__ void __launch_bounds__(LT_NT)
   if (p < npt_total) {
     const int64_t e = p / m.npts;
     const int q = (int)(p % m.npts);
+    // the float law writes its tangent outputs as floats into the same buffer
+    T *outd = reinterpret_cast<T *>(preD) + e * 900 * m.npts + q;
     gradelast_point<TR ? 4 : 1, RES, TAN, T>(S.sm + tid, S.sd + tid, LT_NT, L.par, S.wt[tid],
-                                          preR + e * 30 * m.npts + q, preD + e * 900 * m.npts + q, m.npts);
+                                             preR + e * 30 * m.npts + q, outd, m.npts);
   }
 }
 
@@ -810,7 +812,8 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
     c->prof_elements[2] += c->nelem_total;
   }
   L.preR = c->d_preR;
-  L.preD = c->d_preD;
+  L.preD = tan32 ? nullptr : c->d_preD;
+  L.preDf = tan32 ? reinterpret_cast<const float *>(c->d_preD) : nullptr;
   return IGAPGPU_OK;
 }
 

@@ -96,6 +96,9 @@ struct DevLaw {
   // (else null)
   const double *preR;
   const double *preD;
+  // the tangent's outputs in FP32 (split mode: the law in FP32 arithmetic,
+  // stored in the preD buffer), else null
+  const float *preDf;
 };
 
 struct GraphWork;
@@ -241,6 +244,7 @@ struct Context {
     l.sval = d_sval;
     l.preR = nullptr;
     l.preD = nullptr;
+    l.preDf = nullptr;
     return l;
   }
 };

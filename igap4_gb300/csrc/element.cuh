@@ -248,8 +248,12 @@ __device__ void point_setup(const ElemData &E, PointScratch &P, LawSmem<LAWK> &L
       const int64_t e = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
       if (RES)
         for (int i = lane; i < 30; i += 32) rr[i] = __ldg(L.preR + (e * 30 + i) * m.npts + q);
-      if (TAN && fill_D)
-        for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preD + (e * 900 + i) * m.npts + q);
+      if (TAN && fill_D) {
+        if (L.preDf)
+          for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preDf + (e * 900 + i) * m.npts + q);
+        else
+          for (int i = lane; i < 900; i += 32) D[i] = (DT)__ldg(L.preD + (e * 900 + i) * m.npts + q);
+      }
       __syncwarp();
       return;
     }

@@ -26,7 +26,8 @@
 //             the transient law the inertia + damping residual term;
 //   sd[slot]  delta = (u - u_{n-1})/2 (transient law only).
 // Outputs: rr[30] and D[900] (row-major, row = test slot) scaled by wt,
-// written to out_r[i * ostride] and out_d[(30 i + j) * ostride].
+// written to out_r[i * ostride] (FP64) and out_d[(30 i + j) * ostride] (in
+// the arithmetic type T).
 #pragma once
 #include "df32.cuh"
 #include "gram_common.cuh"
@@ -62,7 +63,7 @@ __device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
 template <int NJ, bool RES, bool TAN, typename T = double>
 __device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in, const double *__restrict__ sd_in,
                                                 int ld, const double *par, double wt_in,
-                                                double *__restrict__ out_r, double *__restrict__ out_d,
+                                                double *__restrict__ out_r, T *__restrict__ out_d,
                                                 int64_t ostride)
 {
   // FP32: the point's inputs converted once into registers (on the integer
@@ -288,7 +289,7 @@ __device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in
       {
 #pragma unroll
         for (int j = 0; j < 30; j++)
-          out_d[(30 * slot(k, 0) + j) * ostride] = lawpt::to_f64((TR && j == slot(k, 0)) ? wt * mass : T(0));
+          out_d[(30 * slot(k, 0) + j) * ostride] = (TR && j == slot(k, 0)) ? wt * mass : T(0);
       }
       // gradient rows (k, 1 + a)
 #pragma unroll
@@ -328,7 +329,7 @@ __device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in
         for (int mm = 0; mm < 3; mm++) acc[slot(k, 4 + symi(a, mm))] += hg[a][mm];
         const int row = slot(k, 1 + a);
 #pragma unroll
-        for (int j = 0; j < 30; j++) out_d[(30 * row + j) * ostride] = lawpt::to_f64(wt * acc[j]);
+        for (int j = 0; j < 30; j++) out_d[(30 * row + j) * ostride] = wt * acc[j];
       }
       // Hessian rows (k, 4 + s)
 #pragma unroll
@@ -346,7 +347,7 @@ __device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in
         }
         const int row = slot(k, 4 + s);
 #pragma unroll
-        for (int j = 0; j < 30; j++) out_d[(30 * row + j) * ostride] = lawpt::to_f64(wt * acc[j]);
+        for (int j = 0; j < 30; j++) out_d[(30 * row + j) * ostride] = wt * acc[j];
       }
     }
   }

@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "element.cuh"
+#include "df32.cuh"
 #include "tcgen05.cuh"
 
 namespace igap {
@@ -173,7 +174,8 @@ __device__ __forceinline__ bool tc_element(TcSmem &S, LawSmem<LAWK> &LS, const D
     } else {  // FP64 geometry, FP32 tangent integrand
       point_setup<LAWK, false, true, float>(S.E, S.Pt[warp], LS, m, L, ex, ey, ez, warp,
                                             ch * PW + warp, lane, S.R[warp], nullptr, S.Dwf[warp]);
-      for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = (float)S.R[warp][i];
+      // FP32 basis for the TF32 split, converted on the integer pipe
+      for (int i = lane; i < NB * NDD; i += 32) S.Rf[warp][i] = f64_to_pair(S.R[warp][i]).x;
     }
     __syncthreads();
     for (int kg = 0; kg < 2; kg++) {
