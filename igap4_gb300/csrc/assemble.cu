@@ -684,21 +684,11 @@ __global__ void __launch_bounds__(LT_NT)
 #pragma unroll
         for (int h = 0; h < 3; h++) s[h] = f32_to_f64(sf[h]);
       } else {
-        // FP64-accurate interpolation on the FP32 pipe: the basis and the state
-        // as float pairs (integer-pipe split), compensated Dot2 sums, one FP64
-        // add per level to join the pair (FP64 issues at ~1/64 of FP32 here)
-        float ps[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
+        for (int h = 0; h < nh; h++) {
+          double acc = 0.0;
 #pragma unroll
-        for (int b = 0; b < NB; b++) {
-          const float2 r = f64_to_pair(S.R[warp][NDD * b + k]);
-#pragma unroll
-          for (int h = 0; h < 3; h++)
-            if (h < nh) dot2(ps[h], pc[h], r, f64_to_pair(S.U[warp][h * NE + 3 * b + d]));
-        }
-#pragma unroll
-        for (int h = 0; h < 3; h++) {
-          const float2 v = dot2_pair(ps[h], pc[h]);
-          s[h] = f32_to_f64(v.x) + f32_to_f64(v.y);
+          for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
+          s[h] = acc;
         }
       }
       if (!TR) {
