@@ -50,6 +50,10 @@ struct Batch {
   int nsm = 0;
   bool all_geof = false;  // every instance has the FP32 geometry cache
   bool all_gop = false;   // every instance has its cached Gram operands
+  int64_t *d_eoff = nullptr;  // [n+1] element offsets (double-FP32 residual)
+  float2 *d_rel = nullptr;    // [elements][81] element residual pairs
+  int *d_einst = nullptr;     // [elements] instance of each element
+  int rdf_state = -1;         // -1 not decided, 0 off, 1 on
   size_t ctrl_bytes() const { return sizeof(int) * (64 + 2 * (size_t)ninst); }
 };
 
@@ -162,8 +166,50 @@ static int check_err_word(Context *c)
   return IGAPGPU_OK;
 }
 
+// The linear law's residual in the split mode in double-FP32 arithmetic
+// (res_df.cu) when every instance has its FP64 geometry cache and the
+// element-residual buffer fits (IGAPGPU_RES_DF=0 keeps the FP64 kernel).
+// Decided and allocated once, when the split mode is selected (outside any
+// graph capture); the assembly only reads the decision.
+static void batch_res_df_setup(Context *c)
+{
+  Batch *b = c->batch;
+  if (b->rdf_state >= 0) return;
+  b->rdf_state = 0;
+  const char *env = getenv("IGAPGPU_RES_DF");
+  bool ok = !(env && env[0] == '0') && c->law == IGAPGPU_LAW_LINGRAD;
+  for (Context *s : b->subs) ok = ok && s->d_geo != nullptr;
+  if (!ok) return;
+  const int64_t nel = b->elem_off[b->ninst];
+  std::vector<int> einst((size_t)nel);
+  for (int i = 0; i < b->ninst; i++)
+    for (int64_t g = b->elem_off[i]; g < b->elem_off[i + 1]; g++) einst[(size_t)g] = i;
+  if (cudaMalloc(&b->d_eoff, sizeof(int64_t) * (b->ninst + 1)) == cudaSuccess &&
+      cudaMalloc(&b->d_einst, sizeof(int) * (size_t)nel) == cudaSuccess &&
+      cudaMalloc(&b->d_rel, sizeof(float2) * NE * (size_t)nel) == cudaSuccess &&
+      cudaMemcpy(b->d_eoff, b->elem_off.data(), sizeof(int64_t) * (b->ninst + 1), cudaMemcpyHostToDevice) ==
+          cudaSuccess &&
+      cudaMemcpy(b->d_einst, einst.data(), sizeof(int) * (size_t)nel, cudaMemcpyHostToDevice) == cudaSuccess) {
+    b->rdf_state = 1;
+    return;
+  }
+  cudaGetLastError();
+  void *bufs[] = {b->d_eoff, b->d_einst, b->d_rel};
+  for (void *p : bufs)
+    if (p) cudaFree(p);
+  b->d_eoff = nullptr;
+  b->d_einst = nullptr;
+  b->d_rel = nullptr;
+}
+
+static bool batch_res_df(const Context *c)
+{
+  return c->batch->rdf_state == 1 && c->prec == IGAPGPU_PREC_SPLIT;
+}
+
 // The two persistent kernels on the first nitems queue items.
-// which: bit 0 = FP64 element kernel, bit 1 = tensor-core tangent kernel.
+// which: bit 0 = FP64 element kernel (or the residual), bit 1 = tensor-core
+// tangent kernel.
 static int batch_kernels(Context *c, bool do_res, bool do_tan, double *RR, double *vals, int64_t nitems,
                          int which = 3)
 {
@@ -171,6 +217,15 @@ static int batch_kernels(Context *c, bool do_res, bool do_tan, double *RR, doubl
   IGAP_CUDA(cudaMemsetAsync(b->d_ctrl, 0, b->ctrl_bytes(), c->stream));
   IGAP_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
   const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT;
+  // the split mode's residual over every element (nitems: the whole queue)
+  if (do_res && nitems == b->nitems && batch_res_df(c)) {
+    do_res = false;
+    if (which & 1) {
+      int r = launch_res_df_batch(c, b->d_mesh, b->d_law, b->d_eoff, b->d_einst, b->d_off, b->ninst,
+                                  b->elem_off[b->ninst], b->d_rel, RR);
+      if (r) return r;
+    }
+  }
   if ((do_res || fp64_tan) && (which & 1)) {
     int grid = 0;
     int r = fp64_grid(c, do_res, fp64_tan, &grid);
@@ -249,7 +304,7 @@ void batch_release(Context *c)
   if (!b) return;
   for (Context *s : b->subs) context_free(s);
   void *bufs[] = {b->d_mesh, b->d_law, b->d_items, b->d_ctrl, b->d_need, b->d_dir_inst, b->d_nbs, b->d_off,
-                  b->d_norms};
+                  b->d_norms, b->d_eoff, b->d_einst, b->d_rel};
   for (void *p : bufs)
     if (p) cudaFree(p);
   delete b;
@@ -283,6 +338,7 @@ __global__ void __launch_bounds__(256) segment_norm_kernel(const double *__restr
 int batch_prepare_split(Context *c)
 {
   Batch *b = c->batch;
+  batch_res_df_setup(c);
   bool all = true;
   for (Context *s : b->subs) {
     const int r = ensure_gram_operands(s);

@@ -296,6 +296,8 @@ int launch_tc_ozaki(Context *c, double *vals);
 // res_df.cu (linear law residual in double-FP32 arithmetic)
 int ensure_res_pairs(Context *c);
 int launch_res_df(Context *c, double *RR);
+int launch_res_df_batch(Context *c, const DevMesh *meshes, const DevLaw *laws, const int64_t *eoff,
+                        const int *einst, const int64_t *doff, int ninst, int64_t nel, float2 *rel, double *RR);
 // builds d_gop once (linear law, FP64 geometry cache present, memory allows)
 int ensure_gram_operands(Context *c);
 // krylov.cu

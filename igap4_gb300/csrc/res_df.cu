@@ -270,6 +270,200 @@ __global__ void res_gather_kernel(const float2 *__restrict__ rel, int ne0, int n
   }
 }
 
+// ------------------------------------------------------ batched instances
+// One weighted output slot (d, k) of the linear law at a point, in pair
+// arithmetic, in the operation order of lin_law_df.
+__device__ __forceinline__ float2 lin_law_entry(const float2 *ud, int d, int k, float2 wt, const DfLaw &L)
+{
+  if (k < 3) {
+    float2 s = df_mul(L.mu, df_add(ud[9 * d + k], ud[9 * k + d]));
+    if (d == k) s = df_add(s, df_mul(L.lam, df_add(df_add(ud[0], ud[9 + 1]), ud[18 + 2])));
+    return df_mul(wt, s);
+  }
+  const int sl = k - 3;
+  const int i = sl < 3 ? 0 : (sl < 5 ? 1 : 2), m = sl < 3 ? sl : (sl < 5 ? sl - 2 : 2);
+  auto H = [&](int a, int x, int y) { return ud[9 * a + 3 + hs6(x, y)]; };
+  auto Dm = [&](int mm) { return df_add(df_add(H(0, 0, mm), H(1, 1, mm)), H(2, 2, mm)); };
+  float2 t;
+  if (i == m) {
+    t = df_mul(L.mu, df_add(H(d, i, i), H(i, d, i)));
+    if (d == i) t = df_add(t, df_mul(L.lam, Dm(i)));
+  } else {
+    t = df_mul(L.mu, df_add(twice(H(d, i, m)), df_add(H(i, d, m), H(m, d, i))));
+    if (d == i) t = df_add(t, df_mul(L.lam, Dm(m)));
+    if (d == m) t = df_add(t, df_mul(L.lam, Dm(i)));
+  }
+  return df_mul(df_mul(wt, L.l2), t);
+}
+
+__device__ __forceinline__ int find_inst(const int64_t *__restrict__ off, int ninst, int64_t x)
+{
+  int lo = 0, hi = ninst;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// The linear-law residual of every element of a batch (instances with their
+// own meshes and law parameters) in double-FP32 arithmetic.  A CTA per
+// element, a warp per Gauss point (8 points per warp): the point's 243
+// physical derivatives and weight are read from the instance's FP64
+// geometry cache and split into pairs on the integer pipe as they are read
+// (the batch keeps no pair cache: 125 KB per element would not fit beside its
+// other caches); lanes 0..26 interpolate one derivative of u each and
+// evaluate one stress slot each; the projection gives each lane 3 of the 81
+// outputs, accumulated over the warp's points, then over the 8 warps.  Each
+// warp loads the next point's geometry into registers before it works on the
+// current one, so that the DRAM latency hides behind the contractions; the
+// element's instance comes from a per-element table (one load, not a search).
+constexpr int RB_THREADS = 256, RB_WARPS = RB_THREADS / 32, RB_LD = (RP_V + 31) / 32;
+__device__ __forceinline__ int rb_geo_index(int v) { return v < NB * 9 ? NDD * (v / 9) + 1 + v % 9 : NB * NDD; }
+
+__global__ void __launch_bounds__(RB_THREADS, 4) res_df_batch_kernel(const DevMesh *__restrict__ meshes,
+                                                                     const DevLaw *__restrict__ laws,
+                                                                     const int64_t *__restrict__ eoff,
+                                                                     const int *__restrict__ einst,
+                                                                     const double *__restrict__ U,
+                                                                     float2 *__restrict__ rel)
+{
+  __shared__ float2 su[NE];
+  __shared__ float2 sR[RB_WARPS][RP_V];
+  __shared__ float2 sU[RB_WARPS][27], sRR[RB_WARPS][27];
+  __shared__ float2 part[RB_WARPS][NE];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t g = blockIdx.x;
+  const int inst = __ldg(einst + g);
+  const DevMesh &m = meshes[inst];
+  const int ne1 = m.nelem[1], ne2 = m.nelem[2], nb1 = m.nbasis[1], nb2 = m.nbasis[2], npts = m.npts;
+  const int64_t e = g - __ldg(eoff + inst);
+  const double *gel = m.geo + e * npts * GEO_STRIDE;
+  double gv[RB_LD];
+  if (warp < npts) {
+#pragma unroll
+    for (int i = 0; i < RB_LD; i++) {
+      const int v = lane + 32 * i;
+      gv[i] = v < RP_V ? __ldg(gel + (int64_t)warp * GEO_STRIDE + rb_geo_index(v)) : 0.0;
+    }
+  }
+  const int ez = (int)(e % ne2), ey = (int)((e / ne2) % ne1);
+  const int64_t ex = e / ((int64_t)ne1 * ne2);
+  for (int t = tid; t < NE; t += RB_THREADS) {
+    const int b = t / 3, d = t % 3;
+    const int64_t cp = ((ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    su[t] = f64_to_pair(__ldg(U + m.dof_off + 3 * cp + d));
+  }
+  DfLaw L;
+  {
+    const double *par = laws[inst].par;
+    L.lam = split_pair(par[0]);
+    L.mu = split_pair(par[1]);
+    L.l2 = split_pair(par[2] * par[2]);
+  }
+  __syncthreads();
+  float ps[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
+  for (int q = warp; q < npts; q += RB_WARPS) {
+#pragma unroll
+    for (int i = 0; i < RB_LD; i++) {
+      const int v = lane + 32 * i;
+      if (v < RP_V) sR[warp][v] = f64_to_pair(gv[i]);
+    }
+    const int qn = q + RB_WARPS;
+    if (qn < npts) {
+#pragma unroll
+      for (int i = 0; i < RB_LD; i++) {
+        const int v = lane + 32 * i;
+        if (v < RP_V) gv[i] = __ldg(gel + (int64_t)qn * GEO_STRIDE + rb_geo_index(v));
+      }
+    }
+    __syncwarp();
+    if (lane < 27) {  // u_dk, lane = 9d + k
+      const int d = lane / 9, k = lane % 9;
+      float s = 0.f, c = 0.f;
+#pragma unroll 9
+      for (int b = 0; b < NB; b++) dot2(s, c, sR[warp][9 * b + k], su[3 * b + d]);
+      sU[warp][lane] = dot2_pair(s, c);
+    }
+    __syncwarp();
+    if (lane < 27) sRR[warp][lane] = lin_law_entry(sU[warp], lane / 9, lane % 9, sR[warp][NB * 9], L);
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int o = lane + 32 * j;
+      if (o < NE) {
+        const int b = o / 3, d = o % 3;
+#pragma unroll
+        for (int k = 0; k < 9; k++) dot2(ps[j], pc[j], sR[warp][9 * b + k], sRR[warp][9 * d + k]);
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int o = lane + 32 * j;
+    if (o < NE) part[warp][o] = dot2_pair(ps[j], pc[j]);
+  }
+  __syncthreads();
+  for (int t = tid; t < NE; t += RB_THREADS) {
+    float2 v = part[0][t];
+#pragma unroll
+    for (int w = 1; w < RB_WARPS; w++) v = df_add(v, part[w][t]);
+    rel[g * NE + t] = v;
+  }
+}
+
+// RR[dof] += the sum of the element residual pairs of the dof's instance, in
+// a fixed element order.
+__global__ void res_gather_batch_kernel(const float2 *__restrict__ rel, const DevMesh *__restrict__ meshes,
+                                        const int64_t *__restrict__ doff, const int64_t *__restrict__ eoff,
+                                        int ninst, int64_t ndof, double *__restrict__ RR)
+{
+  for (int64_t dof = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; dof < ndof;
+       dof += (int64_t)gridDim.x * blockDim.x) {
+    const int inst = find_inst(doff, ninst, dof);
+    const DevMesh &m = meshes[inst];
+    const int ne0 = m.nelem[0], ne1 = m.nelem[1], ne2 = m.nelem[2], nb1 = m.nbasis[1], nb2 = m.nbasis[2];
+    const int64_t loc = dof - __ldg(doff + inst), cp = loc / 3, e0 = __ldg(eoff + inst);
+    const int d = (int)(loc % 3);
+    const int iz = (int)(cp % nb2), iy = (int)((cp / nb2) % nb1), ix = (int)(cp / ((int64_t)nb1 * nb2));
+    float2 s = make_float2(0.f, 0.f);
+    for (int ex = max(ix - P, 0); ex <= min(ix, ne0 - 1); ex++)
+      for (int ey = max(iy - P, 0); ey <= min(iy, ne1 - 1); ey++)
+        for (int ez = max(iz - P, 0); ez <= min(iz, ne2 - 1); ez++) {
+          const int64_t el = e0 + ((int64_t)ex * ne1 + ey) * ne2 + ez;
+          const int b = (ix - ex) * 9 + (iy - ey) * 3 + (iz - ez);
+          s = df_add(s, __ldg(rel + el * NE + 3 * b + d));
+        }
+    RR[dof] += (double)s.x + (double)s.y;
+  }
+}
+
+int launch_res_df_batch(Context *c, const DevMesh *meshes, const DevLaw *laws, const int64_t *eoff,
+                        const int *einst, const int64_t *doff, int ninst, int64_t nel, float2 *rel, double *RR)
+{
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  res_df_batch_kernel<<<(unsigned)nel, RB_THREADS, 0, c->stream>>>(meshes, laws, eoff, einst, c->d_Uhist, rel);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[0].emplace_back(e0, e1);
+    c->prof_launches[0]++;
+    c->prof_elements[0] += nel;
+  }
+  res_gather_batch_kernel<<<152 * 8, 256, 0, c->stream>>>(rel, meshes, doff, eoff, ninst, c->ndof, RR);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
 static float2 host_pair(double x)
 {
   const float h = (float)x;

@@ -68,9 +68,9 @@ def test_batch_bit_identical_to_single_instances(law, cached, prec, monkeypatch)
     # single instances here (their all-points law launch is compared with this
     # in test_gpu_assembly.py: identical in FP64, within the split bound in split)
     monkeypatch.setenv("IGAPGPU_LAW_PRECOMPUTE", "0")
-    # batches keep the FP64 residual kernel in split mode; so do the single
-    # instances here (their double-FP32 residual is compared with FP64 in
-    # test_gpu_split.py)
+    # the FP64 residual kernel in split mode for both (the double-FP32
+    # residuals are compared with FP64 in test_batch_split_residual_double_fp32
+    # and test_gpu_split.py)
     monkeypatch.setenv("IGAPGPU_RES_DF", "0")
     # linear law, split: Gram operands cached (sqrt(w) folded in) or built in the kernel
     monkeypatch.setenv("IGAPGPU_TC_GRAM_CACHE", cached)
@@ -82,6 +82,30 @@ def test_batch_bit_identical_to_single_instances(law, cached, prec, monkeypatch)
     assert B.ndof == sum(A.ndof for A in As) and B.nnz == sum(A.nnz for A in As)
     assert B.nelem_total == sum(A.nelem_total for A in As)
     compare_to_singles(B, As, batch_state(B, 5))
+
+
+def test_batch_split_residual_double_fp32(monkeypatch):
+    """In split mode the batch evaluates the linear law's residual in
+    double-FP32 arithmetic (one launch over every element of every instance,
+    then a gather per DOF in a fixed element order): within 1e-13 of the FP64
+    element kernel per instance, the same bits on every call, and
+    IGAPGPU_RES_DF=0 gives back the FP64 kernel."""
+    law = ig.LAW_LINGRAD
+    insts = instances(law, seed=21)
+    B = ig.BatchAssembly(insts, law=law)
+    U = batch_state(B, 22)
+    R64 = B.residual(U.copy())
+    B.set_precision(ig.PREC_SPLIT)
+    Rdf = B.residual(U.copy())
+    np.testing.assert_array_equal(B.residual(U.copy()), Rdf)
+    assert not np.array_equal(Rdf, R64)  # the pair path ran
+    for i in range(B.ninst):
+        a, e = B.dof_off[i], B.dof_off[i + 1]
+        assert np.linalg.norm(Rdf[a:e] - R64[a:e]) <= 1e-13 * np.linalg.norm(R64[a:e])
+    monkeypatch.setenv("IGAPGPU_RES_DF", "0")
+    B0 = ig.BatchAssembly(insts, law=law)
+    B0.set_precision(ig.PREC_SPLIT)
+    np.testing.assert_allclose(B0.residual(U.copy()), R64, rtol=0, atol=1e-15 * np.abs(R64).max())
 
 
 def test_every_schedule_gives_the_same_bits():
