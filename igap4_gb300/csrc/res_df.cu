@@ -271,29 +271,59 @@ __global__ void res_gather_kernel(const float2 *__restrict__ rel, int ne0, int n
 }
 
 // ------------------------------------------------------ batched instances
-// One weighted output slot (d, k) of the linear law at a point, in pair
-// arithmetic, in the operation order of lin_law_df.
-__device__ __forceinline__ float2 lin_law_entry(const float2 *ud, int d, int k, float2 wt, const DfLaw &L)
+// The linear law of lin_law_df with one output slot per lane and no divergent
+// branches: slot (d, k), lane 9d + k, is
+//   w_k sc (mu (f u[A] + u[B] + u[C]) + lam (u[E] + u[F]))
+// over the point's derivatives u[0..26] with u[27] = 0, u[28] the divergence
+// and u[29 + m] its derivative m.  First-gradient slot i: A = 9d + i,
+// B = 9i + d, f = 1, E the divergence if d = i.  Hessian slot (i, m):
+// A = H_d(i,m) with f = 2, B = H_i(d,m), C = H_m(d,i), E = D_m if d = i,
+// F = D_i if d = m, weight w l^2; a diagonal slot (i = m) counts every term
+// twice and is halved (sc = 1/2, exact), so that each slot repeats the pair
+// operations of lin_law_df.
+// The slot of a lane packed in an int2: x = A | B << 8 | C << 16 | E << 24,
+// y = F | second << 8 | diagonal << 9.
+__device__ __forceinline__ int2 law_slot(int lane)
 {
-  if (k < 3) {
-    float2 s = df_mul(L.mu, df_add(ud[9 * d + k], ud[9 * k + d]));
-    if (d == k) s = df_add(s, df_mul(L.lam, df_add(df_add(ud[0], ud[9 + 1]), ud[18 + 2])));
-    return df_mul(wt, s);
+  int A = 27, B = 27, C = 27, E = 27, F = 27, second = 0, diag = 0;
+  if (lane < 27) {
+    const int d = lane / 9, k = lane % 9;
+    if (k < 3) {
+      A = 9 * d + k;
+      B = 9 * k + d;
+      if (d == k) E = 28;
+    } else {
+      const int sl = k - 3;
+      const int i = sl < 3 ? 0 : (sl < 5 ? 1 : 2), m = sl < 3 ? sl : (sl < 5 ? sl - 2 : 2);
+      A = 9 * d + 3 + hs6(i, m);
+      B = 9 * i + 3 + hs6(d, m);
+      C = 9 * m + 3 + hs6(d, i);
+      second = 1;
+      diag = i == m;
+      if (d == i) E = 29 + m;
+      if (d == m) F = 29 + i;
+    }
   }
-  const int sl = k - 3;
-  const int i = sl < 3 ? 0 : (sl < 5 ? 1 : 2), m = sl < 3 ? sl : (sl < 5 ? sl - 2 : 2);
-  auto H = [&](int a, int x, int y) { return ud[9 * a + 3 + hs6(x, y)]; };
-  auto Dm = [&](int mm) { return df_add(df_add(H(0, 0, mm), H(1, 1, mm)), H(2, 2, mm)); };
-  float2 t;
-  if (i == m) {
-    t = df_mul(L.mu, df_add(H(d, i, i), H(i, d, i)));
-    if (d == i) t = df_add(t, df_mul(L.lam, Dm(i)));
-  } else {
-    t = df_mul(L.mu, df_add(twice(H(d, i, m)), df_add(H(i, d, m), H(m, d, i))));
-    if (d == i) t = df_add(t, df_mul(L.lam, Dm(m)));
-    if (d == m) t = df_add(t, df_mul(L.lam, Dm(i)));
-  }
-  return df_mul(df_mul(wt, L.l2), t);
+  return make_int2(A | B << 8 | C << 16 | E << 24, F | second << 8 | diag << 9);
+}
+
+__device__ __forceinline__ float2 law_slot_eval(const float2 *u, int2 s, float2 wt, float2 wl2, const DfLaw &L)
+{
+  const bool second = (s.y >> 8) & 1;
+  const float f = second ? 2.f : 1.f, sc = (s.y >> 9) & 1 ? 0.5f : 1.f;
+  const float2 a = u[s.x & 255];
+  const float2 h = df_add(make_float2(f * a.x, f * a.y), df_add(u[(s.x >> 8) & 255], u[(s.x >> 16) & 255]));
+  float2 t = df_add(df_mul(L.mu, h), df_mul(L.lam, df_add(u[(s.x >> 24) & 255], u[s.y & 255])));
+  t = make_float2(sc * t.x, sc * t.y);
+  return df_mul(second ? wl2 : wt, t);
+}
+
+// lanes 28..31: the divergence of u and its three derivatives, as lin_law_df sums them
+__device__ __forceinline__ float2 law_divergence(const float2 *u, int j)
+{
+  if (j == 0) return df_add(df_add(u[0], u[9 + 1]), u[18 + 2]);
+  const int m = j - 1;
+  return df_add(df_add(u[3 + hs6(0, m)], u[9 + 3 + hs6(1, m)]), u[18 + 3 + hs6(2, m)]);
 }
 
 __device__ __forceinline__ int find_inst(const int64_t *__restrict__ off, int ninst, int64_t x)
@@ -331,15 +361,17 @@ __global__ void __launch_bounds__(RB_THREADS, 4) res_df_batch_kernel(const DevMe
 {
   __shared__ float2 su[NE];
   __shared__ float2 sR[RB_WARPS][RP_V];
-  __shared__ float2 sU[RB_WARPS][27], sRR[RB_WARPS][27];
+  __shared__ float2 sU[RB_WARPS][32], sRR[RB_WARPS][27];
   __shared__ float2 part[RB_WARPS][NE];
+  __shared__ DfLaw sL;
+  __shared__ int2 sslot[32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t g = blockIdx.x;
   const int inst = __ldg(einst + g);
   const DevMesh &m = meshes[inst];
   const int ne1 = m.nelem[1], ne2 = m.nelem[2], nb1 = m.nbasis[1], nb2 = m.nbasis[2], npts = m.npts;
-  const int64_t e = g - __ldg(eoff + inst);
-  const double *gel = m.geo + e * npts * GEO_STRIDE;
+  const int e = (int)(g - __ldg(eoff + inst));  // element within its instance
+  const double *gel = m.geo + (int64_t)e * npts * GEO_STRIDE;
   double gv[RB_LD];
   if (warp < npts) {
 #pragma unroll
@@ -348,21 +380,22 @@ __global__ void __launch_bounds__(RB_THREADS, 4) res_df_batch_kernel(const DevMe
       gv[i] = v < RP_V ? __ldg(gel + (int64_t)warp * GEO_STRIDE + rb_geo_index(v)) : 0.0;
     }
   }
-  const int ez = (int)(e % ne2), ey = (int)((e / ne2) % ne1);
-  const int64_t ex = e / ((int64_t)ne1 * ne2);
+  const int ez = e % ne2, ey = (e / ne2) % ne1, ex = e / (ne1 * ne2);
   for (int t = tid; t < NE; t += RB_THREADS) {
     const int b = t / 3, d = t % 3;
-    const int64_t cp = ((ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    const int64_t cp = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
     su[t] = f64_to_pair(__ldg(U + m.dof_off + 3 * cp + d));
   }
-  DfLaw L;
-  {
+  if (tid == 0) {
     const double *par = laws[inst].par;
-    L.lam = split_pair(par[0]);
-    L.mu = split_pair(par[1]);
-    L.l2 = split_pair(par[2] * par[2]);
+    sL.lam = split_pair(par[0]);
+    sL.mu = split_pair(par[1]);
+    sL.l2 = split_pair(par[2] * par[2]);
   }
+  if (lane == 27) sU[warp][27] = make_float2(0.f, 0.f);
+  if (tid < 32) sslot[tid] = law_slot(tid);
   __syncthreads();
+  const DfLaw L = sL;
   float ps[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
   for (int q = warp; q < npts; q += RB_WARPS) {
 #pragma unroll
@@ -387,7 +420,12 @@ __global__ void __launch_bounds__(RB_THREADS, 4) res_df_batch_kernel(const DevMe
       sU[warp][lane] = dot2_pair(s, c);
     }
     __syncwarp();
-    if (lane < 27) sRR[warp][lane] = lin_law_entry(sU[warp], lane / 9, lane % 9, sR[warp][NB * 9], L);
+    if (lane >= 28) sU[warp][lane] = law_divergence(sU[warp], lane - 28);
+    __syncwarp();
+    if (lane < 27) {
+      const float2 wt = sR[warp][NB * 9];
+      sRR[warp][lane] = law_slot_eval(sU[warp], sslot[lane], wt, df_mul(wt, L.l2), L);
+    }
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < 3; j++) {
