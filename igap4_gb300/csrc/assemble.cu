@@ -633,11 +633,13 @@ struct LawThreadSmem {
 };
 
 // T: the law's arithmetic (double; float for the tangent of the split mode,
-// whose contraction runs in TF32x3 on the tensor cores).
-template <int LAWK, bool RES, bool TAN, typename T = double>
+// whose contraction runs in TF32x3 on the tensor cores).  PRE: phase 1 copies
+// the law's inputs from lin (pair interpolation, law_in_df_kernel) instead of
+// interpolating them.
+template <int LAWK, bool RES, bool TAN, typename T = double, bool PRE = false>
 __global__ void __launch_bounds__(LT_NT)
     law_thread_kernel(DevMesh m, DevLaw L, const double *__restrict__ Uhist, double *__restrict__ preR,
-                      double *__restrict__ preD, int64_t npt_total)
+                      double *__restrict__ preD, int64_t npt_total, const double *__restrict__ lin)
 {
   constexpr bool TR = LAWK == 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -652,6 +654,15 @@ __global__ void __launch_bounds__(LT_NT)
     const int t = warp * 32 + j;
     const int64_t p = p0 + t;
     if (p >= npt_total) break;  // uniform over the warp
+    if constexpr (PRE) {
+      const double *src = lin + p * 64;
+      if (lane < 30) {
+        S.sm[lane * LT_NT + t] = __ldg(src + lane);
+        if (TR) S.sd[lane * LT_NT + t] = __ldg(src + 30 + lane);
+      }
+      if (lane == 30) S.wt[t] = __ldg(src + 60);
+      continue;
+    }
     const int64_t e = p / m.npts;
     if (e != cur_e) {
       __syncwarp();
@@ -715,13 +726,13 @@ __global__ void __launch_bounds__(LT_NT)
   }
 }
 
-template <int LAWK, bool RES, bool TAN, typename T = double>
+template <int LAWK, bool RES, bool TAN, typename T = double, bool PRE = false>
 static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
   if (m.geo) {
     const size_t smem = sizeof(LawThreadSmem);
-    auto kern = law_thread_kernel<LAWK, RES, TAN, T>;
+    auto kern = law_thread_kernel<LAWK, RES, TAN, T, PRE>;
     static bool attr_set = false;
     if (!attr_set) {
       IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -729,7 +740,7 @@ static int run_law_points(Context *c, const DevLaw &L)
     }
     const int64_t npt = c->nelem_total * m.npts;
     const int64_t nblk = (npt + LT_NT - 1) / LT_NT;
-    kern<<<(unsigned)nblk, LT_NT, smem, c->stream>>>(m, L, c->d_Uhist, c->d_preR, c->d_preD, npt);
+    kern<<<(unsigned)nblk, LT_NT, smem, c->stream>>>(m, L, c->d_Uhist, c->d_preR, c->d_preD, npt, c->d_lin);
     count_launch();
     IGAP_CHECK_LAUNCH();
     return IGAPGPU_OK;
@@ -751,6 +762,7 @@ static int run_law_points(Context *c, const DevLaw &L)
 
 int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
 {
+  c->law_df = false;
   if (c->law == IGAPGPU_LAW_LINGRAD || (!do_res && !do_tan)) return IGAPGPU_OK;
   if (c->pre_state < 0) {
     // decided once, outside any capture: the buffers are allocated when they
@@ -784,9 +796,18 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
   // keeps FP64 for both.
   const char *lf = getenv("IGAPGPU_LAW_F32");
   const bool tan32 = do_tan && c->prec == IGAPGPU_PREC_SPLIT && c->d_geo && !(lf && lf[0] == '0');
+  // the tensor-core modes' residual (residual alone, or beside the FP32-law
+  // tangent): the law's inputs from pair interpolation, the projection on
+  // pairs afterwards (launch_assembly)
+  c->law_df = do_res && c->prec != IGAPGPU_PREC_FP64 && c->rpc_state == 2 && (tan32 || !do_tan);
   int rc = IGAPGPU_OK;
+  if (c->law_df) rc = launch_law_in_df(c);
+  if (rc) return rc;
   if (c->law == IGAPGPU_LAW_GRADELAST) {
-    if (tan32) {
+    if (c->law_df) {
+      rc = run_law_points<1, true, false, double, true>(c, L);
+      if (!rc && do_tan) rc = run_law_points<1, false, true, float>(c, L);
+    } else if (tan32) {
       if (do_res) rc = run_law_points<1, true, false>(c, L);
       if (!rc) rc = run_law_points<1, false, true, float>(c, L);
     } else {
@@ -795,7 +816,10 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
                               : run_law_points<1, false, true>(c, L);
     }
   } else {
-    if (tan32) {
+    if (c->law_df) {
+      rc = run_law_points<2, true, false, double, true>(c, L);
+      if (!rc && do_tan) rc = run_law_points<2, false, true, float>(c, L);
+    } else if (tan32) {
       if (do_res) rc = run_law_points<2, true, false>(c, L);
       if (!rc) rc = run_law_points<2, false, true, float>(c, L);
     } else {
@@ -954,11 +978,13 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   DevLaw L = c->devlaw();
   rc = launch_law_points(c, do_res, do_tan, L);
   if (rc) return rc;
-  // the residual of the tensor-core modes: double-FP32 kernel when its pair
-  // cache was built (linear law)
-  const bool df_res = do_res && c->prec != IGAPGPU_PREC_FP64 && c->d_rpc;
+  // the residual of the tensor-core modes: double-FP32 kernels when their
+  // buffers were built (the linear law's pair cache; the reference's laws'
+  // law-input buffer, with the law outputs of every point)
+  const bool law_df = do_res && c->law_df && c->pre_state == 1;
+  const bool df_res = do_res && c->prec != IGAPGPU_PREC_FP64 && (c->d_rpc || law_df);
   if (df_res) {
-    rc = launch_res_df(c, RR);
+    rc = law_df ? launch_res_law_df(c, c->d_preR, RR) : launch_res_df(c, RR);
     if (rc) return rc;
   }
   const bool k_res = do_res && !df_res, k_tan = fp64_tan;

@@ -162,7 +162,9 @@ struct Context {
   float2 *d_rpc = nullptr;     // linear law: derivative and weight pairs per point (double-FP32 residual)
   float2 *d_rel = nullptr;     // its per-element residual pairs [element][81]
   float2 *d_upair = nullptr;   // the state as pairs [ndof]
-  int rpc_state = -1;          // -1 not decided, 0 off, 1 on
+  int rpc_state = -1;          // -1 not decided, 0 off, 1 linear law, 2 the reference's laws
+  double *d_lin = nullptr;     // the reference's laws: law inputs of every point [point][64] (double-FP32 residual)
+  bool law_df = false;         // the last law launch took its residual inputs from d_lin
   double *d_preR = nullptr;    // law outputs of every point (nonlinear laws, when it fits)
   double *d_preD = nullptr;
   int pre_state = -1;          // -1 not decided, 0 off, 1 on
@@ -296,6 +298,9 @@ int launch_tc_ozaki(Context *c, double *vals);
 // res_df.cu (linear law residual in double-FP32 arithmetic)
 int ensure_res_pairs(Context *c);
 int launch_res_df(Context *c, double *RR);
+// the reference's laws: law inputs by pair interpolation, projection on pairs
+int launch_law_in_df(Context *c);
+int launch_res_law_df(Context *c, const double *preR, double *RR);
 int launch_res_df_batch(Context *c, const DevMesh *meshes, const DevLaw *laws, const int64_t *eoff,
                         const int *einst, const int64_t *doff, int ninst, int64_t nel, float2 *rel, double *RR);
 // builds d_gop once (linear law, FP64 geometry cache present, memory allows)

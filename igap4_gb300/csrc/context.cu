@@ -182,7 +182,7 @@ static int free_ctx(Context *c)
   void *bufs[] = {c->d_wq, c->d_xq, c->d_w, c->d_X, c->d_Uhist, c->d_RR, c->d_vals,
                   c->d_rowptr, c->d_cols, c->d_Dconst, c->d_Fneu, c->d_dir_rows, c->d_dir_g,
                   c->d_stage_a, c->d_stage_b, c->d_stage_v, c->d_V, c->d_Z, c->d_work,
-                  c->d_diag, c->d_bdiag, c->d_cinv, c->d_asmz, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_gop, c->d_oz, c->d_ozexp, c->d_rpc, c->d_rel, c->d_upair, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
+                  c->d_diag, c->d_bdiag, c->d_cinv, c->d_asmz, c->d_red, c->d_partial, c->d_err, c->d_geo, c->d_geof, c->d_gop, c->d_oz, c->d_ozexp, c->d_rpc, c->d_rel, c->d_upair, c->d_lin, c->d_preR, c->d_preD, c->d_dens, c->d_dsparse, c->d_dval, c->d_sval, c->d_bct, c->d_neu};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int d = 0; d < 3; d++) {

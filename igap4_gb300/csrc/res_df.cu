@@ -29,6 +29,7 @@
 #include "common.cuh"
 #include "element.cuh"
 #include "df32.cuh"
+#include "gram_common.cuh"
 
 namespace igap {
 
@@ -502,6 +503,183 @@ int launch_res_df_batch(Context *c, const DevMesh *meshes, const DevLaw *laws, c
   return IGAPGPU_OK;
 }
 
+// ------------------------------------------------- the reference's laws
+// gradelast / gradelasttime in the tensor-core modes (law outputs of every
+// point precomputed, a thread per point, FP64 law): the two contractions
+// around the law on float pairs.
+//  * law_in_df_kernel: the law's inputs (src/assmcore_iga.c:209-229 and the
+//    transient segment of the law kernel), from nodal combinations of the
+//    history levels formed once per assembly in FP64 and split into pairs:
+//    static m = sum_b R_bk u0; transient, at the derivative slots,
+//    m = sum_b R_bk (u1 + u2) / 2 and delta = sum_b R_bk (u0 - u2) / 2, at the
+//    value slots (inertia and damping) damp/(2 dt) sum_b R_b (u0 - u2) +
+//    rho/dt^2 sum_b R_b ((u0 + u2) - 2 u1).  The differences are taken on the
+//    nodal values in FP64 before the interpolation, so that the second
+//    difference of the inertia term carries no cancellation of interpolated
+//    values.  Output per point p: lin[64 p + slot] (m, 30 slots),
+//    lin[64 p + 30 + slot] (delta), lin[64 p + 60] the weight.
+//  * res_law_df_kernel: R_bd = sum_q sum_k N_bk(q) rr_dk(q) over the 10 slots
+//    (value included) from the law outputs (FP64, [element][slot][point]),
+//    element pairs to rel, res_gather_kernel adds them per DOF.
+// Both read the FP64 geometry cache and split it into pairs as they read it
+// (one CTA per element, a warp per Gauss point, the next point's values
+// loaded before the current point's contractions).
+constexpr int LI_THREADS = 256, LI_WARPS = LI_THREADS / 32, LI_NV = NB * NDD, LI_LD = (LI_NV + 1 + 31) / 32;
+
+__global__ void law_state_pair_kernel(const double *__restrict__ U, int64_t ndof, int transient,
+                                      float2 *__restrict__ up)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
+    const double u0 = U[i];
+    if (!transient) {
+      up[i] = split_pair(u0);
+      continue;
+    }
+    const double u1 = U[ndof + i], u2 = U[2 * ndof + i];
+    up[i] = split_pair(u1 + u2);
+    up[ndof + i] = split_pair(u0 - u2);
+    up[2 * ndof + i] = split_pair((u0 + u2) - 2.0 * u1);
+  }
+}
+
+__device__ __forceinline__ double pair_to_f64(float2 a) { return f32_to_f64(a.x) + f32_to_f64(a.y); }
+
+template <bool TR>
+__global__ void __launch_bounds__(LI_THREADS, 4)
+    law_in_df_kernel(const double *__restrict__ geo, const float2 *__restrict__ up, int64_t ndof, int npts,
+                     int ne1, int ne2, int nb1, int nb2, float2 cdamp, float2 crho, double *__restrict__ lin)
+{
+  __shared__ float2 sc[TR ? 3 : 1][NE];
+  __shared__ float2 sR[LI_WARPS][LI_NV];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t e = blockIdx.x;
+  const double *gel = geo + e * npts * GEO_STRIDE;
+  double gv[LI_LD];
+  if (warp < npts) {
+#pragma unroll
+    for (int i = 0; i < LI_LD; i++) {
+      const int v = lane + 32 * i;
+      gv[i] = v <= LI_NV ? __ldg(gel + (int64_t)warp * GEO_STRIDE + v) : 0.0;
+    }
+  }
+  const int ez = (int)(e % ne2), ey = (int)((e / ne2) % ne1);
+  const int64_t ex = e / ((int64_t)ne1 * ne2);
+  for (int t = tid; t < (TR ? 3 : 1) * NE; t += LI_THREADS) {
+    const int c = t / NE, i = t % NE, b = i / 3, d = i % 3;
+    const int64_t cp = ((ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+    sc[c][i] = __ldg(up + c * ndof + 3 * cp + d);
+  }
+  __syncthreads();
+  for (int q = warp; q < npts; q += LI_WARPS) {
+    double *o = lin + (e * npts + q) * 64;
+#pragma unroll
+    for (int i = 0; i < LI_LD; i++) {
+      const int v = lane + 32 * i;
+      if (v < LI_NV) sR[warp][v] = f64_to_pair(gv[i]);
+      if (v == LI_NV) o[60] = gv[i];  // the point's weight, as cached
+    }
+    const int qn = q + LI_WARPS;
+    if (qn < npts) {
+#pragma unroll
+      for (int i = 0; i < LI_LD; i++) {
+        const int v = lane + 32 * i;
+        if (v <= LI_NV) gv[i] = __ldg(gel + (int64_t)qn * GEO_STRIDE + v);
+      }
+    }
+    __syncwarp();
+    if (lane < 30) {
+      const int d = lane / NDD, k = lane % NDD;
+      // transient: value slots take (u0 - u2, second difference), the others
+      // (u1 + u2, u0 - u2)
+      const float2 *sa = sc[TR && k == 0 ? 1 : 0];
+      const float2 *sb = sc[TR ? (k == 0 ? 2 : 1) : 0];
+      float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+#pragma unroll 9
+      for (int b = 0; b < NB; b++) {
+        const float2 n = sR[warp][NDD * b + k];
+        dot2(s1, c1, n, sa[3 * b + d]);
+        if (TR) dot2(s2, c2, n, sb[3 * b + d]);
+      }
+      const float2 A = dot2_pair(s1, c1);
+      if (!TR) {
+        o[lane] = pair_to_f64(A);
+      } else {
+        const float2 B = dot2_pair(s2, c2);
+        if (k == 0) {
+          o[lane] = pair_to_f64(df_add(df_mul(cdamp, A), df_mul(crho, B)));
+          o[30 + lane] = 0.0;
+        } else {
+          o[lane] = pair_to_f64(make_float2(0.5f * A.x, 0.5f * A.y));
+          o[30 + lane] = pair_to_f64(make_float2(0.5f * B.x, 0.5f * B.y));
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(LI_THREADS, 4)
+    res_law_df_kernel(const double *__restrict__ geo, const double *__restrict__ preR, int npts,
+                      float2 *__restrict__ rel)
+{
+  __shared__ float2 sR[LI_WARPS][LI_NV];
+  __shared__ float2 srr[30 * 64];  // [slot][point]
+  __shared__ float2 part[LI_WARPS][NE];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t e = blockIdx.x;
+  const double *gel = geo + e * npts * GEO_STRIDE;
+  double gv[LI_LD];
+  if (warp < npts) {
+#pragma unroll
+    for (int i = 0; i < LI_LD; i++) {
+      const int v = lane + 32 * i;
+      gv[i] = v < LI_NV ? __ldg(gel + (int64_t)warp * GEO_STRIDE + v) : 0.0;
+    }
+  }
+  const double *rr = preR + e * 30 * npts;
+  for (int t = tid; t < 30 * npts; t += LI_THREADS) srr[t] = f64_to_pair(__ldg(rr + t));
+  __syncthreads();
+  float ps[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
+  for (int q = warp; q < npts; q += LI_WARPS) {
+#pragma unroll
+    for (int i = 0; i < LI_LD; i++) {
+      const int v = lane + 32 * i;
+      if (v < LI_NV) sR[warp][v] = f64_to_pair(gv[i]);
+    }
+    const int qn = q + LI_WARPS;
+    if (qn < npts) {
+#pragma unroll
+      for (int i = 0; i < LI_LD; i++) {
+        const int v = lane + 32 * i;
+        if (v < LI_NV) gv[i] = __ldg(gel + (int64_t)qn * GEO_STRIDE + v);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int o = lane + 32 * j;
+      if (o < NE) {
+        const int b = o / 3, d = o % 3;
+#pragma unroll
+        for (int k = 0; k < NDD; k++) dot2(ps[j], pc[j], sR[warp][NDD * b + k], srr[(NDD * d + k) * npts + q]);
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int o = lane + 32 * j;
+    if (o < NE) part[warp][o] = dot2_pair(ps[j], pc[j]);
+  }
+  __syncthreads();
+  for (int t = tid; t < NE; t += LI_THREADS) {
+    float2 v = part[0][t];
+#pragma unroll
+    for (int w = 1; w < LI_WARPS; w++) v = df_add(v, part[w][t]);
+    rel[e * NE + t] = v;
+  }
+}
+
 static float2 host_pair(double x)
 {
   const float h = (float)x;
@@ -516,9 +694,33 @@ int ensure_res_pairs(Context *c)
   c->rpc_state = 0;
   const char *env = getenv("IGAPGPU_RES_DF");
   if (env && env[0] == '0') return IGAPGPU_OK;
-  if (c->law != IGAPGPU_LAW_LINGRAD || !c->d_geo || c->batch || c->porder != 2) return IGAPGPU_OK;
+  if (!c->d_geo || c->batch || c->porder != 2) return IGAPGPU_OK;
   const int npts = c->nquad * c->nquad * c->nquad;
   if (npts > 64) return IGAPGPU_OK;
+  if (c->law == IGAPGPU_LAW_GRADELAST || (c->law == IGAPGPU_LAW_GRADELASTTIME && c->torder >= 2)) {
+    // the reference's laws: the law-input buffer, the nodal combinations and
+    // the element pairs (the law outputs come from the precomputed-law path)
+    const int ncomb = c->law == IGAPGPU_LAW_GRADELASTTIME ? 3 : 1;
+    const size_t lbytes = (size_t)c->nelem_total * npts * 64 * sizeof(double);
+    const size_t rbytes = (size_t)c->nelem_total * NE * sizeof(float2);
+    const size_t ubytes = (size_t)ncomb * c->ndof * sizeof(float2);
+    size_t freeb = 0, totb = 0;
+    IGAP_CUDA(cudaMemGetInfo(&freeb, &totb));
+    if (lbytes + rbytes + ubytes + ((size_t)4 << 30) > freeb / 2) return IGAPGPU_OK;
+    if (cudaMalloc(&c->d_lin, lbytes) != cudaSuccess || cudaMalloc(&c->d_rel, rbytes) != cudaSuccess ||
+        cudaMalloc(&c->d_upair, ubytes) != cudaSuccess) {
+      cudaGetLastError();
+      if (c->d_lin) cudaFree(c->d_lin);
+      if (c->d_rel) cudaFree(c->d_rel);
+      if (c->d_upair) cudaFree(c->d_upair);
+      c->d_lin = nullptr;
+      c->d_rel = c->d_upair = nullptr;
+      return IGAPGPU_OK;
+    }
+    c->rpc_state = 2;
+    return IGAPGPU_OK;
+  }
+  if (c->law != IGAPGPU_LAW_LINGRAD) return IGAPGPU_OK;
   const size_t bytes = (size_t)c->nelem_total * npts * RP_V * sizeof(float2);
   const size_t rbytes = (size_t)c->nelem_total * NE * sizeof(float2);
   const size_t ubytes = (size_t)c->ndof * sizeof(float2);
@@ -572,6 +774,59 @@ int launch_res_df(Context *c, double *RR)
     c->prof_ev[0].emplace_back(e0, e1);
     c->prof_launches[0]++;
     c->prof_elements[0] += ne;
+  }
+  res_gather_kernel<<<152 * 4, 256, 0, c->stream>>>(c->d_rel, c->nelem[0], c->nelem[1], c->nelem[2],
+                                                   c->nbasis[0], c->nbasis[1], c->nbasis[2], RR);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+// The law's inputs at every point from pair interpolation (the reference's
+// laws in the tensor-core modes; before the law kernel).
+int launch_law_in_df(Context *c)
+{
+  const int npts = c->nquad * c->nquad * c->nquad;
+  const bool tr = c->law == IGAPGPU_LAW_GRADELASTTIME;
+  law_state_pair_kernel<<<152 * 4, 256, 0, c->stream>>>(c->d_Uhist, c->ndof, tr ? 1 : 0, c->d_upair);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  const double damp = c->par[6], rho = c->par[5], dt = c->par[7];
+  const float2 cd = tr ? host_pair(damp / (2.0 * dt)) : make_float2(0.f, 0.f);
+  const float2 cr = tr ? host_pair(rho / (dt * dt)) : make_float2(0.f, 0.f);
+  const unsigned grid = (unsigned)c->nelem_total;
+  if (tr)
+    law_in_df_kernel<true><<<grid, LI_THREADS, 0, c->stream>>>(c->d_geo, c->d_upair, c->ndof, npts, c->nelem[1],
+                                                               c->nelem[2], c->nbasis[1], c->nbasis[2], cd, cr,
+                                                               c->d_lin);
+  else
+    law_in_df_kernel<false><<<grid, LI_THREADS, 0, c->stream>>>(c->d_geo, c->d_upair, c->ndof, npts, c->nelem[1],
+                                                                c->nelem[2], c->nbasis[1], c->nbasis[2], cd, cr,
+                                                                c->d_lin);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  return IGAPGPU_OK;
+}
+
+// RR += element residuals of the reference's laws from the precomputed law
+// outputs (projection on pairs, gather per DOF).
+int launch_res_law_df(Context *c, const double *preR, double *RR)
+{
+  const int npts = c->nquad * c->nquad * c->nquad;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->prof) {
+    IGAP_CUDA(cudaEventCreate(&e0));
+    IGAP_CUDA(cudaEventCreate(&e1));
+    IGAP_CUDA(cudaEventRecord(e0, c->stream));
+  }
+  res_law_df_kernel<<<(unsigned)c->nelem_total, LI_THREADS, 0, c->stream>>>(c->d_geo, preR, npts, c->d_rel);
+  count_launch();
+  IGAP_CHECK_LAUNCH();
+  if (c->prof) {
+    IGAP_CUDA(cudaEventRecord(e1, c->stream));
+    c->prof_ev[0].emplace_back(e0, e1);
+    c->prof_launches[0]++;
+    c->prof_elements[0] += c->nelem_total;
   }
   res_gather_kernel<<<152 * 4, 256, 0, c->stream>>>(c->d_rel, c->nelem[0], c->nelem[1], c->nelem[2],
                                                    c->nbasis[0], c->nbasis[1], c->nbasis[2], RR);

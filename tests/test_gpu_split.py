@@ -6,10 +6,11 @@
   FP32 tensor-memory accumulation dominates), for all three laws and every GEMM form
   of the linear law (Gram form from cached sqrt(w)-weighted operands, Gram form built
   from the FP32 geometry cache, and the two-stage form used by the other laws);
-* the residual of the split mode is the FP64 residual, unchanged, for the
-  reference's laws; the linear law's residual runs in double-FP32 arithmetic
-  (pairs of floats, compensated dot products) within 1e-12 of the FP64
-  residual (measured ~1e-15) and of the CPU oracle.
+* the residual of the tensor-core modes runs in double-FP32 arithmetic (pairs of
+  floats, compensated dot products): the linear law's whole element loop, and for
+  the reference's laws the interpolation of the law's inputs and the projection
+  around the FP64 law; within 1e-12 of the FP64 residual (measured ~1e-15) and of
+  the CPU oracle.
 """
 import numpy as np
 import pytest
@@ -64,13 +65,11 @@ def test_split_tangent_vs_fp64(law, nelem, perturb, form, monkeypatch):
     e = rel(Ks, K64)
     print(f"split tangent rel err {e:.3e}")
     assert e <= SPLIT_TOL
-    if lin:
-        er = rel(Rs, R64)
-        print(f"double-FP32 residual rel err {er:.3e}")
-        assert er <= DF_TOL
-        np.testing.assert_array_equal(A.residual(), Rs)  # deterministic
-    else:
-        np.testing.assert_array_equal(Rs, R64)
+    er = rel(Rs, R64)
+    print(f"double-FP32 residual rel err {er:.3e}")
+    assert er <= DF_TOL
+    assert not np.array_equal(Rs, R64)  # the pair path ran
+    np.testing.assert_array_equal(A.residual(), Rs)  # deterministic
     # fused assemble in split mode = the residual above + split tangent
     RR = np.zeros(A.ndof)
     V = np.zeros(A.nnz)
@@ -173,6 +172,57 @@ def test_split_and_fp64_vs_cpu_oracle(law, nelem):
     print(f"law {law} {nelem}: FP64 {e64:.2e}, split {es:.2e} vs the CPU oracle")
     assert e64 <= 1e-12
     assert es <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("law", [po.LAW_GRADELAST, po.LAW_GRADELASTTIME])
+@pytest.mark.parametrize("nquad", [4, 3])
+def test_law_df_residual(law, nquad, monkeypatch):
+    """The reference's laws in the tensor-core modes: the law's inputs by pair
+    interpolation (the history differences formed on the nodal values in
+    FP64), the FP64 law at every point, the projection on pairs.  Within
+    1e-12 of the FP64 residual and of the CPU oracle for random history
+    levels and for nearby levels sampled from a motion at the default time
+    step (the inertia term's second difference); the same bits on every call and in the fused
+    assembly; IGAPGPU_RES_DF=0 gives back the FP64 residual bit for bit."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=(5, 3, 4), law=law, perturb=True, bc_type=bct, neumann=neu, nquad=nquad)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L, prob.p, prob.perturb)
+    mk = lambda: ig.Assembly(prob.nelem, knots, w, X, law=law, par=prob.params(), bc_type=bct, neumann=neu,
+                             nquad=nquad)
+    rng = np.random.default_rng(41)
+    states = [po.random_state(prob, 42)]
+    if prob.torder >= 2:  # u_{n-1}, u_n, u sampled from a smooth motion
+        dt = prob.params()[7]
+        base = rng.uniform(-1e-2, 1e-2, prob.ndof)
+        # |u| / (|a| dt^2) ~ 40: the FP64 residual of the comparison keeps ~1e-14
+        v, a = rng.uniform(-1.0, 1.0, prob.ndof), rng.uniform(-1e3, 1e3, prob.ndof)
+        states.append(np.stack([base + 2 * v * dt + a * dt * dt, base + v * dt, base]))
+    A = mk()
+    R64 = []
+    for U in states:
+        A.set_state(U)
+        R64.append(A.residual())
+    orc = po.OracleCase(prob)
+    for prec in (ig.PREC_SPLIT, ig.PREC_OZAKI):
+        A.set_precision(prec)
+        for U, R in zip(states, R64):
+            A.set_state(U)
+            Rd = A.residual()
+            er, eo = rel(Rd, R), rel(Rd, orc.residual(U))
+            print(f"law {law} nquad {nquad} prec {prec}: double-FP32 residual {er:.2e} vs FP64, {eo:.2e} vs oracle")
+            assert er <= DF_TOL and eo <= DF_TOL
+            assert not np.array_equal(Rd, R)  # the pair path ran
+            np.testing.assert_array_equal(A.residual(), Rd)
+            if prec == ig.PREC_SPLIT:
+                RR, V = np.zeros(A.ndof), np.zeros(A.nnz)
+                A.assemble(None, RR, V)
+                np.testing.assert_array_equal(RR, Rd)
+    monkeypatch.setenv("IGAPGPU_RES_DF", "0")
+    B = mk()
+    B.set_precision(ig.PREC_SPLIT)
+    for U, R in zip(states, R64):
+        B.set_state(U)
+        np.testing.assert_array_equal(B.residual(), R)
 
 
 # ---------------------------------------------------------- FP64-quality mode
