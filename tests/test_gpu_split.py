@@ -198,15 +198,18 @@ def test_law_df_residual(law, nquad, monkeypatch):
         v, a = rng.uniform(-1.0, 1.0, prob.ndof), rng.uniform(-1e3, 1e3, prob.ndof)
         states.append(np.stack([base + 2 * v * dt + a * dt * dt, base + v * dt, base]))
     A = mk()
-    R64 = []
+    R64, K64 = [], []
     for U in states:
         A.set_state(U)
         R64.append(A.residual())
+        K64.append(A.tangent())
     orc = po.OracleCase(prob)
     for prec in (ig.PREC_SPLIT, ig.PREC_OZAKI):
         A.set_precision(prec)
-        for U, R in zip(states, R64):
+        for U, R, K in zip(states, R64, K64):
             A.set_state(U)
+            if prec == ig.PREC_SPLIT:  # the FP32 law's tangent, chunks loaded entry-major
+                assert rel(A.tangent(), K) <= SPLIT_TOL
             Rd = A.residual()
             er, eo = rel(Rd, R), rel(Rd, orc.residual(U))
             print(f"law {law} nquad {nquad} prec {prec}: double-FP32 residual {er:.2e} vs FP64, {eo:.2e} vs oracle")
