@@ -138,7 +138,32 @@ __global__ void tc_selftest_kernel(int variant, float *out, int *err)
 // TMEM, epilogue scatter into the CSR values.  `commits` counts the MMA
 // commits of the CTA (mbarrier phase).  Returns false when a bounded wait
 // expired (S.abort set).  COH: the CSR read-modify-write bypasses L1.
-template <int LAWK, bool COH>
+// PRE (law outputs of every point precomputed in FP32, FP64 geometry cache):
+// each warp loads its point's basis and law outputs of the next chunk into
+// registers while the current chunk's stage 1 and MMAs run (the same values
+// as point_setup reads, so the tangent is bit-identical).
+constexpr int PF_R = (NB * NDD + 31) / 32, PF_D = (900 + 31) / 32;
+
+template <int LAWK>
+__device__ __forceinline__ void tc_prefetch(double (&gR)[PF_R], float (&gD)[PF_D], const DevMesh &m,
+                                            const DevLaw &L, int64_t eg, int q, int lane)
+{
+  const bool valid = q < m.npts;
+  const double *g = m.geo + (eg * m.npts + (valid ? q : 0)) * GEO_STRIDE;
+  const float *dsrc = L.preDf + eg * 900 * (int64_t)m.npts + (valid ? q : 0);
+#pragma unroll
+  for (int t = 0; t < PF_R; t++) {
+    const int i = lane + 32 * t;
+    gR[t] = (valid && i < NB * NDD) ? __ldg(g + i) : 0.0;
+  }
+#pragma unroll
+  for (int t = 0; t < PF_D; t++) {
+    const int i = lane + 32 * t;
+    gD[t] = (valid && i < 900) ? __ldg(dsrc + (int64_t)i * m.npts) : 0.f;
+  }
+}
+
+template <int LAWK, bool COH, bool PRE = false>
 __device__ __forceinline__ bool tc_element(TcSmem &S, LawSmem<LAWK> &LS, const DevMesh &m, const DevLaw &L,
                                            int ex, int ey, int ez, bool const_d,
                                            const double *__restrict__ Uhist, double *__restrict__ vals,
@@ -158,9 +183,25 @@ __device__ __forceinline__ bool tc_element(TcSmem &S, LawSmem<LAWK> &LS, const D
   }
   __syncthreads();
   bool first = true;
+  [[maybe_unused]] double gR[PRE ? PF_R : 1];
+  [[maybe_unused]] float gD[PRE ? PF_D : 1];
+  [[maybe_unused]] const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
+  if constexpr (PRE) tc_prefetch<LAWK>(gR, gD, m, L, eg, warp, lane);
   for (int ch = 0; ch < nchunk; ch++) {
     // phase A: 8 points, one warp each
-    if (const_d) {  // FP32 cached basis and weight; the tangent is constant
+    if constexpr (PRE) {
+#pragma unroll
+      for (int t = 0; t < PF_R; t++) {
+        const int i = lane + 32 * t;
+        if (i < NB * NDD) S.Rf[warp][i] = f64_to_pair(gR[t]).x;
+      }
+#pragma unroll
+      for (int t = 0; t < PF_D; t++) {
+        const int i = lane + 32 * t;
+        if (i < 900) S.Dwf[warp][i] = gD[t];
+      }
+      if (ch + 1 < nchunk) tc_prefetch<LAWK>(gR, gD, m, L, eg, (ch + 1) * PW + warp, lane);
+    } else if (const_d) {  // FP32 cached basis and weight; the tangent is constant
       const int q = ch * PW + warp;
       if (q < m.npts) {
         const int64_t eg = ((int64_t)ex * m.nelem[1] + ey) * m.nelem[2] + ez;
@@ -354,7 +395,7 @@ __device__ __forceinline__ void tc_teardown(TcSmem &S, uint32_t taddr, int *err)
 }
 
 // One persistent CTA per SM walks the elements of one colour.
-template <int LAWK>
+template <int LAWK, bool PRE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_tangent_kernel(DevMesh m, DevLaw L, int cx, int cy, int cz, int ncx, int ncy, int ncz,
                       const double *__restrict__ Uhist, double *__restrict__ vals, int *err)
@@ -376,8 +417,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   for (int ei = blockIdx.x; ei < nelem_c; ei += gridDim.x) {
     const int iz = ei % ncz, iy = (ei / ncz) % ncy, ix = ei / (ncz * ncy);
-    if (!tc_element<LAWK, false>(S, LS, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, const_d, Uhist, vals, taddr,
-                                 idesc, a_base, b_base, commits))
+    if (!tc_element<LAWK, false, PRE>(S, LS, m, L, cx + 3 * ix, cy + 3 * iy, cz + 3 * iz, const_d, Uhist, vals,
+                                      taddr, idesc, a_base, b_base, commits))
       break;
     tc::fence_before_sync();
     __syncthreads();
@@ -456,11 +497,15 @@ static int run_tc(Context *c, const DevLaw &L, double *vals)
 {
   const DevMesh m = c->devmesh();
   const size_t smem = sizeof(TcSmem) + sizeof(LawSmem<LAWK>) + 1024;
-  auto kern = tc_tangent_kernel<LAWK>;
-  static bool attr = false;
-  if (!attr) {
+  // precomputed FP32 law outputs: the prefetching form (IGAPGPU_TC_PREFETCH=0
+  // keeps the point_setup form)
+  const char *pf = getenv("IGAPGPU_TC_PREFETCH");
+  const bool pre = LAWK != 0 && m.geo && L.preR && L.preDf && !(pf && pf[0] == '0');
+  auto kern = pre ? tc_tangent_kernel<LAWK, LAWK != 0> : tc_tangent_kernel<LAWK, false>;
+  static bool attr[2] = {false, false};
+  if (!attr[pre]) {
     IGAP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
+    attr[pre] = true;
   }
   int dev = 0, nsm = 0;
   IGAP_CUDA(cudaGetDevice(&dev));

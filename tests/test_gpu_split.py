@@ -228,6 +228,25 @@ def test_law_df_residual(law, nquad, monkeypatch):
         np.testing.assert_array_equal(B.residual(), R)
 
 
+@pytest.mark.parametrize("law", [po.LAW_GRADELAST, po.LAW_GRADELASTTIME])
+@pytest.mark.parametrize("nquad", [4, 3])
+def test_prefetching_tangent_bit_identical(law, nquad, monkeypatch):
+    """The reference laws' split tangent with the law outputs precomputed: the
+    form that loads the next chunk's basis and law outputs into registers
+    during the current chunk performs the same arithmetic as the point_setup
+    form (IGAPGPU_TC_PREFETCH=0): the same bits."""
+    bct, neu = po.clamp_bc((0,), 1, (0.0, 0.0, -1e-3))
+    prob = po.Problem(nelem=(5, 3, 4), law=law, perturb=True, bc_type=bct, neumann=neu, nquad=nquad)
+    knots, w, X = ig.beam_mesh(prob.nelem, prob.L, prob.p, prob.perturb)
+    A = ig.Assembly(prob.nelem, knots, w, X, law=law, par=prob.params(), bc_type=bct, neumann=neu, nquad=nquad)
+    A.set_state(po.random_state(prob, 51))
+    A.set_precision(ig.PREC_SPLIT)
+    K1 = A.tangent()
+    monkeypatch.setenv("IGAPGPU_TC_PREFETCH", "0")
+    K0 = A.tangent()
+    np.testing.assert_array_equal(K1, K0)
+
+
 # ---------------------------------------------------------- FP64-quality mode
 OZAKI_TOL = 1e-9
 
