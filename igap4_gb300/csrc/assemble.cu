@@ -792,7 +792,7 @@ int launch_law_points(Context *c, bool do_res, bool do_tan, DevLaw &L)
     IGAP_CUDA(cudaEventRecord(e0, c->stream));
   }
   // split precision: the tangent's law outputs in FP32 arithmetic (they feed
-  // the TF32x3 contraction); the residual's stay FP64.  IGAPGPU_LAW_F32=0
+  // the TF32x3 contraction); the residual's law stays FP64.  IGAPGPU_LAW_F32=0
   // keeps FP64 for both.
   const char *lf = getenv("IGAPGPU_LAW_F32");
   const bool tan32 = do_tan && c->prec == IGAPGPU_PREC_SPLIT && c->d_geo && !(lf && lf[0] == '0');
@@ -968,9 +968,10 @@ int launch_assembly(Context *c, bool do_res, bool do_tan, double *RR, double *va
   if (do_res && do_tan) rc = run_colours<LK, true, true>(c, L, RR, vals);   \
   else if (do_res) rc = run_colours<LK, true, false>(c, L, RR, vals);       \
   else rc = run_colours<LK, false, true>(c, L, RR, vals);
-  // split precision: the residual stays FP64, the tangent goes to the tensor
-  // cores (TF32x3); FP64-quality tensor-core precision: the linear law's
-  // tangent from BF16 slices when they were built, else the FP64 kernel
+  // split precision: the tangent goes to the tensor cores (TF32x3);
+  // FP64-quality tensor-core precision: the linear law's tangent from BF16
+  // slices when they were built, else the FP64 kernel; the residual of both
+  // modes below
   const bool oz_tan = do_tan && c->prec == IGAPGPU_PREC_OZAKI && c->d_oz;
   const bool fp64_tan = do_tan && c->prec != IGAPGPU_PREC_SPLIT && !oz_tan;
   // nonlinear laws: every point's law outputs in one launch, so that the
