@@ -623,13 +623,18 @@ __global__ void __launch_bounds__(PW * 32, 1)
 // the weighted outputs in the point-minor layout [element][entry][point], so
 // that a warp's stores are contiguous.
 constexpr int LT_NT = 128;
+// T: the law's arithmetic.  The FP32 law keeps its inputs as floats (the
+// same values its phase 2 used to convert them to), so that the smaller
+// shared-memory footprint lets more CTAs share an SM.
+template <typename T>
 struct LawThreadSmem {
-  double sm[30 * LT_NT];
-  double sd[30 * LT_NT];
+  static constexpr bool F32 = sizeof(T) == 4;
+  T sm[30 * LT_NT];
+  T sd[30 * LT_NT];
   double wt[LT_NT];
   double R[LT_NT / 32][GEO_STRIDE];
-  double U[LT_NT / 32][3 * NE];
-  float Uf[LT_NT / 32][3 * NE];  // the element's state in FP32 (float law)
+  double U[LT_NT / 32][F32 ? 1 : 3 * NE];
+  float Uf[LT_NT / 32][F32 ? 3 * NE : 1];  // the element's state in FP32 (float law)
 };
 
 // T: the law's arithmetic (double; float for the tangent of the split mode,
@@ -643,7 +648,7 @@ __global__ void __launch_bounds__(LT_NT)
 {
   constexpr bool TR = LAWK == 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LawThreadSmem &S = *reinterpret_cast<LawThreadSmem *>(smem_raw);
+  LawThreadSmem<T> &S = *reinterpret_cast<LawThreadSmem<T> *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t p0 = (int64_t)blockIdx.x * LT_NT;
   const int nh = L.nhist;
@@ -657,8 +662,8 @@ __global__ void __launch_bounds__(LT_NT)
     if constexpr (PRE) {
       const double *src = lin + p * 64;
       if (lane < 30) {
-        S.sm[lane * LT_NT + t] = __ldg(src + lane);
-        if (TR) S.sd[lane * LT_NT + t] = __ldg(src + 30 + lane);
+        S.sm[lane * LT_NT + t] = lawpt::to_t<T>(__ldg(src + lane));
+        if (TR) S.sd[lane * LT_NT + t] = lawpt::to_t<T>(__ldg(src + 30 + lane));
       }
       if (lane == 30) S.wt[t] = __ldg(src + 60);
       continue;
@@ -703,12 +708,17 @@ __global__ void __launch_bounds__(LT_NT)
         }
       }
       if (!TR) {
-        S.sm[lane * LT_NT + t] = s[0];
+        S.sm[lane * LT_NT + t] = lawpt::to_t<T>(s[0]);
       } else if (k == 0) {
-        S.sm[lane * LT_NT + t] = damp * (s[0] - s[2]) / (2.0 * dt) + rho_m * (s[0] + s[2] - 2.0 * s[1]) / (dt * dt);
+        // the value slots' inertia and damping term enters the residual only
+        // (the tangent's value rows are the constant mass): no FP64 divisions
+        // in a tangent-only launch
+        S.sm[lane * LT_NT + t] = RES ? lawpt::to_t<T>(damp * (s[0] - s[2]) / (2.0 * dt) +
+                                                      rho_m * (s[0] + s[2] - 2.0 * s[1]) / (dt * dt))
+                                     : T(0);
       } else {
-        S.sm[lane * LT_NT + t] = 0.5 * (s[1] + s[2]);
-        S.sd[lane * LT_NT + t] = 0.5 * (s[0] - s[2]);
+        S.sm[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[1] + s[2]));
+        S.sd[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[0] - s[2]));
       }
     }
     if (lane == 0) S.wt[t] = S.R[warp][NB * NDD];
@@ -731,7 +741,7 @@ static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
   if (m.geo) {
-    const size_t smem = sizeof(LawThreadSmem);
+    const size_t smem = sizeof(LawThreadSmem<T>);
     auto kern = law_thread_kernel<LAWK, RES, TAN, T, PRE>;
     static bool attr_set = false;
     if (!attr_set) {

@@ -20,10 +20,12 @@
 // Terms of degree >= 3 in s never reach the collapse, so the truncation of the
 // s-jets at degree 3 is the one gradelast_warp makes.
 //
-// Inputs per point (shared memory, column t, leading dimension ld):
+// Inputs per point (shared memory, column t, leading dimension ld; FP64, or
+// floats for the FP32 law):
 //   sm[slot]  m at the gradient and Hessian slots (m = u for the static law,
 //             (u_n + u_{n-1})/2 for the transient one); at the value slots of
-//             the transient law the inertia + damping residual term;
+//             the transient law the inertia + damping residual term (read by
+//             the residual only);
 //   sd[slot]  delta = (u - u_{n-1})/2 (transient law only).
 // Outputs: rr[30] and D[900] (row-major, row = test slot) scaled by wt,
 // written to out_r[i * ostride] (FP64) and out_d[(30 i + j) * ostride] (in
@@ -56,12 +58,18 @@ __device__ __forceinline__ double to_t<double>(double x) { return x; }
 template <>
 __device__ __forceinline__ float to_t<float>(double x) { return f64_to_pair(x).x; }
 __device__ __forceinline__ double to_f64(double x) { return x; }
+// the law's inputs as stored by the caller: FP64, or already in the FP32
+// arithmetic type
+template <typename T>
+__device__ __forceinline__ T in_t(double x) { return to_t<T>(x); }
+template <typename T>
+__device__ __forceinline__ T in_t(float x) { return T(x); }
 __device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
 
 }  // namespace lawpt
 
-template <int NJ, bool RES, bool TAN, typename T = double>
-__device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in, const double *__restrict__ sd_in,
+template <int NJ, bool RES, bool TAN, typename T = double, typename IN = double>
+__device__ __forceinline__ void gradelast_point(const IN *__restrict__ sm_in, const IN *__restrict__ sd_in,
                                                 int ld, const double *par, double wt_in,
                                                 double *__restrict__ out_r, T *__restrict__ out_d,
                                                 int64_t ostride)
@@ -73,8 +81,8 @@ __device__ __forceinline__ void gradelast_point(const double *__restrict__ sm_in
   if constexpr (F32) {
 #pragma unroll
     for (int i = 0; i < 30; i++) {
-      smv[i] = lawpt::to_t<T>(sm_in[i * ld]);
-      sdv[i] = NJ > 1 ? lawpt::to_t<T>(sd_in[i * ld]) : T(0);
+      smv[i] = lawpt::in_t<T>(sm_in[i * ld]);
+      sdv[i] = NJ > 1 ? lawpt::in_t<T>(sd_in[i * ld]) : T(0);
     }
   }
   const T wt = lawpt::to_t<T>(wt_in);
