@@ -624,17 +624,18 @@ __global__ void __launch_bounds__(PW * 32, 1)
 // that a warp's stores are contiguous.
 constexpr int LT_NT = 128;
 // T: the law's arithmetic.  The FP32 law keeps its inputs as floats (the
-// same values its phase 2 used to convert them to), so that the smaller
-// shared-memory footprint lets more CTAs share an SM.
-template <typename T>
+// same values its phase 2 used to convert them to), and a launch that copies
+// its inputs (PRE) needs no basis or state: the smaller shared-memory
+// footprints let more CTAs share an SM.
+template <typename T, bool PRE = false>
 struct LawThreadSmem {
   static constexpr bool F32 = sizeof(T) == 4;
   T sm[30 * LT_NT];
   T sd[30 * LT_NT];
   double wt[LT_NT];
-  double R[LT_NT / 32][GEO_STRIDE];
-  double U[LT_NT / 32][F32 ? 1 : 3 * NE];
-  float Uf[LT_NT / 32][F32 ? 3 * NE : 1];  // the element's state in FP32 (float law)
+  double R[LT_NT / 32][PRE ? 1 : GEO_STRIDE];
+  double U[LT_NT / 32][F32 || PRE ? 1 : 3 * NE];
+  float Uf[LT_NT / 32][F32 && !PRE ? 3 * NE : 1];  // the element's state in FP32 (float law)
 };
 
 // T: the law's arithmetic (double; float for the tangent of the split mode,
@@ -648,7 +649,7 @@ __global__ void __launch_bounds__(LT_NT)
 {
   constexpr bool TR = LAWK == 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LawThreadSmem<T> &S = *reinterpret_cast<LawThreadSmem<T> *>(smem_raw);
+  LawThreadSmem<T, PRE> &S = *reinterpret_cast<LawThreadSmem<T, PRE> *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t p0 = (int64_t)blockIdx.x * LT_NT;
   const int nh = L.nhist;
@@ -666,63 +667,63 @@ __global__ void __launch_bounds__(LT_NT)
         if (TR) S.sd[lane * LT_NT + t] = lawpt::to_t<T>(__ldg(src + 30 + lane));
       }
       if (lane == 30) S.wt[t] = __ldg(src + 60);
-      continue;
-    }
-    const int64_t e = p / m.npts;
-    if (e != cur_e) {
+    } else {
+      const int64_t e = p / m.npts;
+      if (e != cur_e) {
+        __syncwarp();
+        const int ez = (int)(e % m.nelem[2]), ey = (int)((e / m.nelem[2]) % m.nelem[1]),
+                  ex = (int)(e / ((int64_t)m.nelem[1] * m.nelem[2]));
+        for (int i = lane; i < nh * NE; i += 32) {
+          const int h = i / NE, r = i % NE, b = r / 3, d = r % 3;
+          const int64_t cp = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
+          const double u = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
+          if constexpr (sizeof(T) == 4) S.Uf[warp][i] = f64_to_pair(u).x;
+          else S.U[warp][i] = u;
+        }
+        cur_e = e;
+      }
+      const double *g = m.geo + p * GEO_STRIDE;
+      for (int i = lane; i < GEO_STRIDE; i += 32) S.R[warp][i] = __ldg(g + i);
       __syncwarp();
-      const int ez = (int)(e % m.nelem[2]), ey = (int)((e / m.nelem[2]) % m.nelem[1]),
-                ex = (int)(e / ((int64_t)m.nelem[1] * m.nelem[2]));
-      for (int i = lane; i < nh * NE; i += 32) {
-        const int h = i / NE, r = i % NE, b = r / 3, d = r % 3;
-        const int64_t cp = ((int64_t)(ex + b / 9) * nb1 + (ey + (b / 3) % 3)) * nb2 + (ez + b % 3);
-        const double u = __ldg(Uhist + (int64_t)h * m.ndof + m.dof_off + 3 * cp + d);
-        if constexpr (sizeof(T) == 4) S.Uf[warp][i] = f64_to_pair(u).x;
-        else S.U[warp][i] = u;
-      }
-      cur_e = e;
-    }
-    const double *g = m.geo + p * GEO_STRIDE;
-    for (int i = lane; i < GEO_STRIDE; i += 32) S.R[warp][i] = __ldg(g + i);
-    __syncwarp();
-    if (lane < 30) {
-      const int d = lane / NDD, k = lane % NDD;
-      double s[3] = {0.0, 0.0, 0.0};
-      if constexpr (sizeof(T) == 4) {  // FP32 interpolation (the basis split on the integer pipe)
-        float sf[3] = {0.f, 0.f, 0.f};
+      if (lane < 30) {
+        const int d = lane / NDD, k = lane % NDD;
+        double s[3] = {0.0, 0.0, 0.0};
+        if constexpr (sizeof(T) == 4) {  // FP32 interpolation (the basis split on the integer pipe)
+          float sf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int b = 0; b < NB; b++) {
-          const float r = f64_to_pair(S.R[warp][NDD * b + k]).x;
+          for (int b = 0; b < NB; b++) {
+            const float r = f64_to_pair(S.R[warp][NDD * b + k]).x;
 #pragma unroll
-          for (int h = 0; h < 3; h++)
-            if (h < nh) sf[h] = fmaf(r, S.Uf[warp][h * NE + 3 * b + d], sf[h]);
+            for (int h = 0; h < 3; h++)
+              if (h < nh) sf[h] = fmaf(r, S.Uf[warp][h * NE + 3 * b + d], sf[h]);
+          }
+#pragma unroll
+          for (int h = 0; h < 3; h++) s[h] = f32_to_f64(sf[h]);
+        } else {
+          for (int h = 0; h < nh; h++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
+            s[h] = acc;
+          }
         }
-#pragma unroll
-        for (int h = 0; h < 3; h++) s[h] = f32_to_f64(sf[h]);
-      } else {
-        for (int h = 0; h < nh; h++) {
-          double acc = 0.0;
-#pragma unroll
-          for (int b = 0; b < NB; b++) acc += S.R[warp][NDD * b + k] * S.U[warp][h * NE + 3 * b + d];
-          s[h] = acc;
+        if (!TR) {
+          S.sm[lane * LT_NT + t] = lawpt::to_t<T>(s[0]);
+        } else if (k == 0) {
+          // the value slots' inertia and damping term enters the residual only
+          // (the tangent's value rows are the constant mass): no FP64 divisions
+          // in a tangent-only launch
+          S.sm[lane * LT_NT + t] = RES ? lawpt::to_t<T>(damp * (s[0] - s[2]) / (2.0 * dt) +
+                                                        rho_m * (s[0] + s[2] - 2.0 * s[1]) / (dt * dt))
+                                       : T(0);
+        } else {
+          S.sm[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[1] + s[2]));
+          S.sd[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[0] - s[2]));
         }
       }
-      if (!TR) {
-        S.sm[lane * LT_NT + t] = lawpt::to_t<T>(s[0]);
-      } else if (k == 0) {
-        // the value slots' inertia and damping term enters the residual only
-        // (the tangent's value rows are the constant mass): no FP64 divisions
-        // in a tangent-only launch
-        S.sm[lane * LT_NT + t] = RES ? lawpt::to_t<T>(damp * (s[0] - s[2]) / (2.0 * dt) +
-                                                      rho_m * (s[0] + s[2] - 2.0 * s[1]) / (dt * dt))
-                                     : T(0);
-      } else {
-        S.sm[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[1] + s[2]));
-        S.sd[lane * LT_NT + t] = lawpt::to_t<T>(0.5 * (s[0] - s[2]));
-      }
+      if (lane == 0) S.wt[t] = S.R[warp][NB * NDD];
+      __syncwarp();
     }
-    if (lane == 0) S.wt[t] = S.R[warp][NB * NDD];
-    __syncwarp();
   }
   __syncthreads();
   const int64_t p = p0 + tid;
@@ -741,7 +742,7 @@ static int run_law_points(Context *c, const DevLaw &L)
 {
   const DevMesh m = c->devmesh();
   if (m.geo) {
-    const size_t smem = sizeof(LawThreadSmem<T>);
+    const size_t smem = sizeof(LawThreadSmem<T, PRE>);
     auto kern = law_thread_kernel<LAWK, RES, TAN, T, PRE>;
     static bool attr_set = false;
     if (!attr_set) {

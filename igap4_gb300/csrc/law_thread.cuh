@@ -94,7 +94,19 @@ __device__ __forceinline__ void gradelast_point(const IN *__restrict__ sm_in, co
 #define LP_DF(k, a) (TR ? LP_SD(slot(k, 1 + (a))) : T(0))
 #define LP_H(k, s) (LP_SM(slot(k, 4 + (s))))
 #define LP_DH(k, s) (TR ? LP_SD(slot(k, 4 + (s))) : T(0))
-  const T s2 = sqrt(T(2.0)), s3 = sqrt(T(3.0)), s6 = sqrt(T(6.0));
+  // FP64: the correctly rounded square roots as constants (the reciprocals
+  // below then fold at compile time; no FP64 square root or division per
+  // point)
+  T s2, s3, s6;
+  if constexpr (sizeof(T) == 8) {
+    s2 = T(1.4142135623730951);
+    s3 = T(1.7320508075688772);
+    s6 = T(2.449489742783178);
+  } else {
+    s2 = sqrt(T(2.0));
+    s3 = sqrt(T(3.0));
+    s6 = sqrt(T(6.0));
+  }
   const T Lv[3] = {1 / s3, 1 / s3, 1 / s3};
   const T L1[3] = {1 / s2, -1 / s2, T(0.0)};
   const T L2[3] = {1 / s6, 1 / s6, -2 / s6};
@@ -171,17 +183,23 @@ __device__ __forceinline__ void gradelast_point(const IN *__restrict__ sm_in, co
                            jscale(jmul(e2, rho), T(4.0) * C));
   // collapse weights: residual (sum_k t_k/(k+1), and the g1 part sum_k t_k/(k+2));
   // tangent (w0, w1, w2)
-  auto colR0 = [](const Jet<NJ, T> &t) -> T {
-    if constexpr (NJ == 1) return t.c[0];
-    else return t.c[0] + t.c[1] / T(2.0) + t.c[2] / T(3.0) + t.c[3] / T(4.0);
+  // x / 3: FP64 multiplies by the rounded third (the FP64 division is a long
+  // sequence on the FP64 pipe; the collapse sums stay within 1e-16 relative)
+  auto div3 = [](T x) -> T {
+    if constexpr (sizeof(T) == 8) return x * T(1.0 / 3.0);
+    else return x / T(3.0);
   };
-  auto colR1 = [](const Jet<NJ, T> &t) -> T {
+  auto colR0 = [&](const Jet<NJ, T> &t) -> T {
+    if constexpr (NJ == 1) return t.c[0];
+    else return t.c[0] + t.c[1] / T(2.0) + div3(t.c[2]) + t.c[3] / T(4.0);
+  };
+  auto colR1 = [&](const Jet<NJ, T> &t) -> T {
     if constexpr (NJ == 1) return T(0.0);
-    else return t.c[0] / T(2.0) + t.c[1] / T(3.0) + t.c[2] / T(4.0);
+    else return t.c[0] / T(2.0) + div3(t.c[1]) + t.c[2] / T(4.0);
   };
-  auto colT = [](const Jet<NJ, T> &t) -> T {
+  auto colT = [&](const Jet<NJ, T> &t) -> T {
     if constexpr (NJ == 1) return t.c[0];
-    else return T(0.5) * (t.c[0] / T(2.0) + t.c[1] / T(3.0) + t.c[2] / T(4.0));
+    else return T(0.5) * (t.c[0] / T(2.0) + div3(t.c[1]) + t.c[2] / T(4.0));
   };
   // d1 of the normal strains
   Jet<NJ, T> d1n[3];
